@@ -1,0 +1,362 @@
+#!/usr/bin/env python
+"""Benchmark: FP64 direct-sum leapfrog steps on a Plummer sphere, N = 262,144.
+
+Workload (the reference's large direct-sum configuration): seeded Plummer
+sphere truncated at r = 10, softening 0.005, leapfrog (order 2) with
+dt = 1e-4, REB_GRAVITY_BASIC in FP64.  One step = drift + O(N^2) force
+evaluation + kick/drift on the device.  Metric: Gpair-int/s = N (N-1) per step
+/ step time.  The same line reports COMPENSATED and the mixed-precision forms,
+their accuracy against FP64, the roofline of the dominant kernel against the
+FP64 pipe peak measured live on this GPU, and an end-to-end figure through the
+C ABI with host buffers.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Inputs are already resident in HBM for `value`; between timed steps L2 is
+flushed by writing 512 MB of scratch on the stream (the j-data of one step is
+only 8 MB and stays L2-resident within a step by design).
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+N_DEFAULT = 262144
+SOFTENING = 0.005
+DT = 1e-4
+SEED = 11
+FLOPS_PER_PAIR = 20          # 3 sub, 6 for r^2+eps^2, sqrt, 2 mul, div, mul by m, 6 accumulate
+L2_FLUSH_BYTES = 512 << 20
+METRIC = "Gpair-int/s FP64 vs mixed, N=262k; ensemble steps/s; p50/p99 latency"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1])]
+        smax = max([num(r[2]) for r in rows if num(r[2])] or [0])
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.strip().lower() in ("active", "1"):
+                    reasons.add(n)
+        load = [x for x in sm if x > 0.5 * smax] or sm
+        return {"sm_mhz": statistics.median(load) if load else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def oracle_cpu_rate(particles, seconds=10.0, label="sample"):
+    """Oracle (port of the reference's OpenMP BASIC gather, src/gravity.c:215-233)
+    on all host cores: time a bounded block of i-rows against all N j-bodies."""
+    from oracle import oracle as O
+    n = len(particles)
+    s = O.Sim(particles, softening=SOFTENING)
+    rows = 512
+    t0 = time.perf_counter()
+    O.lib().orc_gravity_basic_omp_rows(s.ref, 0, rows)
+    dt = time.perf_counter() - t0
+    rows = int(min(n, max(512, rows * seconds / max(dt, 1e-6))))
+    t0 = time.perf_counter()
+    O.lib().orc_gravity_basic_omp_rows(s.ref, 0, rows)
+    dt = time.perf_counter() - t0
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return rows * (n - 1) / dt / 1e9, cores, f"{rows} of {n} i-rows x {n} j-bodies, FP64 BASIC gather ({dt:.1f} s)"
+
+
+def config_block(n, world):
+    return {"workload": f"Plummer N={n}, softening {SOFTENING}, leapfrog dt={DT}, REB_GRAVITY_BASIC FP64",
+            "N": n, "softening": SOFTENING, "dt": DT, "seed": SEED, "gravity": "basic", "integrator": "leapfrog",
+            "parallelism": f"replicas{world}" if world > 1 else "single-gpu",
+            "l2": "flushed between timed steps (512 MB scratch write)"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    O.build()
+    import numpy as np
+    # Inputs from the reference's own Plummer construction (restated in the oracle harness).
+    p = plummer_oracle(args.n)
+    s = O.Sim(p, softening=SOFTENING)
+    L = O.lib()
+    n = args.n
+    rows = 256
+    t0 = time.perf_counter()
+    L.orc_gravity_basic_omp_rows(s.ref, 0, rows)
+    dt = time.perf_counter() - t0
+    rows = int(min(n, max(256, rows * args.ref_seconds / max(dt, 1e-6))))
+    times = []
+    for k in range(args.warmup + args.steps):
+        r0 = (k * rows) % max(1, n - rows)
+        t0 = time.perf_counter()
+        L.orc_gravity_basic_omp_rows(s.ref, r0, r0 + rows)
+        el = time.perf_counter() - t0
+        if k >= args.warmup:
+            times.append(el)
+    rate = rows * (n - 1) * len(times) / sum(times) / 1e9
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    sample = f"{rows} of {n} i-rows x {n} j-bodies per step (oracle port of the OpenMP BASIC gather, src/gravity.c:215-233)"
+    out = {"metric": METRIC, "value": rate, "unit": "Gpair-int/s", "impl": "reference", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n * (n - 1) / (rate * 1e9),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded Plummer sphere)", "config": config_block(n, 1),
+           "cpu_baseline": {"value": rate, "unit": "Gpair-int/s", "cores": cores, "kind": "port", "sample": sample},
+           "e2e": {"value": rate, "unit": "Gpair-int/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def plummer_oracle(n):
+    """Seeded Plummer sphere for the reference arm without the product library."""
+    import numpy as np
+    from oracle import oracle as O
+    out = np.zeros(n, dtype=O.PARTICLE_DTYPE)
+    O.lib().orc_ic_plummer(SEED, n, 1.0, 1.0, 10.0, out.ctypes.data)
+    return out
+
+
+def run_gb300(args):
+    rank, world, local = dist_env()
+    import numpy as np
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import rebound_gb300 as R
+    L = R.load()
+    n = args.n
+    p = R.ics.plummer(n, seed=SEED)
+
+    def make(gravity):
+        sim = R.Simulation()
+        sim.softening = SOFTENING
+        sim.dt = DT
+        sim.gravity = gravity
+        sim.integrator = "leapfrog"
+        sim.add(p)
+        return sim
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    sim = make("basic")
+    h = sim.handle
+    ms = ctypes.c_double(0.)
+    for _ in range(args.warmup):
+        R._lib.check(L.rgpu_sim_time_steps(h, 1, ctypes.byref(ms)), h)
+    L.rgpu_sim_kernel_timer(h, 1)
+    clocks = Clocks(local)
+    launches0 = L.rgpu_launch_count()
+    barrier()
+    clocks.start()
+    total_ms = 0.0
+    for _ in range(args.steps):
+        R._lib.check(L.rgpu_l2_flush(h, L2_FLUSH_BYTES), h)
+        R._lib.check(L.rgpu_sim_time_steps(h, 1, ctypes.byref(ms)), h)
+        total_ms += ms.value
+    barrier()
+    clk = clocks.stop()
+    launches = L.rgpu_launch_count() - launches0
+    kms, kn = ctypes.c_double(0.), ctypes.c_int64(0)
+    L.rgpu_sim_kernel_time(h, ctypes.byref(kms), ctypes.byref(kn))
+    if dist:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    pairs = n * (n - 1)
+    value = pairs * args.steps * world / (total_ms * 1e-3) / 1e9
+    ms_step = total_ms / args.steps
+    kernel_ms = kms.value / max(1, kn.value)
+
+    # FP64 pipe peak measured live (DFMA lane-ops/s x 2 flops).
+    rate = ctypes.c_double(0.)
+    L.rgpu_probe_rate(0, ctypes.byref(rate))
+    fp64_peak = 2 * rate.value / 1e12
+    L.rgpu_probe_rate(1, ctypes.byref(rate))
+    fp32_peak = 2 * rate.value / 1e12
+    achieved = FLOPS_PER_PAIR * pairs / (kernel_ms * 1e-3) / 1e12
+    traffic = profiled_traffic()
+
+    # Accuracy and speed of the other forms (force evaluation at step 0).
+    forms = {}
+    ref_sim = make("compensated")
+    ref_sim.update_acceleration()
+    a_ref = R.accelerations(ref_sim)
+    del ref_sim
+    for form in ("basic", "compensated", "mixed", "mixed_split"):
+        fs = make(form)
+        fh = fs.handle
+        R._lib.check(L.rgpu_sim_time_steps(fh, 1, ctypes.byref(ms)), fh)       # warm
+        fs.set_particles_array(p)
+        fs.update_acceleration()
+        a = R.accelerations(fs)
+        den = np.linalg.norm(a_ref, axis=1)
+        err = np.linalg.norm(a - a_ref, axis=1) / np.where(den > 0, den, 1)
+        fh = fs.handle
+        L.rgpu_sim_kernel_timer(fh, 1)
+        steps_f = 2
+        tf = 0.0
+        for _ in range(steps_f):
+            L.rgpu_l2_flush(fh, L2_FLUSH_BYTES)
+            R._lib.check(L.rgpu_sim_time_steps(fh, 1, ctypes.byref(ms)), fh)
+            tf += ms.value
+        fk, fkn = ctypes.c_double(0.), ctypes.c_int64(0)
+        L.rgpu_sim_kernel_time(fh, ctypes.byref(fk), ctypes.byref(fkn))
+        forms[form] = {"gpair_per_s": pairs * steps_f / (tf * 1e-3) / 1e9, "ms_per_step": tf / steps_f,
+                       "kernel_ms": fk.value / max(1, fkn.value),
+                       "median_rel_err_vs_compensated": float(np.median(err)),
+                       "max_rel_err_vs_compensated": float(err.max())}
+        del fs
+    forms["mixed_speedup_vs_fp64"] = forms["mixed"]["gpair_per_s"] / forms["basic"]["gpair_per_s"]
+    forms["mixed_split_speedup_vs_fp64"] = forms["mixed_split"]["gpair_per_s"] / forms["basic"]["gpair_per_s"]
+
+    # End to end through the C ABI: pinned host AoS in, step, AoS out.
+    host = torch.empty(n * 112, dtype=torch.uint8, pin_memory=True)
+    hv = host.numpy().view(R.PARTICLE_DTYPE)
+    hv[:] = p
+    e2e_steps = max(2, min(args.steps, 3))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        R._lib.check(L.rgpu_sim_set_particles(h, host.data_ptr(), n, 112), h)
+        R._lib.check(L.rgpu_steps(h, 1), h)
+        R._lib.check(L.rgpu_sim_get_particles(h, host.data_ptr(), n, 112), h)
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": pairs * e2e_steps * world / e2e_s / 1e9, "unit": "Gpair-int/s",
+           "h2d_bytes_per_step": n * 112, "d2h_bytes_per_step": n * 88}
+
+    extra = {}
+    if args.ensemble and rank == 0:
+        try:
+            from rebound_gb300 import ensemble as E
+            extra["ensemble"] = E.bench_summary(quick=args.quick)
+        except Exception as ex:  # reported, not hidden
+            extra["ensemble"] = {"error": repr(ex)}
+    if args.serve and rank == 0:
+        try:
+            from rebound_gb300 import serve as S
+            extra["serving"] = S.bench_summary(quick=args.quick)
+        except Exception as ex:
+            extra["serving"] = {"error": repr(ex)}
+
+    if rank == 0:
+        cpu_val, cores, sample = oracle_cpu_rate(p, seconds=args.cpu_seconds)
+        out = {"metric": METRIC, "value": value, "unit": "Gpair-int/s", "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Plummer sphere)",
+               "config": config_block(n, world),
+               "e2e": e2e, "gpu_launches": int(launches),
+               "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                            "frac": achieved / fp64_peak if fp64_peak else None, "traffic": traffic,
+                            "kernel": "direct_kernel<BASIC> (FP64 pair sum)", "kernel_ms": kernel_ms,
+                            "flops_per_pair": FLOPS_PER_PAIR,
+                            "peak_source": "live DFMA probe on this GPU (rgpu_probe_rate); measured-peaks file has no FP64 figure",
+                            "fp32_peak_tflops": fp32_peak},
+               "forms": forms,
+               "cpu_baseline": {"value": cpu_val, "unit": "Gpair-int/s", "cores": cores, "kind": "port",
+                                "sample": sample},
+               "clocks": clk}
+        out.update(extra)
+        print(json.dumps(out), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if present."""
+    path = os.path.join(REPO, "profiles", "direct_basic_fp64.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--ref-seconds", type=float, default=3.0)
+    ap.add_argument("--no-ensemble", dest="ensemble", action="store_false")
+    ap.add_argument("--no-serve", dest="serve", action="store_false")
+    ap.add_argument("--quick", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

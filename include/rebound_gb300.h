@@ -1,0 +1,186 @@
+/*
+ * rebound_gb300.h -- C ABI of the GB300-native (sm_103a) force-and-step path
+ * for REBOUND 5.0.0.
+ *
+ * Plain C types only: pointers, sizes, doubles.  No CUDA or torch types cross
+ * this boundary.  The library keeps particle state resident in GPU memory
+ * between calls; the host copy is only touched by rgpu_sim_set_particles /
+ * rgpu_sim_get_particles, exactly the points where REBOUND's own core hands
+ * over or reads back `r->particles`.
+ *
+ * Every function returns 0 (RGPU_OK) on success or an RGPU_ERR_* code; the
+ * message for the last failure of a handle is available from
+ * rgpu_sim_last_error().  Nothing here calls exit() or traps the GPU: device
+ * errors (non-finite input, duplicate tree positions, Kepler non-convergence,
+ * output overflow) are written to a device status word that the host reads.
+ *
+ * Each entry point names the reference interface it replaces (file:line in the
+ * REBOUND source tree).
+ */
+#ifndef REBOUND_GB300_H
+#define REBOUND_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define RGPU_OK                 0
+#define RGPU_ERR_ARG            1   /* invalid argument or configuration */
+#define RGPU_ERR_CUDA           2   /* CUDA runtime error (no device, launch failure) */
+#define RGPU_ERR_NOMEM          3   /* device allocation failed */
+#define RGPU_ERR_UNSUPPORTED    4   /* mode combination the reference also rejects */
+#define RGPU_ERR_NONFINITE      5   /* particle with non-finite coordinates (src/tree.c:66-69) */
+#define RGPU_ERR_OUT_OF_BOX     6   /* particle outside the root boxes (src/tree.c:263-268) */
+#define RGPU_ERR_DUPLICATE      7   /* two particles at the same position in the tree (src/tree.c:119-123) */
+#define RGPU_ERR_TREE_DEPTH     8   /* octree deeper than the device key supports */
+#define RGPU_ERR_OVERFLOW       9   /* caller's output buffer too small (count is still reported) */
+#define RGPU_ERR_CAPACITY      10   /* request exceeds a fixed capacity of the entry point */
+
+/* ---- enumerations: values equal REBOUND's enums (src/rebound.h:372-393) -- */
+enum { RGPU_GRAVITY_NONE = 0, RGPU_GRAVITY_BASIC = 1, RGPU_GRAVITY_COMPENSATED = 2,
+       RGPU_GRAVITY_TREE = 3,
+       /* GB300 additions: FP64 displacement, FP32 rsqrt/force, compensated FP32-pair
+        * accumulation (MIXED); the same with the FP64 displacement formed exactly
+        * from a two-float split of each coordinate (MIXED_SPLIT). */
+       RGPU_GRAVITY_MIXED = 64, RGPU_GRAVITY_MIXED_SPLIT = 65 };
+enum { RGPU_COLLISION_NONE = 0, RGPU_COLLISION_DIRECT = 1, RGPU_COLLISION_TREE = 2 };
+enum { RGPU_BOUNDARY_NONE = 0, RGPU_BOUNDARY_OPEN = 1, RGPU_BOUNDARY_PERIODIC = 2, RGPU_BOUNDARY_SHEAR = 3 };
+enum { RGPU_INTEGRATOR_LEAPFROG = 0, RGPU_INTEGRATOR_SEI = 1, RGPU_INTEGRATOR_WHFAST = 2 };
+enum { RGPU_RESOLVE_HALT = 0, RGPU_RESOLVE_HARDSPHERE = 1, RGPU_RESOLVE_NONE = 2 };
+
+/* Hot-path fields of struct reb_simulation (src/rebound.h:238-413). */
+typedef struct rgpu_config {
+    double G;                  /* :240 */
+    double softening;          /* :241 */
+    double dt;                 /* :244 */
+    double t;                  /* current time; advanced by the steppers */
+    double OMEGA, OMEGAZ;      /* :242-243 (SEI, shear boundary); OMEGAZ=-1 means OMEGA */
+    double root_size;          /* :313 */
+    double opening_angle2;     /* :276 */
+    double coefficient_of_restitution;  /* constant epsilon for hardsphere resolve */
+    double minimum_collision_velocity;  /* src/collision.c:624-628 */
+    int64_t N_active;          /* -1: all particles active (SIZE_MAX in REBOUND) */
+    int32_t testparticle_type;
+    int32_t gravity_ignore_terms;       /* 0 none, 1 between 0 and 1, 2 involving 0 */
+    int32_t N_root_x, N_root_y, N_root_z;
+    int32_t N_ghost_x, N_ghost_y, N_ghost_z;
+    int32_t gravity;           /* RGPU_GRAVITY_* */
+    int32_t collision;         /* RGPU_COLLISION_* */
+    int32_t collision_resolve; /* RGPU_RESOLVE_* */
+    int32_t boundary;          /* RGPU_BOUNDARY_* */
+    int32_t integrator;        /* RGPU_INTEGRATOR_* */
+    int32_t whfast_safe_mode;  /* src/integrator_whfast.h: safe_mode, default 1 */
+    uint32_t rand_seed;        /* src/rebound.h:359; drives the pair-list shuffle */
+    int32_t status;            /* REB_STATUS_* value after a step (7 = collision halt) */
+    int64_t collisions_log_n;  /* number of resolved hardsphere collisions */
+} rgpu_config;
+
+/* One overlapping, approaching pair: same layout as struct reb_collision
+ * (src/rebound.h:144-149). gb = ghost-box offset (x,y,z,vx,vy,vz). */
+typedef struct rgpu_collision {
+    size_t p1, p2;
+    double gb[6];
+    size_t ri;                 /* root box of p2 (TREE search) */
+} rgpu_collision;
+
+typedef struct rgpu_sim rgpu_sim;   /* opaque device-resident simulation */
+
+/* rgpu_config with REBOUND's defaults (src/simulation.c:100-120). */
+void rgpu_config_default(rgpu_config* cfg);
+
+/* Create / destroy a device-resident simulation on the current CUDA device.
+ * Replaces the integrator-state create/free callbacks (src/rebound.h:170-179). */
+int  rgpu_sim_create(rgpu_sim** out);
+void rgpu_sim_free(rgpu_sim* sim);
+const char* rgpu_sim_last_error(const rgpu_sim* sim);
+
+/* Set / read the hot-path configuration (t, status, rand_seed and
+ * collisions_log_n are updated by the steppers). */
+int rgpu_sim_configure(rgpu_sim* sim, const rgpu_config* cfg);
+int rgpu_sim_get_config(const rgpu_sim* sim, rgpu_config* cfg);
+
+/* Upload / download particles.  `particles` points at N records of `stride`
+ * bytes whose first 11 doubles are x,y,z,vx,vy,vz,ax,ay,az,m,r -- the layout of
+ * struct reb_particle (src/rebound.h:86-104, stride 112) or a dense 88-byte
+ * record.  get_particles writes only those 11 doubles of each record.
+ * set_particles marks the state modified (r->did_modify_particles,
+ * src/particle.c:75) so WHFast recomputes Jacobi coordinates. */
+int rgpu_sim_set_particles(rgpu_sim* sim, const void* particles, size_t N, size_t stride);
+int rgpu_sim_get_particles(rgpu_sim* sim, void* particles, size_t N, size_t stride);
+size_t rgpu_sim_N(const rgpu_sim* sim);
+
+/* Accelerations for the configured gravity mode.
+ * Replaces reb_simulation_update_acceleration (src/simulation.c:640-689) for
+ * REB_GRAVITY_NONE/BASIC/COMPENSATED/TREE (src/gravity.c:47-531). */
+int rgpu_update_acceleration(rgpu_sim* sim);
+
+/* Overlapping + approaching pairs for the configured collision mode, in the
+ * reference's discovery order, before its random shuffle.  Replaces the search
+ * half of reb_collision_search (src/collision.c:49-342).  *n_found receives the
+ * full count; if it exceeds cap, RGPU_ERR_OVERFLOW is returned. */
+int rgpu_collision_search(rgpu_sim* sim, rgpu_collision* out, size_t cap, size_t* n_found);
+
+/* N_steps full steps: integrator step (leapfrog order 2, SEI, or WHFast
+ * Jacobi/DEFAULT kernel), boundary check, collision search + shuffle + resolve.
+ * Replaces reb_simulation_steps (src/simulation.c:500-512) with the step body
+ * reb_simulation_step (src/simulation.c:514-603). */
+int rgpu_steps(rgpu_sim* sim, int64_t N_steps);
+
+/* Integrate to t = tmax with fixed dt, the last step shortened to land on tmax
+ * (exact_finish_time = 1, src/simulation.c:318-341, 456-460). */
+int rgpu_integrate(rgpu_sim* sim, double tmax);
+
+/* WHFast: bring inertial particles up to date (src/integrator_whfast.c:1051-1111). */
+int rgpu_synchronize(rgpu_sim* sim);
+
+/* Total energy, unsoftened, test-particle aware (src/tools.c:108-162). */
+int rgpu_energy(rgpu_sim* sim, double* energy);
+
+/* Wait for the simulation's stream; returns the first device error, if any. */
+int rgpu_sim_sync(rgpu_sim* sim);
+
+/* ---- measurement helpers ---------------------------------------------- */
+/* Average duration (ms) of the last launch of the dominant force kernel of
+ * this handle, measured with CUDA events on the handle's stream. */
+double rgpu_sim_last_kernel_ms(const rgpu_sim* sim);
+/* Dominant-kernel timer: when enabled, every launch of the handle's force
+ * kernel is bracketed by CUDA events on the handle's stream; kernel_time
+ * returns the summed device time and the number of launches since enabling. */
+int rgpu_sim_kernel_timer(rgpu_sim* sim, int enable);
+int rgpu_sim_kernel_time(rgpu_sim* sim, double* total_ms, int64_t* launches);
+/* Run n steps bracketed by CUDA events on the handle's stream; *ms = device time. */
+int rgpu_sim_time_steps(rgpu_sim* sim, int64_t n, double* ms);
+/* Overwrite `bytes` of scratch on the handle's stream (evicts L2 between timed steps). */
+int rgpu_l2_flush(rgpu_sim* sim, size_t bytes);
+/* Select how the FP64 kernels evaluate m/r^3 (0: library rsqrt; 1: FP32-seeded
+ * binomial series in FP64; 2: the same with its h^2 term in FP32) and how MIXED
+ * rounds the FP64 displacement to FP32 (1: conversion instruction; 0: integer
+ * truncation).  All variants meet the FP64 / mixed tolerances. */
+int rgpu_set_kernel_variant(int rinv_variant, int mixed_cvt);
+/* Count of this library's kernel launches since load. */
+int64_t rgpu_launch_count(void);
+/* Measured sustained lane-operation rate (ops/s) of one instruction class on
+ * the current device: 0 = FP64 FMA, 1 = FP32 FMA, 2 = FP64<->FP32 conversion,
+ * 3 = FP32 rsqrt (MUFU). */
+int rgpu_probe_rate(int which, double* ops_per_s);
+
+/* ---- seeded synthetic workloads (reference RNG conventions) ------------ */
+/* Plummer sphere as reb_simulation_add_plummer (src/tools.c:463-502), keeping
+ * only draws with r <= rmax; masses M/N. */
+int rgpu_ic_plummer(unsigned int seed, size_t N, double M, double R, double rmax, void* out, size_t stride);
+/* Shearing-sheet ring patch (examples/shearing_sheet/problem.c shape). */
+int rgpu_ic_ring_patch(unsigned int seed, double Lx, double Ly, double Lz, double OMEGA, double surface_density,
+                       double particle_density, double rmin, double rmax, double sigma_z, double sigma_v,
+                       void* out, size_t stride, size_t cap, size_t* n_out);
+/* One star + k planets (orbital elements as reb_particle_from_orbit,
+ * src/tools.c:940-996), moved to the barycentre; *seed is advanced. */
+int rgpu_ic_planetary(unsigned int* seed, int k, double G, double mmin, double mmax, double amin, double amax,
+                      double sig_e, double sig_i, double hill_sep, void* out, size_t stride, double* p_inner);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,224 @@
+"""Host-side mirror of REBOUND's Simulation interface for the GPU hot path.
+
+`rebound_gb300.Simulation` follows the reference's Python API
+(rebound/simulation.py of REBOUND 5.0.0): modes are set by string
+(`sim.gravity = "basic"`, `sim.integrator = "whfast"`, `sim.collision = "tree"`,
+`sim.boundary = "shear"`), particles are added with `sim.add(...)`, and
+`sim.integrate(tmax)` / `sim.steps(n)` advance the state.  Everything below
+the attribute layer is one C-ABI call into librebound_gb300.so; particle state
+lives on the GPU between calls and is copied back only when `particles` is
+read (the synchronize-on-read protocol of the reference's WHFast, where the
+device copy is authoritative between steps).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import PARTICLE_DTYPE, COLLISION_DTYPE, Config, check
+
+_CFG_FLOATS = ("G", "softening", "dt", "t", "OMEGA", "OMEGAZ", "root_size", "opening_angle2",
+               "coefficient_of_restitution", "minimum_collision_velocity")
+_CFG_INTS = ("testparticle_type", "N_root_x", "N_root_y", "N_root_z", "N_ghost_x", "N_ghost_y",
+             "N_ghost_z", "rand_seed", "gravity_ignore_terms")
+
+
+class WHFastSettings:
+    """Subset of rebound's ri_whfast used on the GPU path (safe_mode)."""
+
+    def __init__(self, sim):
+        self._sim = sim
+
+    @property
+    def safe_mode(self):
+        return self._sim._cfg.whfast_safe_mode
+
+    @safe_mode.setter
+    def safe_mode(self, v):
+        self._sim._cfg.whfast_safe_mode = int(v)
+
+
+class Simulation:
+    def __init__(self):
+        self._L = _lib.load()
+        h = ctypes.c_void_p()
+        check(self._L.rgpu_sim_create(ctypes.byref(h)))
+        self._h = h
+        self._cfg = Config()
+        self._L.rgpu_config_default(ctypes.byref(self._cfg))
+        self._host = np.zeros(0, dtype=PARTICLE_DTYPE)
+        self._host_dirty = False      # host particles changed since the last upload
+        self._device_newer = False    # device stepped since the last download
+        self.ri_whfast = WHFastSettings(self)
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None) and self._h.value:
+                self._L.rgpu_sim_free(self._h)
+                self._h = ctypes.c_void_p()
+        except Exception:
+            pass
+
+    # ---- scalar settings ---------------------------------------------------
+    def __getattr__(self, name):
+        if name in _CFG_FLOATS or name in _CFG_INTS:
+            return getattr(self.__dict__["_cfg"], name)
+        raise AttributeError(name)
+
+    def __setattr__(self, name, value):
+        if name in _CFG_FLOATS:
+            setattr(self._cfg, name, float(value))
+        elif name in _CFG_INTS:
+            setattr(self._cfg, name, int(value))
+        else:
+            object.__setattr__(self, name, value)
+
+    def _enum(field, table):
+        def get(self):
+            v = getattr(self._cfg, field)
+            return next(k for k, x in table.items() if x == v)
+
+        def set_(self, value):
+            setattr(self._cfg, field, table[value.lower()] if isinstance(value, str) else int(value))
+        return property(get, set_)
+
+    gravity = _enum("gravity", _lib.GRAVITY)
+    collision = _enum("collision", _lib.COLLISION)
+    boundary = _enum("boundary", _lib.BOUNDARY)
+    integrator = _enum("integrator", _lib.INTEGRATOR)
+    collision_resolve = _enum("collision_resolve", _lib.RESOLVE)
+    del _enum
+
+    @property
+    def N_active(self):
+        v = self._cfg.N_active
+        return self.N if v < 0 else v
+
+    @N_active.setter
+    def N_active(self, v):
+        self._cfg.N_active = -1 if v is None else int(v)
+
+    @property
+    def status(self):
+        return self._cfg.status
+
+    @property
+    def collisions_log_n(self):
+        return self._cfg.collisions_log_n
+
+    def configure_box(self, root_size, N_root_x=1, N_root_y=1, N_root_z=1):
+        self._cfg.root_size = float(root_size)
+        self._cfg.N_root_x, self._cfg.N_root_y, self._cfg.N_root_z = int(N_root_x), int(N_root_y), int(N_root_z)
+
+    def configure_ghostboxes(self, N_ghost_x=0, N_ghost_y=0, N_ghost_z=0):
+        self._cfg.N_ghost_x, self._cfg.N_ghost_y, self._cfg.N_ghost_z = int(N_ghost_x), int(N_ghost_y), int(N_ghost_z)
+
+    # ---- particles ---------------------------------------------------------
+    @property
+    def N(self):
+        return len(self._host)
+
+    def add(self, particles=None, **kw):
+        """Add one particle by keyword (m, r, x, y, z, vx, vy, vz) or an array of records."""
+        self._pull()
+        if particles is not None:
+            arr = np.asarray(particles)
+            if arr.dtype != PARTICLE_DTYPE:
+                rec = np.zeros(len(arr), dtype=PARTICLE_DTYPE)
+                for f in arr.dtype.names:
+                    if f in PARTICLE_DTYPE.names:
+                        rec[f] = arr[f]
+                arr = rec
+            self._host = np.concatenate([self._host, arr])
+        else:
+            rec = np.zeros(1, dtype=PARTICLE_DTYPE)
+            for k, v in kw.items():
+                rec[k] = v
+            self._host = np.concatenate([self._host, rec])
+        self._host_dirty = True
+
+    @property
+    def particles(self):
+        """Host copy of the particle array (synchronized from the GPU)."""
+        self._pull()
+        self._host_dirty = True    # the caller may modify the returned array
+        return self._host
+
+    def set_particles_array(self, arr):
+        self._host = np.ascontiguousarray(arr, dtype=PARTICLE_DTYPE).copy()
+        self._host_dirty = True
+        self._device_newer = False
+
+    def _push(self):
+        check(self._L.rgpu_sim_configure(self._h, ctypes.byref(self._cfg)), self._h)
+        if self._host_dirty:
+            check(self._L.rgpu_sim_set_particles(self._h, self._host.ctypes.data, len(self._host),
+                                                 PARTICLE_DTYPE.itemsize), self._h)
+            self._host_dirty = False
+
+    def _pull(self):
+        if self._device_newer:
+            if self._cfg.integrator == _lib.INTEGRATOR["whfast"]:
+                check(self._L.rgpu_synchronize(self._h), self._h)
+            check(self._L.rgpu_sim_get_particles(self._h, self._host.ctypes.data, len(self._host),
+                                                 PARTICLE_DTYPE.itemsize), self._h)
+            self._device_newer = False
+
+    def _after(self, rc):
+        check(self._L.rgpu_sim_get_config(self._h, ctypes.byref(self._cfg)))
+        self._device_newer = True
+        check(rc, self._h)
+
+    # ---- hot path ----------------------------------------------------------
+    def update_acceleration(self):
+        """reb_simulation_update_acceleration (src/simulation.c:640)."""
+        self._push()
+        self._after(self._L.rgpu_update_acceleration(self._h))
+
+    def steps(self, n):
+        """reb_simulation_steps (src/simulation.c:500)."""
+        self._push()
+        self._after(self._L.rgpu_steps(self._h, int(n)))
+
+    def integrate(self, tmax):
+        """reb_simulation_integrate (src/simulation.c:465) with exact_finish_time = 1."""
+        self._push()
+        self._after(self._L.rgpu_integrate(self._h, float(tmax)))
+
+    def collision_search(self):
+        """Pair list of the search half of reb_collision_search (src/collision.c:49)."""
+        self._push()
+        n = ctypes.c_size_t(0)
+        cap = max(1024, 4 * self.N)
+        while True:
+            out = np.zeros(cap, dtype=COLLISION_DTYPE)
+            rc = self._L.rgpu_collision_search(self._h, out.ctypes.data, cap, ctypes.byref(n))
+            if rc == 9 and n.value > cap:
+                cap = int(n.value)
+                continue
+            self._after(rc)
+            return out[:n.value]
+
+    def energy(self):
+        """reb_simulation_energy (src/tools.c:108)."""
+        self._push()
+        e = ctypes.c_double(0.)
+        check(self._L.rgpu_energy(self._h, ctypes.byref(e)), self._h)
+        return e.value
+
+    def synchronize(self):
+        self._push()
+        self._after(self._L.rgpu_synchronize(self._h))
+
+    def last_kernel_ms(self):
+        return self._L.rgpu_sim_last_kernel_ms(self._h)
+
+    @property
+    def handle(self):
+        self._push()
+        return self._h
+
+
+def accelerations(sim):
+    p = sim.particles
+    return np.stack([p["ax"], p["ay"], p["az"]], axis=1)

@@ -1,0 +1,335 @@
+"""Generate golden fixtures from the UNMODIFIED reference (REBOUND 5.0.0).
+
+Run in a container that has the reference sources (it reads them where they
+lie and never copies them):
+
+    make -f oracle/ref.mk REF=<reference checkout>      # builds oracle/_ref/
+    python tests/golden/make_golden.py <reference checkout>
+
+The reference's own Python package is imported from the checkout and loads the
+serial, -ffp-contract=off build of its C core from oracle/_ref/.  Each fixture
+stores the input state next to the reference's outputs so that tests replay
+identical inputs through the oracle and the CUDA path on any machine.
+"""
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("REBOUND_REF", "/root/reference")
+sys.dont_write_bytecode = True
+sys.path[:0] = [os.path.join(REPO, "oracle", "_ref"), REF, REPO]
+
+import rebound  # noqa: E402  (the reference package)
+from rebound import clibrebound  # noqa: E402
+
+from oracle.oracle import PARTICLE_DTYPE, COLLISION_DTYPE, CELL_DTYPE  # noqa: E402
+
+FIELDS = ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "m", "r")
+clibrebound.reb_simulation_add_plummer.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_double, ctypes.c_double]
+clibrebound.reb_random_uniform.restype = ctypes.c_double
+clibrebound.reb_random_normal.restype = ctypes.c_double
+clibrebound.reb_random_powerlaw.restype = ctypes.c_double
+clibrebound.reb_random_rayleigh.restype = ctypes.c_double
+clibrebound.reb_simulation_energy.restype = ctypes.c_double
+
+
+def state(sim):
+    """Copy the reference's particle array (struct reb_particle AoS) into our dtype."""
+    n = sim.N
+    buf = (ctypes.c_char * (112 * n)).from_address(ctypes.addressof(sim.particles[0]))
+    arr = np.frombuffer(bytes(buf), dtype=PARTICLE_DTYPE).copy()
+    arr["name"] = 0
+    arr["ap"] = 0
+    arr["sim"] = 0
+    return arr
+
+
+def load(sim, arr):
+    for p in arr:
+        sim.add(m=float(p["m"]), r=float(p["r"]), x=float(p["x"]), y=float(p["y"]), z=float(p["z"]),
+                vx=float(p["vx"]), vy=float(p["vy"]), vz=float(p["vz"]))
+
+
+def accel(sim):
+    clibrebound.reb_simulation_update_acceleration(ctypes.byref(sim))
+    s = state(sim)
+    return np.stack([s["ax"], s["ay"], s["az"]], axis=1)
+
+
+def energy(sim):
+    return clibrebound.reb_simulation_energy(ctypes.byref(sim))
+
+
+def plummer_truncated(n, seed, rmax=10.0):
+    """reb_simulation_add_plummer (src/tools.c:463-502), keeping r <= rmax in order."""
+    scratch = rebound.Simulation()
+    scratch.rand_seed = seed
+    clibrebound.reb_simulation_add_plummer(ctypes.byref(scratch), int(n * 1.05) + 64, 1.0, 1.0)
+    s = state(scratch)
+    rr = np.sqrt(s["x"] ** 2 + s["y"] ** 2 + s["z"] ** 2)
+    s = s[rr <= rmax][:n].copy()
+    s["m"] = 1.0 / n
+    return s
+
+
+def fixture_gravity_plummer():
+    n, seed = 4096, 11
+    raw = rebound.Simulation()
+    raw.rand_seed = seed
+    clibrebound.reb_simulation_add_plummer(ctypes.byref(raw), 64, 1.0, 1.0)
+    plummer_raw = state(raw)                      # first 64 untruncated draws, for the IC generator
+    p0 = plummer_truncated(n, seed)
+    out = {"plummer_raw": plummer_raw, "plummer_seed": np.int64(seed), "particles": p0}
+    for mode in ("basic", "compensated"):
+        sim = rebound.Simulation()
+        sim.softening = 0.01
+        sim.gravity = mode
+        load(sim, p0)
+        out["acc_" + mode] = accel(sim)
+    sim = rebound.Simulation()
+    sim.softening = 0.01
+    sim.gravity = "basic"
+    sim.integrator = "leapfrog"
+    sim.dt = 1e-3
+    load(sim, p0)
+    out["energy0"] = np.float64(energy(sim))
+    sim.steps(10)
+    out["after10"] = state(sim)
+    sim.steps(990)
+    out["after1000"] = state(sim)
+    out["energy1000"] = np.float64(energy(sim))
+    np.savez_compressed(os.path.join(HERE, "gravity_plummer.npz"), **out)
+
+
+def fixture_gravity_cases():
+    """Edge cases of src/gravity.c: test particles, ignore terms, ghost boxes, no softening."""
+    rng = np.random.default_rng(5)
+    out = {}
+    for name, n, n_active, tp, ign, ghost, soft in (
+            ("plain", 37, None, 0, 0, 0, 0.0),
+            ("testp0", 41, 29, 0, 0, 0, 0.02),
+            ("testp1", 41, 29, 1, 0, 0, 0.02),
+            ("ignore01", 23, None, 0, 1, 0, 0.0),
+            ("ignore0", 23, None, 0, 2, 0, 0.0),
+            ("ghost", 19, None, 0, 0, 1, 0.05),
+            ("single", 1, None, 0, 0, 0, 0.0),
+            ("two", 2, None, 0, 0, 0, 0.0)):
+        p = np.zeros(n, dtype=PARTICLE_DTYPE)
+        for k in ("x", "y", "z"):
+            p[k] = rng.uniform(-0.9, 0.9, n)
+        for k in ("vx", "vy", "vz"):
+            p[k] = rng.normal(0, 0.1, n)
+        p["m"] = rng.uniform(0.1, 1.0, n) / n
+        for mode in ("basic", "compensated"):
+            if ghost and mode == "compensated":
+                continue                          # COMPENSATED has no ghost-box loop (src/gravity.c:284-531)
+            sim = rebound.Simulation()
+            sim.softening = soft
+            sim.gravity = mode
+            if ghost:
+                sim.root_size = 2.0
+                sim.boundary = "periodic"
+                sim.N_ghost_x = sim.N_ghost_y = sim.N_ghost_z = 1
+            load(sim, p)
+            if n_active is not None:
+                sim.N_active = n_active
+            sim.testparticle_type = tp
+            sim.gravity_ignore = ign
+            out[f"{name}_particles"] = p
+            out[f"{name}_acc_{mode}"] = accel(sim)
+        out[f"{name}_meta"] = np.array([n, -1 if n_active is None else n_active, tp, ign, ghost, soft * 1e6],
+                                       dtype=np.float64)
+    np.savez_compressed(os.path.join(HERE, "gravity_cases.npz"), **out)
+
+
+def ring_patch(L, seed, omega=1.3143527e-4, surface_density=400., rho=400.):
+    """Config-3 style shearing-sheet patch (examples/shearing_sheet/problem.c pattern)."""
+    sim = rebound.Simulation()
+    sim.rand_seed = seed
+    sim.OMEGA = omega
+    sim.G = 6.674e-11
+    sim.softening = 0.1
+    sim.dt = 1e-3 * 2. * np.pi / omega
+    sim.integrator = "sei"
+    sim.boundary = "shear"
+    sim.gravity = "tree"
+    sim.collision = "tree"
+    sim.collision_resolve = "hardsphere"
+    sim.root_size = 20.0
+    sim.N_root_x = int(L / 20)
+    sim.N_root_y = int(L / 20)
+    sim.N_root_z = 1
+    sim.N_ghost_x = 2
+    sim.N_ghost_y = 2
+    sim.N_ghost_z = 0
+    sim.opening_angle2 = 0.25
+    sp = ctypes.byref(sim)
+    total = 0.0
+    lx = ly = L
+    while total < surface_density * lx * ly:
+        rad = clibrebound.reb_random_powerlaw(sp, ctypes.c_double(1.), ctypes.c_double(4.), ctypes.c_double(-3.))
+        x = clibrebound.reb_random_uniform(sp, ctypes.c_double(-lx / 2), ctypes.c_double(lx / 2))
+        y = clibrebound.reb_random_uniform(sp, ctypes.c_double(-ly / 2), ctypes.c_double(ly / 2))
+        while True:
+            z = clibrebound.reb_random_normal(sp, ctypes.c_double(25.0))   # variance = sigma^2, sigma = 5 m
+            if abs(z) < 10.0:
+                break
+        vx = clibrebound.reb_random_normal(sp, ctypes.c_double(0.0005 ** 2))
+        vy = -1.5 * x * omega + clibrebound.reb_random_normal(sp, ctypes.c_double(0.0005 ** 2))
+        vz = clibrebound.reb_random_normal(sp, ctypes.c_double(0.0005 ** 2))
+        m = rho * 4. / 3. * np.pi * rad ** 3
+        sim.add(m=m, r=rad, x=x, y=y, z=z, vx=vx, vy=vy, vz=vz)
+        total += m
+    return sim
+
+
+class TreeCellC(ctypes.Structure):
+    pass
+
+
+TreeCellC._fields_ = [(k, ctypes.c_double) for k in ("x", "y", "z", "w", "m", "mx", "my", "mz")] + [
+    ("oct", ctypes.POINTER(TreeCellC) * 8), ("pt", ctypes.c_int), ("remote", ctypes.c_int)]
+
+
+def export_tree(sim):
+    """Walk the reference's pointer octree (src/tree.h:81-103) depth-first, octants 0..7."""
+    sp = ctypes.byref(sim)
+    clibrebound.reb_tree_construct(sp)
+    clibrebound.reb_tree_calculate_gravity_data(sp)
+    nroot = sim.N_root_x * sim.N_root_y * sim.N_root_z
+    roots = ctypes.cast(sim._tree_root, ctypes.POINTER(ctypes.POINTER(TreeCellC) * nroot)).contents
+    cells = []
+
+    def rec(c, root, depth, path):
+        cells.append((root, depth, path, c.x, c.y, c.z, c.w, c.m, c.mx, c.my, c.mz, c.pt))
+        for o in range(8):
+            if c.oct[o]:
+                rec(c.oct[o].contents, root, depth + 1, (path << 3) | o)
+
+    for i in range(nroot):
+        if roots[i]:
+            rec(roots[i].contents, i, 0, 0)
+    clibrebound.reb_tree_delete(sp)
+    return np.array(cells, dtype=CELL_DTYPE)
+
+
+NOOP_RESOLVE = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_byte * 72)(lambda s, c: 0)
+
+
+def collision_pairs(sim, mode):
+    """reb_collision_search (src/collision.c:49) with a no-op resolver; returns the stored pair list."""
+    sim.collision = mode
+    sim._collision_resolve = ctypes.cast(NOOP_RESOLVE, type(sim._collision_resolve))
+    clibrebound.reb_collision_search(ctypes.byref(sim))
+    n = sim.N_collisions
+    if n == 0:
+        return np.zeros(0, dtype=COLLISION_DTYPE)
+    buf = (ctypes.c_char * (72 * n)).from_address(sim.collisions)
+    return np.frombuffer(bytes(buf), dtype=COLLISION_DTYPE).copy()
+
+
+def fixture_ring():
+    sim = ring_patch(200.0, seed=7)
+    out = {"particles": state(sim),
+           "meta": np.array([sim.G, sim.OMEGA, sim.softening, sim.dt, sim.root_size, sim.N_root_x,
+                             sim.N_root_y, sim.N_root_z, 2, 2, 0, sim.opening_angle2, sim.t], dtype=np.float64)}
+    out["cells"] = export_tree(sim)
+    out["acc_tree"] = accel(sim)
+    sim.gravity = "basic"
+    out["acc_basic"] = accel(sim)
+    sim.gravity = "tree"
+    out["pairs_direct"] = collision_pairs(sim, "direct")
+    out["pairs_tree"] = collision_pairs(sim, "tree")
+    # A few full SEI + tree gravity + tree collision + hardsphere steps.
+    sim2 = ring_patch(200.0, seed=7)
+    sim2.coefficient_of_restitution = lambda s, v: 0.5
+    sim2.steps(5)
+    out["after5"] = state(sim2)
+    out["after5_t"] = np.float64(sim2.t)
+    out["after5_seed"] = np.int64(sim2.rand_seed)
+    out["after5_collisions_log_n"] = np.int64(sim2.collisions_log_n)
+    np.savez_compressed(os.path.join(HERE, "ring_patch.npz"), **out)
+
+
+def planetary_system(sim, k, seed_sim):
+    """Config-4 style system: star + k planets (log-uniform m, a; Rayleigh e, i)."""
+    sp = ctypes.byref(seed_sim)
+    U = lambda a, b: clibrebound.reb_random_uniform(sp, ctypes.c_double(a), ctypes.c_double(b))
+    R = lambda s: clibrebound.reb_random_rayleigh(sp, ctypes.c_double(s))
+    sim.add(m=1.0)
+    while True:
+        ms = np.exp([U(np.log(1e-7), np.log(1e-3)) for _ in range(k)])
+        a = np.sort(np.exp([U(np.log(0.5), np.log(30.)) for _ in range(k)]))
+        rh = ((ms[:-1] + ms[1:]) / 3.) ** (1. / 3.) * (a[:-1] + a[1:]) / 2.
+        if np.all(np.diff(a) >= 3. * rh):
+            break
+    for j in range(k):
+        sim.add(m=float(ms[j]), a=float(a[j]), e=float(R(0.02)), inc=float(R(0.01)),
+                Omega=U(0, 2 * np.pi), omega=U(0, 2 * np.pi), f=U(0, 2 * np.pi))
+    sim.move_to_com()
+    return 2 * np.pi * np.sqrt(a[0] ** 3)
+
+
+def fixture_whfast():
+    seeder = rebound.Simulation()
+    seeder.rand_seed = 3
+    systems = []
+    for s in range(8):
+        k = 2 + (s % 9)
+        sim = rebound.Simulation()
+        p_inner = planetary_system(sim, k, seeder)
+        sim.integrator = "whfast"
+        sim.dt = p_inner / 20.
+        p0 = state(sim)
+        e0 = energy(sim)
+        sim.steps(100)
+        p100 = state(sim)
+        sim.steps(900)
+        systems.append((p0, p100, state(sim), sim.dt, e0, energy(sim)))
+    out = {}
+    for s, (p0, p100, p1000, dt, e0, e1) in enumerate(systems):
+        out[f"sys{s}_p0"] = p0
+        out[f"sys{s}_p100"] = p100
+        out[f"sys{s}_p1000"] = p1000
+        out[f"sys{s}_meta"] = np.array([dt, e0, e1])
+    # Kepler solver cases (src/integrator_whfast.c:241), elliptic and hyperbolic, incl. steps > 1 period.
+    rng = np.random.default_rng(9)
+    ks = np.zeros(64, dtype=PARTICLE_DTYPE)
+    for k in ("x", "y", "z"):
+        ks[k] = rng.normal(size=64)
+    for k in ("vx", "vy", "vz"):
+        ks[k] = rng.normal(size=64) * np.where(np.arange(64) % 4 == 0, 2.0, 0.7)
+    mus = rng.uniform(0.5, 2.0, 64)
+    dts = rng.uniform(-3.0, 3.0, 64) * np.where(np.arange(64) % 5 == 0, 10.0, 0.1)
+    clibrebound.reb_integrator_whfast_kepler_solver.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_void_p]
+    kout = ks.copy()
+    for i in range(64):
+        clibrebound.reb_integrator_whfast_kepler_solver(kout[i:i + 1].ctypes.data, mus[i], dts[i], None)
+    out["kepler_in"] = ks
+    out["kepler_mu"] = mus
+    out["kepler_dt"] = dts
+    out["kepler_out"] = kout
+    np.savez_compressed(os.path.join(HERE, "whfast.npz"), **out)
+
+
+def fixture_sei_periodic():
+    """SEI + BASIC gravity + shear boundary without collisions (trajectory parity)."""
+    sim = ring_patch(100.0, seed=21)
+    sim.collision = "none"
+    sim.gravity = "basic"
+    p0 = state(sim)
+    meta = np.array([sim.G, sim.OMEGA, sim.softening, sim.dt, sim.root_size,
+                     sim.N_root_x, sim.N_root_y, sim.N_root_z, 2, 2, 0, sim.t])
+    sim.steps(20)
+    np.savez_compressed(os.path.join(HERE, "sei_shear.npz"), particles=p0, after20=state(sim), meta=meta)
+
+
+if __name__ == "__main__":
+    which = sys.argv[2:] or ["gravity_cases", "ring", "whfast", "sei", "gravity_plummer"]
+    for w in which:
+        print("generating", w, flush=True)
+        globals()["fixture_" + w]() if w != "sei" else fixture_sei_periodic()
