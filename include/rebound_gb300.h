@@ -156,9 +156,10 @@ int rgpu_sim_time_steps(rgpu_sim* sim, int64_t n, double* ms);
 /* Overwrite `bytes` of scratch on the handle's stream (evicts L2 between timed steps). */
 int rgpu_l2_flush(rgpu_sim* sim, size_t bytes);
 /* Select how the FP64 kernels evaluate m/r^3 (0: library rsqrt; 1: FP32-seeded
- * binomial series in FP64; 2: the same with its h^2 term in FP32) and how MIXED
- * rounds the FP64 displacement to FP32 (1: conversion instruction; 0: integer
- * truncation).  All variants meet the FP64 / mixed tolerances. */
+ * binomial series in FP64; 2: the same with its h^2 term in FP32 via cvt; 3 (default):
+ * as 2 with the conversions done on the integer pipe) and how MIXED
+ * rounds the FP64 displacement to FP32 (1: conversion instruction; 0 (default):
+ * integer-pipe rounding).  All variants meet the FP64 / mixed tolerances. */
 int rgpu_set_kernel_variant(int rinv_variant, int mixed_cvt);
 /* Count of this library's kernel launches since load. */
 int64_t rgpu_launch_count(void);
@@ -166,6 +167,43 @@ int64_t rgpu_launch_count(void);
  * the current device: 0 = FP64 FMA, 1 = FP32 FMA, 2 = FP64<->FP32 conversion,
  * 3 = FP32 rsqrt (MUFU). */
 int rgpu_probe_rate(int which, double* ops_per_s);
+
+/* Kepler drift of n independent bodies with gravitational parameters mu[i]
+ * over dt[i] (universal variables, Stumpff series, Newton / quartic solver
+ * with bisection fallback).  Device counterpart of the reference's public
+ * reb_integrator_whfast_kepler_solver (src/integrator_whfast.c:241-427).
+ * Inputs: records of `stride` bytes starting with x, y, z, vx, vy, vz; outputs
+ * 6 doubles per body. */
+int rgpu_kepler_solve(const void* bodies, size_t stride, const double* mu, const double* dt,
+                      double* out, size_t n);
+
+/* ---- batched WHFast ensemble ------------------------------------------ */
+/* Many independent small systems (2..16 bodies each; each one a REBOUND
+ * simulation with WHFast, Jacobi coordinates, DEFAULT kernel, safe_mode 1,
+ * no softening; src/integrator_whfast.c:1113-1259) advanced together.
+ * particles: all systems' records back to back (stride bytes each, layout of
+ * struct reb_particle); system s owns records [offsets[s], offsets[s+1]).
+ * dts: per-system timestep.  exact != 0 selects kernels compiled without FMA
+ * contraction (bit-identical to the reference's serial build); 0 selects the
+ * faster FMA-contracted kernels. */
+typedef struct rgpu_ensemble rgpu_ensemble;
+int  rgpu_ensemble_create(rgpu_ensemble** out, const void* particles, size_t stride, const int64_t* offsets,
+                          size_t n_systems, const double* dts, double G, int exact);
+void rgpu_ensemble_free(rgpu_ensemble* ens);
+const char* rgpu_ensemble_last_error(const rgpu_ensemble* ens);
+/* CTA size (32/64/128/256) and steps fused per kernel launch. */
+int  rgpu_ensemble_set_launch(rgpu_ensemble* ens, int block, int64_t steps_per_launch);
+/* Advance every system by n steps (CUDA-graph replays of fused chunks). */
+int  rgpu_ensemble_steps(rgpu_ensemble* ens, int64_t n);
+int  rgpu_ensemble_time_steps(rgpu_ensemble* ens, int64_t n, double* ms);
+/* Time probe_steps for each CTA size, keep the fastest; set steps per launch. */
+int  rgpu_ensemble_autotune(rgpu_ensemble* ens, int64_t probe_steps, int64_t max_steps_per_launch,
+                            int* best_block, double* best_ms_per_step);
+/* Write positions, velocities and masses back into the caller's records. */
+int  rgpu_ensemble_get_particles(rgpu_ensemble* ens, void* particles, size_t stride);
+/* Per-system total energy (src/tools.c:108-162) and time. */
+int  rgpu_ensemble_energy(rgpu_ensemble* ens, double* energies);
+int  rgpu_ensemble_times(rgpu_ensemble* ens, double* t);
 
 /* ---- seeded synthetic workloads (reference RNG conventions) ------------ */
 /* Plummer sphere as reb_simulation_add_plummer (src/tools.c:463-502), keeping

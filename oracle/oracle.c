@@ -1033,3 +1033,29 @@ void orc_ic_plummer(unsigned int seed, size_t N, double M, double R, double rmax
         out[n++] = p;
     }
 }
+
+/* Rows [i0, i1) of the OpenMP COMPENSATED gather (src/gravity.c:308-343),
+ * no ghost boxes, all particles active: an accurate reference for a sample of
+ * rows at sizes where the full O(N^2) sum is too slow on the host. */
+void orc_gravity_compensated_omp_rows(orc_sim* r, size_t i0, size_t i1) {
+    orc_particle* const P = r->particles;
+    const size_t N = r->N;
+    const double G = r->G, eps2 = r->softening * r->softening;
+    if (i1 > N) i1 = N;
+#pragma omp parallel for schedule(guided)
+    for (size_t i = i0; i < i1; i++) {
+        double ax = 0., ay = 0., az = 0., cx = 0., cy = 0., cz = 0.;
+        for (size_t j = 0; j < N; j++) {
+            if (i == j) continue;
+            const double dx = P[i].x - P[j].x, dy = P[i].y - P[j].y, dz = P[i].z - P[j].z;
+            const double r2 = dx * dx + dy * dy + dz * dz + eps2;
+            const double rr = sqrt(r2);
+            const double pf = G / (r2 * rr);
+            const double pfj = -pf * P[j].m;
+            KAHAN_ADD(ax, cx, pfj * dx);
+            KAHAN_ADD(ay, cy, pfj * dy);
+            KAHAN_ADD(az, cz, pfj * dz);
+        }
+        P[i].ax = ax; P[i].ay = ay; P[i].az = az;
+    }
+}

@@ -76,6 +76,7 @@ void orc_gravity_basic_omp(orc_sim* r);
 void orc_gravity_basic_omp_rows(orc_sim* r, size_t i0, size_t i1);
 void orc_gravity_compensated_serial(orc_sim* r);
 void orc_gravity_compensated_omp(orc_sim* r);
+void orc_gravity_compensated_omp_rows(orc_sim* r, size_t i0, size_t i1);
 void orc_gravity_tree(orc_sim* r);
 int  orc_tree_export(orc_sim* r, orc_cell* out, size_t cap, size_t* n_out);
 

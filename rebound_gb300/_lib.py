@@ -79,6 +79,19 @@ SIGNATURES = {
     "rgpu_l2_flush": (ctypes.c_int, [_P, ctypes.c_size_t]),
     "rgpu_set_kernel_variant": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     "rgpu_probe_rate": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    "rgpu_kepler_solve": (ctypes.c_int, [_P, ctypes.c_size_t, _P, _P, _P, ctypes.c_size_t]),
+    "rgpu_ensemble_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), _P, ctypes.c_size_t, _P,
+                                            ctypes.c_size_t, _P, ctypes.c_double, ctypes.c_int]),
+    "rgpu_ensemble_free": (None, [_P]),
+    "rgpu_ensemble_last_error": (ctypes.c_char_p, [_P]),
+    "rgpu_ensemble_set_launch": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int64]),
+    "rgpu_ensemble_steps": (ctypes.c_int, [_P, ctypes.c_int64]),
+    "rgpu_ensemble_time_steps": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.POINTER(ctypes.c_double)]),
+    "rgpu_ensemble_autotune": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(ctypes.c_int),
+                                              ctypes.POINTER(ctypes.c_double)]),
+    "rgpu_ensemble_get_particles": (ctypes.c_int, [_P, _P, ctypes.c_size_t]),
+    "rgpu_ensemble_energy": (ctypes.c_int, [_P, _P]),
+    "rgpu_ensemble_times": (ctypes.c_int, [_P, _P]),
     "rgpu_ic_plummer": (ctypes.c_int, [ctypes.c_uint, ctypes.c_size_t, ctypes.c_double, ctypes.c_double,
                                        ctypes.c_double, _P, ctypes.c_size_t]),
     "rgpu_ic_ring_patch": (ctypes.c_int, [ctypes.c_uint] + [ctypes.c_double] * 10 +

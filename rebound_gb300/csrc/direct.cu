@@ -11,7 +11,11 @@
 //
 // GB300 executes FP64 arithmetic on a narrow pipe (about 1/64 of the FP32
 // rate), so the FP64 kernel minimises FP64 instructions:
-//   displacement 3 DADD, r^2 3 DFMA, G m / r^3 5-7, accumulate 3 DFMA.
+//   displacement 3 DADD, r^2 3 DFMA, G m / r^3 6, accumulate 3 DFMA = 15
+// per pair (all format conversions run on the integer pipe).  BASIC sums each
+// 256-body tile with FMAs and folds the tile sums in with Kahan compensation,
+// so its error does not grow with N (the plain sequential sum of 262,144 terms
+// is off by up to ~3e-14 relative).
 // 1/r^3 is seeded in FP32 (MUFU rsqrt) from an integer truncation of r^2 and
 // corrected in FP64 with the binomial series
 //   (1-h)^(-3/2) = 1 + 3/2 h + 15/8 h^2 + O(h^3),   h = 1 - r^2 y0^2,
@@ -26,7 +30,7 @@ constexpr int kBlock = 256;   // threads per CTA = i-particles per CTA = j-tile 
 
 enum Mode { kBasic = 0, kComp = 1, kMixed = 2, kMixedSplit = 3 };
 // How m/r^3 is evaluated in the FP64 modes.
-enum RinvVariant { kRinvLib = 0, kRinvSeries = 1, kRinvSeriesF32 = 2 };
+enum RinvVariant { kRinvLib = 0, kRinvSeries = 1, kRinvSeriesF32 = 2, kRinvSeriesInt = 3 };
 
 // --- exact bit-level conversions on the integer pipe --------------------------
 // Positive double -> float by truncating the mantissa; valid for v in [2^-126, 2^128).
@@ -45,7 +49,15 @@ __device__ __forceinline__ float trunc_to_float(double v) {
     const unsigned f = ((hi & 0x7FFFFFFFu) < 0x38100000u) ? 0u : (mag | (hi & 0x80000000u));
     return __uint_as_float(f);
 }
-// Positive normal float -> double, exactly.
+// Signed double -> float rounded to nearest (ties away from zero); |v| < 2^-126 gives 0.
+__device__ __forceinline__ float round_to_float(double v) {
+    const unsigned lo = (unsigned)__double2loint(v);
+    const unsigned hi = (unsigned)__double2hiint(v);
+    const unsigned mag = ((__funnelshift_l(lo, hi, 3) - 0xC0000000u) + ((lo >> 28) & 1u)) & 0x7FFFFFFFu;
+    const unsigned f = ((hi & 0x7FFFFFFFu) < 0x38100000u) ? 0u : (mag | (hi & 0x80000000u));
+    return __uint_as_float(f);
+}
+// Positive normal float -> double, exactly (0 maps to 2^-127, harmless where used).
 __device__ __forceinline__ double exact_to_double(float f) {
     const unsigned b = __float_as_uint(f);
     return __hiloint2double((int)((b >> 3) + 0x38000000u), (int)(b << 29));
@@ -71,6 +83,11 @@ __device__ __forceinline__ double m_rinv3(double r2, double m) {
         if (RV == kRinvSeriesF32) {
             const float hf = (float)h;
             c = fma(h, 1.5, (double)(1.875f * hf * hf));   // 15/8 h^2 needs ~11 bits
+        } else if (RV == kRinvSeriesInt) {
+            // The same with both conversions on the integer pipe (GB300 runs cvt
+            // on the FP64 pipe): 15/8 h^2 < 2^-40 needs only ~11 correct bits.
+            const float hf = trunc_to_float(h);
+            c = fma(h, 1.5, exact_to_double(1.875f * hf * hf));
         } else {
             c = h * fma(h, 1.875, 1.5);
         }
@@ -147,6 +164,9 @@ __global__ void __launch_bounds__(kBlock) direct_kernel(DirectArgs a, const Ghos
         __syncthreads();
         const int nt = min(kBlock, j1 - jt);
         for (int g = 0; g < ng; g++) {
+            // BASIC: FMA-accumulate this tile, then fold the tile sum into the running
+            // total with Kahan compensation (error O(tile) instead of O(N) terms).
+            double tx = 0., ty = 0., tz = 0.;
             // The reference shifts particle i by the ghost offset: dx_ref = (gb + x_i) - x_j;
             // here d = x_j - (gb + x_i) and the force is +s*d.
             double gxi = xi, gyi = yi, gzi = zi;
@@ -170,7 +190,7 @@ __global__ void __launch_bounds__(kBlock) direct_kernel(DirectArgs a, const Ghos
                     double s = m_rinv3<RV>(r2, q.w);
                     s = skip ? 0.0 : s;
                     if (MODE == kBasic) {
-                        sx = fma(s, dx, sx); sy = fma(s, dy, sy); sz = fma(s, dz, sz);
+                        tx = fma(s, dx, tx); ty = fma(s, dy, ty); tz = fma(s, dz, tz);
                     } else {
                         // Kahan per component (src/gravity.c:325-343).
                         double t, y;
@@ -184,7 +204,7 @@ __global__ void __launch_bounds__(kBlock) direct_kernel(DirectArgs a, const Ghos
                         const double4_32a q = tile[k];
                         const double dx = q.x - gxi, dy = q.y - gyi, dz = q.z - gzi;   // FP64 displacement
                         if (CVT) { dxf = (float)dx; dyf = (float)dy; dzf = (float)dz; mf = (float)q.w; }
-                        else { dxf = trunc_to_float(dx); dyf = trunc_to_float(dy); dzf = trunc_to_float(dz); mf = trunc_to_float(q.w); }
+                        else { dxf = round_to_float(dx); dyf = round_to_float(dy); dzf = round_to_float(dz); mf = round_to_float(q.w); }
                     } else {
                         const float4 h = tile_s[2 * k], l = tile_s[2 * k + 1];
                         // The FP64 displacement from the two-float split: the hi difference is
@@ -205,12 +225,18 @@ __global__ void __launch_bounds__(kBlock) direct_kernel(DirectArgs a, const Ghos
                     y = fmaf(s, dzf, -fcz); t = fsz + y; fcz = (t - fsz) - y; fsz = t;
                 }
             }
+            if (MODE == kBasic) {
+                double t, y;
+                y = tx - cx; t = sx + y; cx = (t - sx) - y; sx = t;
+                y = ty - cy; t = sy + y; cy = (t - sy) - y; sy = t;
+                y = tz - cz; t = sz + y; cz = (t - sz) - y; sz = t;
+            }
         }
     }
     if (!live) return;
     if (MODE == kMixed || MODE == kMixedSplit) {
         sx = (double)fsx - (double)fcx; sy = (double)fsy - (double)fcy; sz = (double)fsz - (double)fcz;
-    } else if (MODE == kComp) {
+    } else {
         sx -= cx; sy -= cy; sz -= cz;
     }
     if (a.splits == 1) {
@@ -336,8 +362,8 @@ int choose_splits(int nbi, int jmax) {
 }
 
 GhostList* g_ghost_dev = nullptr;
-int g_rinv_variant = kRinvSeries;
-bool g_mixed_cvt = true;
+int g_rinv_variant = kRinvSeriesInt;
+bool g_mixed_cvt = false;
 
 template <int MODE, bool GEN>
 void launch_mode(dim3 grid, cudaStream_t st, const DirectArgs& a) {
@@ -345,7 +371,8 @@ void launch_mode(dim3 grid, cudaStream_t st, const DirectArgs& a) {
         switch (g_rinv_variant) {
             case kRinvLib: direct_kernel<MODE, GEN, kRinvLib, true><<<grid, kBlock, 0, st>>>(a, g_ghost_dev); break;
             case kRinvSeriesF32: direct_kernel<MODE, GEN, kRinvSeriesF32, true><<<grid, kBlock, 0, st>>>(a, g_ghost_dev); break;
-            default: direct_kernel<MODE, GEN, kRinvSeries, true><<<grid, kBlock, 0, st>>>(a, g_ghost_dev); break;
+            case kRinvSeries: direct_kernel<MODE, GEN, kRinvSeries, true><<<grid, kBlock, 0, st>>>(a, g_ghost_dev); break;
+            default: direct_kernel<MODE, GEN, kRinvSeriesInt, true><<<grid, kBlock, 0, st>>>(a, g_ghost_dev); break;
         }
     } else if (MODE == kMixed && !g_mixed_cvt) {
         direct_kernel<MODE, GEN, kRinvSeries, false><<<grid, kBlock, 0, st>>>(a, g_ghost_dev);
@@ -357,7 +384,7 @@ void launch_mode(dim3 grid, cudaStream_t st, const DirectArgs& a) {
 }  // namespace
 
 extern "C" int rgpu_set_kernel_variant(int rinv_variant, int mixed_cvt) {
-    if (rinv_variant < 0 || rinv_variant > 2) return RGPU_ERR_ARG;
+    if (rinv_variant < 0 || rinv_variant > 3) return RGPU_ERR_ARG;
     g_rinv_variant = rinv_variant;
     g_mixed_cvt = mixed_cvt != 0;
     return RGPU_OK;

@@ -1,0 +1,317 @@
+// Batched WHFast ensemble: thousands of independent small planetary systems
+// (one REBOUND simulation each, WHFast Jacobi / DEFAULT kernel / safe_mode 1)
+// advanced together on one GPU.
+//
+// Systems are grouped into buckets by body count; each bucket is a
+// structure-of-arrays block [field][body][system] in HBM and is advanced by its
+// own kernel instantiation (one thread per system, fully unrolled over bodies).
+// Buckets run concurrently on separate streams; a chunk of `steps_per_launch`
+// steps per kernel is captured once into a CUDA graph (fork/join over the
+// bucket streams) and replayed.  An autotuner picks the CTA size and the steps
+// per launch by timing short runs.
+#define ENSEMBLE_NS ens_fast
+#include "ensemble_kernels.cuh"
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <new>
+#include <vector>
+
+void* ensemble_exact_steps_fn(int nb);
+void* ensemble_exact_energy_fn(int nb);
+
+struct EnsBucket {
+    int nb = 0;
+    int count = 0;
+    double* st = nullptr;        // 7 * nb * count
+    double* dt = nullptr;        // count
+    double* t = nullptr;         // count
+    std::vector<int> ids;        // system index of each slot
+    cudaStream_t stream = nullptr;
+};
+
+struct rgpu_ensemble {
+    std::vector<EnsBucket> b;
+    std::vector<int64_t> offsets;      // n_systems + 1 particle offsets
+    size_t n_systems = 0;
+    double G = 1.0;
+    int exact = 0;
+    int block = 128;
+    int64_t steps_per_launch = 256;
+    cudaStream_t stream = nullptr;
+    uint32_t* d_status = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr, fork = nullptr;
+    std::vector<cudaEvent_t> joins;
+    cudaGraphExec_t graph = nullptr;
+    int64_t graph_steps = -1;
+    int graph_block = -1;
+    std::string msg;
+};
+
+namespace {
+
+int ens_err(rgpu_ensemble* e, int code, const std::string& m) {
+    if (e) e->msg = m;
+    return code;
+}
+
+#define ENS_CUDA(e, expr) do { cudaError_t _x = (expr); if (_x != cudaSuccess) { \
+    return ens_err((e), _x == cudaErrorMemoryAllocation ? RGPU_ERR_NOMEM : RGPU_ERR_CUDA, \
+                   std::string(#expr) + ": " + cudaGetErrorString(_x)); } } while (0)
+
+typedef void (*StepsFn)(double*, const double*, double*, int, int, double, uint32_t*);
+typedef void (*EnergyFn)(const double*, int, double, double*);
+
+StepsFn steps_fn(const rgpu_ensemble* e, int nb) {
+    return e->exact ? (StepsFn)ensemble_exact_steps_fn(nb) : ens_fast::steps_for(nb);
+}
+EnergyFn energy_fn(const rgpu_ensemble* e, int nb) {
+    return e->exact ? (EnergyFn)ensemble_exact_energy_fn(nb) : ens_fast::energy_for(nb);
+}
+
+// Enqueue one chunk of `n` steps for every bucket (fork/join over bucket streams).
+int enqueue_chunk(rgpu_ensemble* e, int n) {
+    ENS_CUDA(e, cudaEventRecord(e->fork, e->stream));
+    for (size_t k = 0; k < e->b.size(); k++) {
+        EnsBucket& B = e->b[k];
+        ENS_CUDA(e, cudaStreamWaitEvent(B.stream, e->fork, 0));
+        StepsFn f = steps_fn(e, B.nb);
+        const unsigned grid = (unsigned)((B.count + e->block - 1) / e->block);
+        f<<<grid, e->block, 0, B.stream>>>(B.st, B.dt, B.t, B.count, n, e->G, e->d_status);
+        g_launches++;
+        ENS_CUDA(e, cudaEventRecord(e->joins[k], B.stream));
+        ENS_CUDA(e, cudaStreamWaitEvent(e->stream, e->joins[k], 0));
+    }
+    return RGPU_OK;
+}
+
+int build_graph(rgpu_ensemble* e, int64_t n) {
+    if (e->graph && e->graph_steps == n && e->graph_block == e->block) return RGPU_OK;
+    if (e->graph) { cudaGraphExecDestroy(e->graph); e->graph = nullptr; }
+    cudaGraph_t g;
+    ENS_CUDA(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = enqueue_chunk(e, (int)n);
+    const cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+    if (rc) return rc;
+    ENS_CUDA(e, ce);
+    const cudaError_t ie = cudaGraphInstantiate(&e->graph, g, 0);
+    cudaGraphDestroy(g);
+    ENS_CUDA(e, ie);
+    e->graph_steps = n;
+    e->graph_block = e->block;
+    return RGPU_OK;
+}
+
+int run_steps(rgpu_ensemble* e, int64_t n) {
+    const int64_t spl = std::max<int64_t>(1, e->steps_per_launch);
+    int64_t full = n / spl, rest = n % spl;
+    if (full > 0) {
+        const int rc = build_graph(e, spl);
+        if (rc) return rc;
+        for (int64_t k = 0; k < full; k++) ENS_CUDA(e, cudaGraphLaunch(e->graph, e->stream));
+    }
+    if (rest > 0) return enqueue_chunk(e, (int)rest);
+    return RGPU_OK;
+}
+
+int read_status(rgpu_ensemble* e) {
+    uint32_t st = 0;
+    ENS_CUDA(e, cudaMemcpyAsync(&st, e->d_status, sizeof(st), cudaMemcpyDeviceToHost, e->stream));
+    ENS_CUDA(e, cudaStreamSynchronize(e->stream));
+    if (st) {
+        cudaMemsetAsync(e->d_status, 0, sizeof(uint32_t), e->stream);
+        return ens_err(e, RGPU_ERR_ARG, "Kepler solver hit its iteration cap");
+    }
+    return RGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rgpu_ensemble_create(rgpu_ensemble** out, const void* particles, size_t stride, const int64_t* offsets,
+                         size_t n_systems, const double* dts, double G, int exact) {
+    if (!out || !particles || !offsets || !dts || stride < 88 || n_systems == 0) return RGPU_ERR_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { cudaGetLastError(); return RGPU_ERR_CUDA; }
+    rgpu_ensemble* e = new (std::nothrow) rgpu_ensemble();
+    if (!e) return RGPU_ERR_NOMEM;
+    e->n_systems = n_systems;
+    e->G = G;
+    e->exact = exact != 0;
+    e->offsets.assign(offsets, offsets + n_systems + 1);
+    std::map<int, std::vector<int>> groups;
+    for (size_t s = 0; s < n_systems; s++) {
+        const int64_t nb = offsets[s + 1] - offsets[s];
+        if (nb < 2 || nb > wh::kMaxBodies) { delete e; return RGPU_ERR_UNSUPPORTED; }
+        groups[(int)nb].push_back((int)s);
+    }
+    int rc = RGPU_OK;
+    if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&e->d_status, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMemset(e->d_status, 0, sizeof(uint32_t)) != cudaSuccess ||
+        cudaEventCreate(&e->e0) != cudaSuccess || cudaEventCreate(&e->e1) != cudaSuccess ||
+        cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming) != cudaSuccess)
+        rc = RGPU_ERR_CUDA;
+    const char* base = (const char*)particles;
+    for (auto& kv : groups) {
+        if (rc) break;
+        EnsBucket B;
+        B.nb = kv.first;
+        B.count = (int)kv.second.size();
+        B.ids = kv.second;
+        const size_t nf = (size_t)B.nb * B.count;
+        std::vector<double> h(7 * nf), hdt(B.count), ht(B.count, 0.0);
+        for (int q = 0; q < B.count; q++) {
+            const int s = B.ids[q];
+            hdt[q] = dts[s];
+            for (int i = 0; i < B.nb; i++) {
+                const double* r = (const double*)(base + (size_t)(offsets[s] + i) * stride);
+                const size_t o = (size_t)i * B.count + q;
+                h[0 * nf + o] = r[0]; h[1 * nf + o] = r[1]; h[2 * nf + o] = r[2];
+                h[3 * nf + o] = r[3]; h[4 * nf + o] = r[4]; h[5 * nf + o] = r[5];
+                h[6 * nf + o] = r[9];
+            }
+        }
+        if (cudaMalloc(&B.st, sizeof(double) * 7 * nf) != cudaSuccess ||
+            cudaMalloc(&B.dt, sizeof(double) * B.count) != cudaSuccess ||
+            cudaMalloc(&B.t, sizeof(double) * B.count) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&B.stream, cudaStreamNonBlocking) != cudaSuccess) {
+            rc = RGPU_ERR_NOMEM;
+        } else {
+            cudaMemcpy(B.st, h.data(), sizeof(double) * 7 * nf, cudaMemcpyHostToDevice);
+            cudaMemcpy(B.dt, hdt.data(), sizeof(double) * B.count, cudaMemcpyHostToDevice);
+            cudaMemcpy(B.t, ht.data(), sizeof(double) * B.count, cudaMemcpyHostToDevice);
+        }
+        e->b.push_back(B);
+        cudaEvent_t j;
+        cudaEventCreateWithFlags(&j, cudaEventDisableTiming);
+        e->joins.push_back(j);
+    }
+    if (rc) { rgpu_ensemble_free(e); return rc; }
+    *out = e;
+    return RGPU_OK;
+}
+
+void rgpu_ensemble_free(rgpu_ensemble* e) {
+    if (!e) return;
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    if (e->graph) cudaGraphExecDestroy(e->graph);
+    for (auto& B : e->b) {
+        if (B.stream) cudaStreamSynchronize(B.stream);
+        cudaFree(B.st); cudaFree(B.dt); cudaFree(B.t);
+        if (B.stream) cudaStreamDestroy(B.stream);
+    }
+    for (auto j : e->joins) cudaEventDestroy(j);
+    if (e->fork) cudaEventDestroy(e->fork);
+    if (e->e0) cudaEventDestroy(e->e0);
+    if (e->e1) cudaEventDestroy(e->e1);
+    cudaFree(e->d_status);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+}
+
+const char* rgpu_ensemble_last_error(const rgpu_ensemble* e) { return e ? e->msg.c_str() : "null handle"; }
+
+int rgpu_ensemble_set_launch(rgpu_ensemble* e, int block, int64_t steps_per_launch) {
+    if (!e || (block != 32 && block != 64 && block != 128 && block != 256) || steps_per_launch < 1) return RGPU_ERR_ARG;
+    e->block = block;
+    e->steps_per_launch = steps_per_launch;
+    return RGPU_OK;
+}
+
+int rgpu_ensemble_steps(rgpu_ensemble* e, int64_t n) {
+    if (!e || n < 0) return RGPU_ERR_ARG;
+    RGPU_TRY(run_steps(e, n));
+    return read_status(e);
+}
+
+int rgpu_ensemble_time_steps(rgpu_ensemble* e, int64_t n, double* ms) {
+    if (!e || !ms || n < 0) return RGPU_ERR_ARG;
+    ENS_CUDA(e, cudaEventRecord(e->e0, e->stream));
+    RGPU_TRY(run_steps(e, n));
+    ENS_CUDA(e, cudaEventRecord(e->e1, e->stream));
+    ENS_CUDA(e, cudaEventSynchronize(e->e1));
+    float f = 0.f;
+    ENS_CUDA(e, cudaEventElapsedTime(&f, e->e0, e->e1));
+    *ms = f;
+    return read_status(e);
+}
+
+// Autotuner: time `probe_steps` steps for each CTA size and keep the fastest;
+// then pick the largest steps-per-launch not above `max_steps_per_launch`
+// (more steps per launch amortise launches; the cap bounds time-to-first-result).
+// The probed steps advance the state (callers tune on a scratch copy).
+int rgpu_ensemble_autotune(rgpu_ensemble* e, int64_t probe_steps, int64_t max_steps_per_launch,
+                           int* best_block, double* best_ms_per_step) {
+    if (!e || probe_steps < 1 || max_steps_per_launch < 1) return RGPU_ERR_ARG;
+    const int blocks[4] = {32, 64, 128, 256};
+    double best = 1e300;
+    int bb = e->block;
+    for (int k = 0; k < 4; k++) {
+        e->block = blocks[k];
+        e->steps_per_launch = probe_steps;
+        double ms = 0.;
+        RGPU_TRY(rgpu_ensemble_time_steps(e, probe_steps, &ms));   // includes graph build
+        RGPU_TRY(rgpu_ensemble_time_steps(e, probe_steps, &ms));
+        if (ms < best) { best = ms; bb = blocks[k]; }
+    }
+    e->block = bb;
+    e->steps_per_launch = max_steps_per_launch;
+    if (best_block) *best_block = bb;
+    if (best_ms_per_step) *best_ms_per_step = best / (double)probe_steps;
+    return RGPU_OK;
+}
+
+int rgpu_ensemble_get_particles(rgpu_ensemble* e, void* particles, size_t stride) {
+    if (!e || !particles || stride < 88) return RGPU_ERR_ARG;
+    ENS_CUDA(e, cudaStreamSynchronize(e->stream));
+    char* base = (char*)particles;
+    for (auto& B : e->b) {
+        const size_t nf = (size_t)B.nb * B.count;
+        std::vector<double> h(7 * nf);
+        ENS_CUDA(e, cudaMemcpy(h.data(), B.st, sizeof(double) * 7 * nf, cudaMemcpyDeviceToHost));
+        for (int q = 0; q < B.count; q++) {
+            const int s = B.ids[q];
+            for (int i = 0; i < B.nb; i++) {
+                double* r = (double*)(base + (size_t)(e->offsets[s] + i) * stride);
+                const size_t o = (size_t)i * B.count + q;
+                r[0] = h[0 * nf + o]; r[1] = h[1 * nf + o]; r[2] = h[2 * nf + o];
+                r[3] = h[3 * nf + o]; r[4] = h[4 * nf + o]; r[5] = h[5 * nf + o];
+                r[9] = h[6 * nf + o];
+            }
+        }
+    }
+    return RGPU_OK;
+}
+
+int rgpu_ensemble_energy(rgpu_ensemble* e, double* energies) {
+    if (!e || !energies) return RGPU_ERR_ARG;
+    for (auto& B : e->b) {
+        double* d = nullptr;
+        ENS_CUDA(e, cudaMalloc(&d, sizeof(double) * B.count));
+        EnergyFn f = energy_fn(e, B.nb);
+        f<<<(B.count + 127) / 128, 128, 0, e->stream>>>(B.st, B.count, e->G, d);
+        g_launches++;
+        std::vector<double> h(B.count);
+        const cudaError_t ce = cudaMemcpyAsync(h.data(), d, sizeof(double) * B.count, cudaMemcpyDeviceToHost, e->stream);
+        cudaStreamSynchronize(e->stream);
+        cudaFree(d);
+        ENS_CUDA(e, ce);
+        for (int q = 0; q < B.count; q++) energies[B.ids[q]] = h[q];
+    }
+    return RGPU_OK;
+}
+
+int rgpu_ensemble_times(rgpu_ensemble* e, double* t) {
+    if (!e || !t) return RGPU_ERR_ARG;
+    for (auto& B : e->b) {
+        std::vector<double> h(B.count);
+        ENS_CUDA(e, cudaMemcpy(h.data(), B.t, sizeof(double) * B.count, cudaMemcpyDeviceToHost));
+        for (int q = 0; q < B.count; q++) t[B.ids[q]] = h[q];
+    }
+    return RGPU_OK;
+}
+
+}  // extern "C"

@@ -5,6 +5,3 @@ int tree_collisions(rgpu_sim* s, rgpu_collision*, size_t, size_t*, bool) { retur
 void tree_free(rgpu_sim*) {}
 int direct_collisions(rgpu_sim* s, rgpu_collision*, size_t, size_t*, bool) { return set_error(s, RGPU_ERR_UNSUPPORTED, "direct collisions not built"); }
 int resolve_collisions_device(rgpu_sim* s) { return set_error(s, RGPU_ERR_UNSUPPORTED, "resolve not built"); }
-int whfast_step(rgpu_sim* s) { return set_error(s, RGPU_ERR_UNSUPPORTED, "whfast not built"); }
-int whfast_synchronize(rgpu_sim*) { return RGPU_OK; }
-void whfast_free(rgpu_sim*) {}

@@ -1,0 +1,383 @@
+// WHFast (Wisdom-Holman, Jacobi coordinates, DEFAULT kernel, no correctors)
+// for one small system held by one thread: src/integrator_whfast.c and
+// src/transformations.c of REBOUND 5.0.0.
+//
+// Each function restates the reference routine it names with the same
+// sequence of floating-point operations, so a translation unit compiled with
+// --fmad=false reproduces the reference bit for bit (IEEE division and square
+// root are correctly rounded on both).  The batched ensemble includes this
+// header from a unit compiled with FMA contraction, trading bit-identity for
+// fewer FP64 instructions.
+//
+// Every data-dependent loop carries an iteration cap; on hitting it the
+// solver records DEV_ERR_KEPLER in the device status word and continues with
+// its current estimate instead of spinning.
+#pragma once
+#include "rgpu_internal.cuh"
+
+namespace wh {
+
+constexpr int kMaxBodies = 16;
+
+template <int NB>
+struct System {
+    double x[NB], y[NB], z[NB], vx[NB], vy[NB], vz[NB], m[NB];
+};
+
+template <int NB>
+struct Jacobi {
+    double x[NB], y[NB], z[NB], vx[NB], vy[NB], vz[NB], m[NB];
+};
+
+__device__ static const double kInvFact[14] = {
+    1., 1., 1. / 2., 1. / 6., 1. / 24., 1. / 120., 1. / 720., 1. / 5040., 1. / 40320., 1. / 362880.,
+    1. / 3628800., 1. / 39916800., 1. / 479001600., 1. / 6227020800.};
+
+// stumpff_cs3 (src/integrator_whfast.c:189-212).
+__device__ __forceinline__ void stumpff_c3(double cs[4], double z, uint32_t* status) {
+    unsigned n = 0;
+    while (fabs(z) > 0.1) {
+        z = z / 4.;
+        n++;
+        if (n > 1200) { atomicOr(status, DEV_ERR_KEPLER); break; }   // z = inf would never shrink
+    }
+    const int nmax = 13;
+    double co = kInvFact[nmax], ce = kInvFact[nmax - 1];
+#pragma unroll
+    for (int np = nmax - 2; np >= 3; np -= 2) {
+        co = kInvFact[np] - z * co;
+        ce = kInvFact[np - 1] - z * ce;
+    }
+    cs[3] = co;
+    cs[2] = ce;
+    cs[1] = kInvFact[1] - z * co;
+    cs[0] = kInvFact[0] - z * ce;
+    for (; n > 0; n--) {
+        cs[3] = (cs[2] + cs[0] * cs[3]) * 0.25;
+        cs[2] = cs[1] * cs[1] * 0.5;
+        cs[1] = cs[0] * cs[1];
+        cs[0] = 2. * cs[0] * cs[0] - 1.;
+    }
+}
+
+// stiefel_Gs3 (src/integrator_whfast.c:226-232).
+__device__ __forceinline__ void stiefel_g3(double Gs[4], double beta, double X, uint32_t* status) {
+    const double X2 = X * X;
+    stumpff_c3(Gs, beta * X2, status);
+    Gs[1] *= X;
+    Gs[2] *= X2;
+    Gs[3] *= X2 * X;
+}
+
+// reb_integrator_whfast_kepler_solver (src/integrator_whfast.c:241-427) for one body.
+__device__ inline void kepler_solver(double& px, double& py, double& pz, double& pvx, double& pvy, double& pvz,
+                                     double mu, double dt, uint32_t* status) {
+    const double x = px, y = py, z = pz, vx = pvx, vy = pvy, vz = pvz;
+    const double r0 = sqrt(x * x + y * y + z * z);
+    const double r0i = 1. / r0;
+    const double v2 = vx * vx + vy * vy + vz * vz;
+    const double beta = 2. * mu * r0i - v2;
+    const double eta0 = x * vx + y * vy + z * vz;
+    const double zeta0 = mu - beta * r0;
+    double X, Gs[4], invperiod = 0, X_per_period = __longlong_as_double(0x7ff8000000000000LL);
+    if (beta > 0.) {
+        const double sb = sqrt(beta);
+        invperiod = sb * beta / (2. * M_PI * mu);
+        X_per_period = 2. * M_PI / sb;
+        const double dtr0i = dt * r0i;
+        X = dtr0i * (1. - dtr0i * eta0 * 0.5 * r0i);
+    } else {
+        X = 0.;
+    }
+    int converged = 0;
+    double oldX = X;
+    stiefel_g3(Gs, beta, X, status);
+    const double e1 = eta0 * Gs[1] + zeta0 * Gs[2];
+    double ri = 1. / (r0 + e1);
+    X = ri * (X * e1 - eta0 * Gs[2] - zeta0 * Gs[3] + dt);
+    if (fabs(X - oldX) > 0.01 * X_per_period) {
+        // Quartic (Laguerre-type) solver, up to 64 iterations, converged when X repeats.
+        X = beta * dt / mu;
+        double prevX[64];
+        for (int nl = 1; nl < 64; nl++) {
+            stiefel_g3(Gs, beta, X, status);
+            const double f = r0 * X + eta0 * Gs[2] + zeta0 * Gs[3] - dt;
+            const double fp = r0 + eta0 * Gs[1] + zeta0 * Gs[2];
+            const double fpp = eta0 * Gs[0] + zeta0 * Gs[1];
+            const double den = fp + sqrt(fabs(16. * fp * fp - 20. * f * fpp));
+            X = (X * den - 5. * f) / den;
+            for (int i = 1; i < nl; i++) {
+                if (X == prevX[i]) { nl = 64; converged = 1; break; }
+            }
+            if (nl < 64) prevX[nl] = X;
+        }
+        const double e2 = eta0 * Gs[1] + zeta0 * Gs[2];
+        ri = 1. / (r0 + e2);
+    } else {
+        double oldX2;
+        for (int nh = 1; nh < 32; nh++) {
+            oldX2 = oldX;
+            oldX = X;
+            stiefel_g3(Gs, beta, X, status);
+            const double e2 = eta0 * Gs[1] + zeta0 * Gs[2];
+            ri = 1. / (r0 + e2);
+            X = ri * (X * e2 - eta0 * Gs[2] - zeta0 * Gs[3] + dt);
+            if (X == oldX || X == oldX2) { converged = 1; break; }
+        }
+    }
+    if (!converged) {
+        // Bisection fallback (src/integrator_whfast.c:333-370), capped.
+        double Xmin, Xmax;
+        if (beta > 0.) {
+            Xmin = X_per_period * floor(dt * invperiod);
+            Xmax = Xmin + X_per_period;
+        } else {
+            const double h2 = r0 * r0 * v2 - eta0 * eta0;
+            const double q = h2 / mu / (1. + sqrt(1. - h2 * beta / (mu * mu)));
+            const double vq = copysign(sqrt(h2) / q, dt);
+            Xmin = dt / (fabs(vq * dt) + r0);
+            Xmax = dt / q;
+            if (dt < 0.) { const double t = Xmin; Xmin = Xmax; Xmax = t; }
+        }
+        X = (Xmax + Xmin) / 2.;
+        int it = 0;
+        do {
+            stiefel_g3(Gs, beta, X, status);
+            const double s = r0 * X + eta0 * Gs[2] + zeta0 * Gs[3] - dt;
+            if (s >= 0.) Xmax = X; else Xmin = X;
+            X = (Xmax + Xmin) / 2.;
+            if (++it > 4096) { atomicOr(status, DEV_ERR_KEPLER); break; }
+        } while (fabs(Xmax - Xmin) > fabs((Xmax + Xmin) * 1e-15));
+        const double e2 = eta0 * Gs[1] + zeta0 * Gs[2];
+        ri = 1. / (r0 + e2);
+    }
+    if (isnan(ri)) { ri = 0.; Gs[1] = 0.; Gs[2] = 0.; Gs[3] = 0.; }
+    const double f = -mu * Gs[2] * r0i;
+    const double g = dt - mu * Gs[3];
+    const double fd = -mu * Gs[1] * r0i * ri;
+    const double gd = -mu * Gs[2] * ri;
+    px += f * x + g * vx;
+    py += f * y + g * vy;
+    pz += f * z + g * vz;
+    pvx += fd * x + gd * vx;
+    pvy += fd * y + gd * vy;
+    pvz += fd * z + gd * vz;
+}
+
+// reb_transformations_inertial_to_jacobi_posvel (src/transformations.c:34-81).
+template <int NB>
+__device__ __forceinline__ void to_jacobi(const System<NB>& s, Jacobi<NB>& j, int N, int Na) {
+    double eta = s.m[0];
+    double sx = eta * s.x[0], sy = eta * s.y[0], sz = eta * s.z[0];
+    double svx = eta * s.vx[0], svy = eta * s.vy[0], svz = eta * s.vz[0];
+#pragma unroll
+    for (int i = 1; i < NB; i++) {
+        if (i >= Na) break;
+        const double ei = 1. / eta;
+        eta += s.m[i];
+        const double pme = eta * ei;
+        j.m[i] = s.m[i];
+        j.x[i] = s.x[i] - sx * ei; j.y[i] = s.y[i] - sy * ei; j.z[i] = s.z[i] - sz * ei;
+        j.vx[i] = s.vx[i] - svx * ei; j.vy[i] = s.vy[i] - svy * ei; j.vz[i] = s.vz[i] - svz * ei;
+        sx = sx * pme + s.m[i] * j.x[i]; sy = sy * pme + s.m[i] * j.y[i]; sz = sz * pme + s.m[i] * j.z[i];
+        svx = svx * pme + s.m[i] * j.vx[i]; svy = svy * pme + s.m[i] * j.vy[i]; svz = svz * pme + s.m[i] * j.vz[i];
+    }
+    const double ei = 1. / eta;
+#pragma unroll
+    for (int i = 1; i < NB; i++) {
+        if (i < Na || i >= N) continue;
+        j.m[i] = s.m[i];
+        j.x[i] = s.x[i] - sx * ei; j.y[i] = s.y[i] - sy * ei; j.z[i] = s.z[i] - sz * ei;
+        j.vx[i] = s.vx[i] - svx * ei; j.vy[i] = s.vy[i] - svy * ei; j.vz[i] = s.vz[i] - svz * ei;
+    }
+    const double mti = 1. / eta;
+    j.m[0] = eta;
+    j.x[0] = sx * mti; j.y[0] = sy * mti; j.z[0] = sz * mti;
+    j.vx[0] = svx * mti; j.vy[0] = svy * mti; j.vz[0] = svz * mti;
+}
+
+// reb_transformations_jacobi_to_inertial_posvel (src/transformations.c:178-226).
+template <int NB>
+__device__ __forceinline__ void to_inertial(System<NB>& s, const Jacobi<NB>& j, int N, int Na) {
+    double eta = j.m[0];
+    double sx = j.x[0] * eta, sy = j.y[0] * eta, sz = j.z[0] * eta;
+    double svx = j.vx[0] * eta, svy = j.vy[0] * eta, svz = j.vz[0] * eta;
+#pragma unroll
+    for (int i = NB - 1; i >= 1; i--) {
+        if (i >= N || i < Na) continue;
+        const double ei = 1. / eta;
+        s.x[i] = j.x[i] + sx * ei; s.y[i] = j.y[i] + sy * ei; s.z[i] = j.z[i] + sz * ei;
+        s.vx[i] = j.vx[i] + svx * ei; s.vy[i] = j.vy[i] + svy * ei; s.vz[i] = j.vz[i] + svz * ei;
+    }
+#pragma unroll
+    for (int i = NB - 1; i >= 1; i--) {
+        if (i >= Na) continue;
+        const double ei = 1. / eta;
+        const double mi = s.m[i];
+        sx = (sx - mi * j.x[i]) * ei; sy = (sy - mi * j.y[i]) * ei; sz = (sz - mi * j.z[i]) * ei;
+        svx = (svx - mi * j.vx[i]) * ei; svy = (svy - mi * j.vy[i]) * ei; svz = (svz - mi * j.vz[i]) * ei;
+        s.x[i] = j.x[i] + sx; s.y[i] = j.y[i] + sy; s.z[i] = j.z[i] + sz;
+        s.vx[i] = j.vx[i] + svx; s.vy[i] = j.vy[i] + svy; s.vz[i] = j.vz[i] + svz;
+        eta -= mi;
+        sx *= eta; sy *= eta; sz *= eta; svx *= eta; svy *= eta; svz *= eta;
+    }
+    const double mi = 1. / eta;
+    s.x[0] = sx * mi; s.y[0] = sy * mi; s.z[0] = sz * mi;
+    s.vx[0] = svx * mi; s.vy[0] = svy * mi; s.vz[0] = svz * mi;
+}
+
+// Kepler drift of every Jacobi body, serial-eta branch (src/integrator_whfast.c:589-636).
+template <int NB>
+__device__ __forceinline__ void kepler_step(Jacobi<NB>& j, double m0, double G, double dt, int N, int Na,
+                                            uint32_t* status) {
+    double eta = m0;
+#pragma unroll
+    for (int i = 1; i < NB; i++) {
+        if (i >= N) break;
+        if (i < Na) eta += j.m[i];
+        kepler_solver(j.x[i], j.y[i], j.z[i], j.vx[i], j.vy[i], j.vz[i], eta * G, dt, status);
+    }
+}
+
+// reb_integrator_whfast_com_step (src/integrator_whfast.c:638-651).
+template <int NB>
+__device__ __forceinline__ void com_step(Jacobi<NB>& j, double dt) {
+    j.x[0] += dt * j.vx[0];
+    j.y[0] += dt * j.vy[0];
+    j.z[0] += dt * j.vz[0];
+}
+
+// BASIC gravity with gravity_ignore_terms = 1 (skip the 0-1 pair), serial
+// pairwise order (src/gravity.c:195-257, starti = 2, startj = 0).
+template <int NB>
+__device__ __forceinline__ void gravity_01(const System<NB>& s, double ax[NB], double ay[NB], double az[NB],
+                                           double G, double eps2, int N, int Na, int tp) {
+#pragma unroll
+    for (int i = 0; i < NB; i++) { ax[i] = 0.; ay[i] = 0.; az[i] = 0.; }
+#pragma unroll
+    for (int i = 2; i < NB; i++) {
+        if (i >= Na) break;
+#pragma unroll
+        for (int jj = 0; jj < i; jj++) {
+            const double dx = (0. + s.x[i]) - s.x[jj];
+            const double dy = (0. + s.y[i]) - s.y[jj];
+            const double dz = (0. + s.z[i]) - s.z[jj];
+            const double r = sqrt(dx * dx + dy * dy + dz * dz + eps2);
+            const double pf = G / (r * r * r);
+            const double pfj = -pf * s.m[jj];
+            const double pfi = pf * s.m[i];
+            ax[i] += pfj * dx; ay[i] += pfj * dy; az[i] += pfj * dz;
+            ax[jj] += pfi * dx; ay[jj] += pfi * dy; az[jj] += pfi * dz;
+        }
+    }
+    const int st = Na > 2 ? Na : 2;
+#pragma unroll
+    for (int i = 2; i < NB; i++) {
+        if (i < st || i >= N) continue;
+#pragma unroll
+        for (int jj = 0; jj < NB; jj++) {
+            if (jj >= Na) break;
+            const double dx = (0. + s.x[i]) - s.x[jj];
+            const double dy = (0. + s.y[i]) - s.y[jj];
+            const double dz = (0. + s.z[i]) - s.z[jj];
+            const double r = sqrt(dx * dx + dy * dy + dz * dz + eps2);
+            const double pf = G / (r * r * r);
+            const double pfj = -pf * s.m[jj];
+            ax[i] += pfj * dx; ay[i] += pfj * dy; az[i] += pfj * dz;
+            if (tp) {
+                const double pfi = pf * s.m[i];
+                ax[jj] += pfi * dx; ay[jj] += pfi * dy; az[jj] += pfi * dz;
+            }
+        }
+    }
+}
+
+// Interaction (kick) step in Jacobi coordinates: inertial_to_jacobi_acc
+// (src/transformations.c:147-176) then src/integrator_whfast.c:447-472.
+template <int NB>
+__device__ __forceinline__ void interaction_step(Jacobi<NB>& j, const System<NB>& s, const double ax[NB],
+                                                 const double ay[NB], const double az[NB], double G, double dt,
+                                                 int N, int Na) {
+    double jax[NB], jay[NB], jaz[NB];
+    double eta = s.m[0];
+    double sx = eta * ax[0], sy = eta * ay[0], sz = eta * az[0];
+#pragma unroll
+    for (int i = 1; i < NB; i++) {
+        if (i >= Na) break;
+        const double ei = 1. / eta;
+        eta += s.m[i];
+        const double pme = eta * ei;
+        jax[i] = ax[i] - sx * ei; jay[i] = ay[i] - sy * ei; jaz[i] = az[i] - sz * ei;
+        sx = sx * pme + s.m[i] * jax[i]; sy = sy * pme + s.m[i] * jay[i]; sz = sz * pme + s.m[i] * jaz[i];
+    }
+    {
+        const double ei = 1. / eta;
+#pragma unroll
+        for (int i = 1; i < NB; i++) {
+            if (i < Na || i >= N) continue;
+            jax[i] = ax[i] - sx * ei; jay[i] = ay[i] - sy * ei; jaz[i] = az[i] - sz * ei;
+        }
+    }
+    eta = s.m[0];
+#pragma unroll
+    for (int i = 1; i < NB; i++) {
+        if (i >= N) break;
+        const double qx = j.x[i], qy = j.y[i], qz = j.z[i];
+        if (i < Na) eta += j.m[i];
+        j.vx[i] += dt * jax[i];
+        j.vy[i] += dt * jay[i];
+        j.vz[i] += dt * jaz[i];
+        if (i > 1) {
+            const double rj2i = 1. / (qx * qx + qy * qy + qz * qz);
+            const double rji = sqrt(rj2i);
+            const double rj3iM = rji * rj2i * G * eta;
+            const double pf = dt * rj3iM;
+            j.vx[i] += pf * qx;
+            j.vy[i] += pf * qy;
+            j.vz[i] += pf * qz;
+        }
+    }
+}
+
+// One WHFast step with safe_mode = 1 (src/integrator_whfast.c:1113-1259 with
+// the synchronize of :1051-1111): the state enters and leaves synchronized.
+template <int NB>
+__device__ __forceinline__ void step_safe(System<NB>& s, double G, double eps2, double dt, int N, int Na, int tp,
+                                          uint32_t* status) {
+    Jacobi<NB> j;
+    to_jacobi(s, j, N, Na);
+    kepler_step(j, s.m[0], G, dt / 2., N, Na, status);
+    com_step(j, dt / 2.);
+    to_inertial(s, j, N, Na);
+    double ax[NB], ay[NB], az[NB];
+    gravity_01(s, ax, ay, az, G, eps2, N, Na, tp);
+    interaction_step(j, s, ax, ay, az, G, dt, N, Na);
+    kepler_step(j, s.m[0], G, dt / 2., N, Na, status);
+    com_step(j, dt / 2.);
+    to_inertial(s, j, N, Na);
+}
+
+// Total energy (src/tools.c:108-162) of one system.
+template <int NB>
+__device__ __forceinline__ double energy(const System<NB>& s, double G, int N, int Na, int tp) {
+    const int Ni = tp == 0 ? Na : N;
+    double ek = 0., ep = 0.;
+#pragma unroll
+    for (int i = 0; i < NB; i++) {
+        if (i >= Ni) break;
+        ek += 0.5 * s.m[i] * (s.vx[i] * s.vx[i] + s.vy[i] * s.vy[i] + s.vz[i] * s.vz[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < NB; i++) {
+        if (i >= Na) break;
+#pragma unroll
+        for (int jj = i + 1; jj < NB; jj++) {
+            if (jj >= Ni) break;
+            const double dx = s.x[i] - s.x[jj], dy = s.y[i] - s.y[jj], dz = s.z[i] - s.z[jj];
+            ep -= G * s.m[jj] * s.m[i] / sqrt(dx * dx + dy * dy + dz * dz);
+        }
+    }
+    return ek + ep;
+}
+
+}  // namespace wh

