@@ -117,6 +117,15 @@ size_t rgpu_sim_N(const rgpu_sim* sim);
  * REB_GRAVITY_NONE/BASIC/COMPENSATED/TREE (src/gravity.c:47-531). */
 int rgpu_update_acceleration(rgpu_sim* sim);
 
+/* Build the octree for the current positions (src/tree.c:254-271 and
+ * :209-229) and write its cells depth-first (roots by index, octants 0..7) as
+ * 88-byte records {int32 root, int32 depth, uint64 path (3 bits per level),
+ * double x, y, z, w, m, mx, my, mz, int64 pt} -- pt is the particle index of a
+ * leaf or minus the particle count of an internal cell (struct reb_treecell,
+ * src/tree.h:81-103).  Requires root_size > 0.  RGPU_ERR_OVERFLOW if more than
+ * cap cells (the count is still written). */
+int rgpu_tree_export(rgpu_sim* sim, void* cells, size_t cap, size_t* n_cells);
+
 /* Overlapping + approaching pairs for the configured collision mode, in the
  * reference's discovery order, before its random shuffle.  Replaces the search
  * half of reb_collision_search (src/collision.c:49-342).  *n_found receives the

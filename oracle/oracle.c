@@ -1059,3 +1059,29 @@ void orc_gravity_compensated_omp_rows(orc_sim* r, size_t i0, size_t i1) {
         P[i].ax = ax; P[i].ay = ay; P[i].az = az;
     }
 }
+
+/* Tree gravity (src/gravity.c:47-106) for rows [i0, i1) only: same tree and
+ * walk, so a sample of particles can be checked at sizes where the full walk
+ * is too slow on the host. */
+void orc_gravity_tree_rows(orc_sim* r, size_t i0, size_t i1) {
+    otree t = {0};
+    if (tree_build(r, &t)) { tree_free(&t); return; }
+    for (size_t i = 0; i < t.n_root; i++) if (t.root[i]) cell_gravity_data(r, t.root[i]);
+    orc_particle* const P = r->particles;
+    if (i1 > r->N) i1 = r->N;
+#pragma omp parallel for schedule(dynamic)
+    for (size_t i = i0; i < i1; i++) {
+        double ax = 0., ay = 0., az = 0.;
+        for (int gx = -r->N_ghost_x; gx <= r->N_ghost_x; gx++)
+        for (int gy = -r->N_ghost_y; gy <= r->N_ghost_y; gy++)
+        for (int gz = -r->N_ghost_z; gz <= r->N_ghost_z; gz++) {
+            double gb[6];
+            orc_boundary_ghostbox(r, gx, gy, gz, gb);
+            const double sx = gb[0] + P[i].x, sy = gb[1] + P[i].y, sz = gb[2] + P[i].z;
+            for (size_t k = 0; k < t.n_root; k++)
+                if (t.root[k]) cell_accel(r, (long)i, t.root[k], sx, sy, sz, &ax, &ay, &az);
+        }
+        P[i].ax = ax; P[i].ay = ay; P[i].az = az;
+    }
+    tree_free(&t);
+}

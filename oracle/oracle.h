@@ -78,6 +78,7 @@ void orc_gravity_compensated_serial(orc_sim* r);
 void orc_gravity_compensated_omp(orc_sim* r);
 void orc_gravity_compensated_omp_rows(orc_sim* r, size_t i0, size_t i1);
 void orc_gravity_tree(orc_sim* r);
+void orc_gravity_tree_rows(orc_sim* r, size_t i0, size_t i1);
 int  orc_tree_export(orc_sim* r, orc_cell* out, size_t cap, size_t* n_out);
 
 /* Boundary (src/boundary.c). */

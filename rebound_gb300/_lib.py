@@ -18,6 +18,9 @@ PARTICLE_DTYPE = np.dtype([
     ("name", "u8"), ("ap", "u8"), ("sim", "u8")])
 # struct reb_collision (src/rebound.h:144-149), 72 bytes.
 COLLISION_DTYPE = np.dtype([("p1", "u8"), ("p2", "u8"), ("gb", "f8", 6), ("ri", "u8")])
+# Tree cell export record (rgpu_tree_export), 88 bytes.
+CELL_DTYPE = np.dtype([("root", "i4"), ("depth", "i4"), ("path", "u8"), ("x", "f8"), ("y", "f8"), ("z", "f8"),
+                       ("w", "f8"), ("m", "f8"), ("mx", "f8"), ("my", "f8"), ("mz", "f8"), ("pt", "i8")])
 
 RGPU_OK = 0
 ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: "unsupported",
@@ -66,6 +69,7 @@ SIGNATURES = {
     "rgpu_sim_N": (ctypes.c_size_t, [_P]),
     "rgpu_update_acceleration": (ctypes.c_int, [_P]),
     "rgpu_collision_search": (ctypes.c_int, [_P, _P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+    "rgpu_tree_export": (ctypes.c_int, [_P, _P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
     "rgpu_steps": (ctypes.c_int, [_P, ctypes.c_int64]),
     "rgpu_integrate": (ctypes.c_int, [_P, ctypes.c_double]),
     "rgpu_synchronize": (ctypes.c_int, [_P]),

@@ -55,6 +55,14 @@ struct rgpu_sim {
     bool did_modify = true;
     bool whfast_synchronized = true;
     SeiCache sei{};
+    // last collision search result (device), consumed by the resolve stage
+    size_t n_pairs = 0;
+    rgpu_collision* dev_pairs = nullptr;
+    int* pc_count = nullptr;            // direct search: per (ghost box, particle) counts
+    long long* pc_off = nullptr;
+    size_t pc_cap = 0;
+    rgpu_collision* dp_pairs = nullptr; // direct search output
+    size_t dp_cap = 0;
     TreeBuffers* tree = nullptr;
     WhfastBuffers* wh = nullptr;
     std::string msg;
@@ -80,6 +88,7 @@ void tree_free(rgpu_sim* s);
 // collide.cu
 int direct_collisions(rgpu_sim* s, rgpu_collision* out, size_t cap, size_t* n_found, bool device_only);
 int resolve_collisions_device(rgpu_sim* s);
+void collide_free(rgpu_sim* s);
 // whfast.cu
 int whfast_step(rgpu_sim* s);
 int whfast_synchronize(rgpu_sim* s);

@@ -382,6 +382,7 @@ void rgpu_sim_free(rgpu_sim* s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     tree_free(s);
     whfast_free(s);
+    collide_free(s);
     cudaFree(s->soa_block);
     cudaFree(s->jpos);
     cudaFree(s->jsplit);

@@ -199,6 +199,20 @@ class Simulation:
             self._after(rc)
             return out[:n.value]
 
+    def tree_cells(self):
+        """Octree cells (depth-first) for the current positions."""
+        self._push()
+        n = ctypes.c_size_t(0)
+        cap = 4 * self.N + 1024
+        while True:
+            out = np.zeros(cap, dtype=_lib.CELL_DTYPE)
+            rc = self._L.rgpu_tree_export(self._h, out.ctypes.data, cap, ctypes.byref(n))
+            if rc == 9 and n.value > cap:
+                cap = int(n.value)
+                continue
+            check(rc, self._h)
+            return out[:n.value]
+
     def energy(self):
         """reb_simulation_energy (src/tools.c:108)."""
         self._push()

@@ -247,6 +247,7 @@ def fixture_ring():
     # A few full SEI + tree gravity + tree collision + hardsphere steps.
     sim2 = ring_patch(200.0, seed=7)
     sim2.coefficient_of_restitution = lambda s, v: 0.5
+    out["after5_seed0"] = np.int64(sim2.rand_seed)       # shuffle seed when stepping starts
     sim2.steps(5)
     out["after5"] = state(sim2)
     out["after5_t"] = np.float64(sim2.t)

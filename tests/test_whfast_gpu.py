@@ -22,10 +22,12 @@ def max_diff(a, b):
 
 def test_kepler_solver_bit_exact(gpu):
     g = golden("whfast.npz")
-    k = g["kepler_in"]
+    k = np.ascontiguousarray(g["kepler_in"])
+    mu = np.ascontiguousarray(g["kepler_mu"])      # keep the arrays alive across the call
+    dt = np.ascontiguousarray(g["kepler_dt"])
     out = np.zeros((len(k), 6))
-    rc = gpu.load().rgpu_kepler_solve(k.ctypes.data, k.dtype.itemsize, g["kepler_mu"].ctypes.data,
-                                      g["kepler_dt"].ctypes.data, out.ctypes.data, len(k))
+    rc = gpu.load().rgpu_kepler_solve(k.ctypes.data, k.dtype.itemsize, mu.ctypes.data, dt.ctypes.data,
+                                      out.ctypes.data, len(k))
     assert rc == 0
     ref = np.stack([g["kepler_out"][f] for f in XV], axis=1)
     assert np.array_equal(out, ref)
