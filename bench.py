@@ -241,11 +241,15 @@ def run_gb300(args):
 
     # Accuracy and speed of the other forms (force evaluation at step 0).
     forms = {}
-    ref_sim = make("compensated")
-    ref_sim.update_acceleration()
-    a_ref = R.accelerations(ref_sim)
-    del ref_sim
-    for form in ("basic", "compensated", "mixed", "mixed_split"):
+    form_list = () if args.lite else ("basic", "compensated", "mixed", "mixed_split")
+    ref_sim = make("compensated") if form_list else None
+    if ref_sim is None:
+        a_ref = None
+    else:
+        ref_sim.update_acceleration()
+        a_ref = R.accelerations(ref_sim)
+        del ref_sim
+    for form in form_list:
         fs = make(form)
         fh = fs.handle
         R._lib.check(L.rgpu_sim_time_steps(fh, 1, ctypes.byref(ms)), fh)       # warm
@@ -269,8 +273,9 @@ def run_gb300(args):
                        "median_rel_err_vs_compensated": float(np.median(err)),
                        "max_rel_err_vs_compensated": float(err.max())}
         del fs
-    forms["mixed_speedup_vs_fp64"] = forms["mixed"]["gpair_per_s"] / forms["basic"]["gpair_per_s"]
-    forms["mixed_split_speedup_vs_fp64"] = forms["mixed_split"]["gpair_per_s"] / forms["basic"]["gpair_per_s"]
+    if form_list:
+        forms["mixed_speedup_vs_fp64"] = forms["mixed"]["gpair_per_s"] / forms["basic"]["gpair_per_s"]
+        forms["mixed_split_speedup_vs_fp64"] = forms["mixed_split"]["gpair_per_s"] / forms["basic"]["gpair_per_s"]
 
     # End to end through the C ABI: pinned host AoS in, step, AoS out.
     host = torch.empty(n * 112, dtype=torch.uint8, pin_memory=True)
@@ -289,18 +294,20 @@ def run_gb300(args):
            "h2d_bytes_per_step": n * 112, "d2h_bytes_per_step": n * 88}
 
     extra = {}
-    if args.ensemble and rank == 0:
+    if args.ensemble and rank == 0 and not args.lite:
         try:
             from rebound_gb300 import ensemble as E
             extra["ensemble"] = E.bench_summary(quick=args.quick)
         except Exception as ex:  # reported, not hidden
             extra["ensemble"] = {"error": repr(ex)}
-    if args.serve and rank == 0:
-        try:
+    if args.serve and rank == 0 and not args.lite:
+        import importlib.util
+        if importlib.util.find_spec("rebound_gb300.serve") is not None:
             from rebound_gb300 import serve as S
-            extra["serving"] = S.bench_summary(quick=args.quick)
-        except Exception as ex:
-            extra["serving"] = {"error": repr(ex)}
+            try:
+                extra["serving"] = S.bench_summary(quick=args.quick)
+            except Exception as ex:
+                extra["serving"] = {"error": repr(ex)}
 
     if rank == 0:
         cpu_val, cores, sample = oracle_cpu_rate(p, seconds=args.cpu_seconds)
@@ -350,6 +357,8 @@ def main():
     ap.add_argument("--no-ensemble", dest="ensemble", action="store_false")
     ap.add_argument("--no-serve", dest="serve", action="store_false")
     ap.add_argument("--quick", action="store_true")
+    ap.add_argument("--lite", action="store_true",
+                    help="headline FP64 step only (no other forms, ensemble or serving), for profiling runs")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
