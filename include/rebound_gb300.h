@@ -186,6 +186,24 @@ int rgpu_probe_rate(int which, double* ops_per_s);
 int rgpu_kepler_solve(const void* bodies, size_t stride, const double* mu, const double* dt,
                       double* out, size_t n);
 
+/* Direct-sum accelerations that allocate nothing -- for callers that cannot
+ * call cudaMalloc when they need forces (a host framework that owns every
+ * device allocation through its own pool, an embedding process whose
+ * allocator is locked down).  No counterpart in the reference: REBOUND
+ * computes forces on host memory it owns.
+ * x, y, z, m (inputs) and ax, ay, az (outputs) are the caller's DEVICE arrays
+ * of n doubles; stream is a cudaStream_t passed as a plain pointer (NULL for the
+ * default stream); the call is asynchronous on that stream.  gravity is BASIC,
+ * COMPENSATED, MIXED or MIXED_SPLIT; all particles active, no ghost boxes.
+ * Scratch lives in a fixed 10 MiB device array inside the library (held by
+ * every GPU that loads it until exit): n <= 65,536, else RGPU_ERR_CAPACITY.
+ * The first call on each device looks up that array's address with the device
+ * current; make it before any stream capture.  Calls share the array: calls
+ * that overlap on the GPU race and must be serialised by the caller. */
+int rgpu_direct_accel_noalloc(const double* x, const double* y, const double* z, const double* m,
+                              double* ax, double* ay, double* az, int64_t n, double G, double softening,
+                              int gravity, void* stream);
+
 /* ---- batched WHFast ensemble ------------------------------------------ */
 /* Many independent small systems (2..16 bodies each; each one a REBOUND
  * simulation with WHFast, Jacobi coordinates, DEFAULT kernel, safe_mode 1,

@@ -83,6 +83,8 @@ SIGNATURES = {
     "rgpu_l2_flush": (ctypes.c_int, [_P, ctypes.c_size_t]),
     "rgpu_set_kernel_variant": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     "rgpu_probe_rate": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    "rgpu_direct_accel_noalloc": (ctypes.c_int, [_P] * 7 + [ctypes.c_int64, ctypes.c_double, ctypes.c_double,
+                                                            ctypes.c_int, _P]),
     "rgpu_kepler_solve": (ctypes.c_int, [_P, ctypes.c_size_t, _P, _P, _P, ctypes.c_size_t]),
     "rgpu_ensemble_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), _P, ctypes.c_size_t, _P,
                                             ctypes.c_size_t, _P, ctypes.c_double, ctypes.c_int]),

@@ -495,3 +495,112 @@ int direct_energy(rgpu_sim* s, double* e) {
     *e = ek + ep;
     return RGPU_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free direct summation.
+//
+// Some callers cannot allocate device memory at the moment they need forces:
+// a host framework that owns every device allocation through its own pool, a
+// REBOUND build embedded in a process whose allocator is locked down, or code
+// running where cudaMalloc is not allowed.  rgpu_direct_accel_noalloc takes the
+// caller's device arrays for inputs and outputs and keeps its scratch (the
+// packed j-bodies, their float split and the j-split partial sums) in the
+// file-scope device array below, which every GPU that loads the library holds
+// until the process exits.
+//
+// Sizes: at most kNoAllocMaxN particles; the j-range is cut into at most
+// kNoAllocMaxSplits chunks.  Every scratch slot the reduction reads is written
+// earlier in the same call, so nothing needs clearing between calls.  All
+// calls share the one array: calls that overlap on the GPU (different streams,
+// or different host threads) race on it and must be serialised by the caller.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace {
+
+constexpr int kNoAllocMaxN = 65536;
+constexpr int kNoAllocMaxSplits = 4;
+constexpr size_t kNoAllocJpos = (size_t)kNoAllocMaxN * sizeof(double4_32a);       // 2 MiB
+constexpr size_t kNoAllocJsplit = (size_t)kNoAllocMaxN * 2 * sizeof(float4);     // 2 MiB
+constexpr size_t kNoAllocPartial = (size_t)kNoAllocMaxSplits * 3 * kNoAllocMaxN * sizeof(double);  // 6 MiB
+constexpr size_t kNoAllocBytes = kNoAllocJpos + kNoAllocJsplit + kNoAllocPartial;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+void* g_noalloc_addr[kNoAllocMaxDevices] = {nullptr};
+std::mutex g_noalloc_mu;
+
+// Device address of the scratch array on the current device.  Host code cannot
+// use the symbol itself (it names a host-side shadow); the address is looked
+// up once per device with that device current.
+int noalloc_scratch(void** out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return RGPU_ERR_CUDA; }
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return RGPU_ERR_CAPACITY;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || p == nullptr) { cudaGetLastError(); return RGPU_ERR_CUDA; }
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return RGPU_OK;
+}
+
+}  // namespace
+
+extern "C" int rgpu_direct_accel_noalloc(const double* x, const double* y, const double* z, const double* m,
+                                         double* ax, double* ay, double* az, int64_t n, double G,
+                                         double softening, int gravity, void* stream) {
+    if (n < 0 || (n > 0 && (!x || !y || !z || !m || !ax || !ay || !az))) return RGPU_ERR_ARG;
+    if (n > kNoAllocMaxN) return RGPU_ERR_CAPACITY;
+    int mode;
+    switch (gravity) {
+        case RGPU_GRAVITY_BASIC: mode = kBasic; break;
+        case RGPU_GRAVITY_COMPENSATED: mode = kComp; break;
+        case RGPU_GRAVITY_MIXED: mode = kMixed; break;
+        case RGPU_GRAVITY_MIXED_SPLIT: mode = kMixedSplit; break;
+        default: return RGPU_ERR_ARG;
+    }
+    void* base = nullptr;
+    const int rc = noalloc_scratch(&base);      // first call on a device: symbol lookup
+    if (rc) return rc;
+    if (n == 0) return RGPU_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int N = (int)n;
+    double4_32a* jpos = (double4_32a*)base;
+    float4* jsplit = (float4*)((char*)base + kNoAllocJpos);
+    double* partial = (double*)((char*)base + kNoAllocJpos + kNoAllocJsplit);
+
+    ParticlesSoA p{};
+    p.x = const_cast<double*>(x); p.y = const_cast<double*>(y); p.z = const_cast<double*>(z);
+    p.m = const_cast<double*>(m);
+    pack_j<<<grid_for(N, 256), 256, 0, st>>>(p, N, G, jpos, mode == kMixedSplit ? jsplit : nullptr);
+    const int nbi = (N + kBlock - 1) / kBlock;
+    int splits = choose_splits(nbi, N);
+    if (splits > kNoAllocMaxSplits) splits = kNoAllocMaxSplits;
+    DirectArgs a;
+    a.jpos = jpos; a.jsplit = jsplit;
+    a.N = N; a.Na = N; a.tp = 0; a.ign = 0;
+    a.eps2 = softening * softening;
+    a.splits = splits;
+    a.ax = ax; a.ay = ay; a.az = az;
+    a.partial = partial; a.cap = (size_t)kNoAllocMaxN;
+    const dim3 grid(nbi, splits);
+    switch (mode) {
+        case kBasic: launch_mode<kBasic, false>(grid, st, a); break;
+        case kComp: launch_mode<kComp, false>(grid, st, a); break;
+        case kMixed: launch_mode<kMixed, false>(grid, st, a); break;
+        default: launch_mode<kMixedSplit, false>(grid, st, a); break;
+    }
+    if (splits > 1) {
+        if (mode == kComp)
+            reduce_partials<true><<<grid_for(N, 256), 256, 0, st>>>(partial, splits, (size_t)kNoAllocMaxN, N, ax, ay, az);
+        else
+            reduce_partials<false><<<grid_for(N, 256), 256, 0, st>>>(partial, splits, (size_t)kNoAllocMaxN, N, ax, ay, az);
+    }
+    g_launches += splits > 1 ? 3 : 2;
+    return cudaGetLastError() == cudaSuccess ? RGPU_OK : RGPU_ERR_CUDA;
+}
