@@ -38,6 +38,7 @@ extern "C" {
 #define RGPU_ERR_TREE_DEPTH     8   /* octree deeper than the device key supports */
 #define RGPU_ERR_OVERFLOW       9   /* caller's output buffer too small (count is still reported) */
 #define RGPU_ERR_CAPACITY      10   /* request exceeds a fixed capacity of the entry point */
+#define RGPU_ERR_TIMEOUT       11   /* a host-side wait ran out; the request is still in flight */
 
 /* ---- enumerations: values equal REBOUND's enums (src/rebound.h:372-393) -- */
 enum { RGPU_GRAVITY_NONE = 0, RGPU_GRAVITY_BASIC = 1, RGPU_GRAVITY_COMPENSATED = 2,
@@ -231,6 +232,46 @@ int  rgpu_ensemble_get_particles(rgpu_ensemble* ens, void* particles, size_t str
 /* Per-system total energy (src/tools.c:108-162) and time. */
 int  rgpu_ensemble_energy(rgpu_ensemble* ens, double* energies);
 int  rgpu_ensemble_times(rgpu_ensemble* ens, double* t);
+
+/* ---- serving: continuous batching of integrate requests --------------- */
+/* A request is one system the reference would run as one reb_simulation:
+ * RGPU_SERVE_WHFAST: 2..16 bodies, WHFast (Jacobi, DEFAULT kernel, safe_mode 1),
+ *   G = 1, no softening;
+ * RGPU_SERVE_CLUSTER: any N up to the pool, leapfrog (order 2) with the
+ *   mixed-precision direct sum (RGPU_GRAVITY_MIXED_SPLIT), softening given.
+ * A worker thread admits queued requests FIFO while the device bytes of the
+ * resident ones stay within hbm_budget_bytes, and advances every resident
+ * request in batched kernels each tick (WHFast: steps_per_launch steps per
+ * slot; clusters: cluster_steps_per_tick leapfrog steps).  A request's result
+ * does not depend on which other requests share its ticks. */
+enum { RGPU_SERVE_WHFAST = 1, RGPU_SERVE_CLUSTER = 2 };
+typedef struct rgpu_server_config {
+    size_t hbm_budget_bytes;         /* default 120 GiB */
+    int64_t steps_per_launch;        /* WHFast steps per slot per tick (default 256) */
+    int32_t slots_per_bucket;        /* WHFast slots per body count (default 16,384) */
+    int32_t pool_particles;          /* cluster particle pool (default 4,194,304) */
+    int32_t cluster_steps_per_tick;  /* default 8 */
+    int32_t reserved;
+} rgpu_server_config;
+typedef struct rgpu_server_stats {
+    int64_t completed, waiting, resident, ticks;
+    double system_steps;             /* WHFast system-steps + cluster steps done */
+    double pair_interactions;        /* cluster pair interactions done */
+    size_t bytes_in_use;
+} rgpu_server_stats;
+typedef struct rgpu_server rgpu_server;
+void rgpu_server_config_default(rgpu_server_config* cfg);
+int  rgpu_server_create(rgpu_server** out, const rgpu_server_config* cfg);
+void rgpu_server_free(rgpu_server* srv);
+/* Queue one request (records of `stride` bytes as struct reb_particle); thread-safe. */
+int  rgpu_server_submit(rgpu_server* srv, int kind, const void* particles, size_t n, size_t stride, double dt,
+                        int64_t n_steps, double G, double softening, int64_t* request_id);
+/* Wait up to timeout_s for a request; on completion copy its particles out (if
+ * non-NULL), report submit-to-finish latency and forget the request.
+ * RGPU_ERR_TIMEOUT if it is still running (call again). */
+int  rgpu_server_wait(rgpu_server* srv, int64_t request_id, void* particles, size_t stride, double timeout_s,
+                      double* latency_s);
+int  rgpu_server_get_stats(rgpu_server* srv, rgpu_server_stats* out);
 
 /* ---- seeded synthetic workloads (reference RNG conventions) ------------ */
 /* Plummer sphere as reb_simulation_add_plummer (src/tools.c:463-502), keeping

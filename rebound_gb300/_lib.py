@@ -25,7 +25,7 @@ CELL_DTYPE = np.dtype([("root", "i4"), ("depth", "i4"), ("path", "u8"), ("x", "f
 RGPU_OK = 0
 ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: "unsupported",
           5: "non-finite particle", 6: "particle outside box", 7: "duplicate positions in tree",
-          8: "tree too deep", 9: "output overflow", 10: "capacity exceeded"}
+          8: "tree too deep", 9: "output overflow", 10: "capacity exceeded", 11: "timeout"}
 
 GRAVITY = {"none": 0, "basic": 1, "compensated": 2, "tree": 3, "mixed": 64, "mixed_split": 65}
 COLLISION = {"none": 0, "direct": 1, "tree": 2}
@@ -45,6 +45,18 @@ class Config(ctypes.Structure):
         ("gravity", ctypes.c_int32), ("collision", ctypes.c_int32), ("collision_resolve", ctypes.c_int32),
         ("boundary", ctypes.c_int32), ("integrator", ctypes.c_int32), ("whfast_safe_mode", ctypes.c_int32),
         ("rand_seed", ctypes.c_uint32), ("status", ctypes.c_int32), ("collisions_log_n", ctypes.c_int64)]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_size_t), ("steps_per_launch", ctypes.c_int64),
+                ("slots_per_bucket", ctypes.c_int32), ("pool_particles", ctypes.c_int32),
+                ("cluster_steps_per_tick", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("completed", ctypes.c_int64), ("waiting", ctypes.c_int64), ("resident", ctypes.c_int64),
+                ("ticks", ctypes.c_int64), ("system_steps", ctypes.c_double),
+                ("pair_interactions", ctypes.c_double), ("bytes_in_use", ctypes.c_size_t)]
 
 
 class RGPUError(RuntimeError):
@@ -98,6 +110,15 @@ SIGNATURES = {
     "rgpu_ensemble_get_particles": (ctypes.c_int, [_P, _P, ctypes.c_size_t]),
     "rgpu_ensemble_energy": (ctypes.c_int, [_P, _P]),
     "rgpu_ensemble_times": (ctypes.c_int, [_P, _P]),
+    "rgpu_server_config_default": (None, [ctypes.POINTER(ServerConfig)]),
+    "rgpu_server_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ServerConfig)]),
+    "rgpu_server_free": (None, [_P]),
+    "rgpu_server_submit": (ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_double,
+                                          ctypes.c_int64, ctypes.c_double, ctypes.c_double,
+                                          ctypes.POINTER(ctypes.c_int64)]),
+    "rgpu_server_wait": (ctypes.c_int, [_P, ctypes.c_int64, _P, ctypes.c_size_t, ctypes.c_double,
+                                        ctypes.POINTER(ctypes.c_double)]),
+    "rgpu_server_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(ServerStats)]),
     "rgpu_ic_plummer": (ctypes.c_int, [ctypes.c_uint, ctypes.c_size_t, ctypes.c_double, ctypes.c_double,
                                        ctypes.c_double, _P, ctypes.c_size_t]),
     "rgpu_ic_ring_patch": (ctypes.c_int, [ctypes.c_uint] + [ctypes.c_double] * 10 +
