@@ -300,6 +300,11 @@ def run_gb300(args):
             extra["ensemble"] = E.bench_summary(quick=args.quick)
         except Exception as ex:  # reported, not hidden
             extra["ensemble"] = {"error": repr(ex)}
+    if args.tree and rank == 0 and not args.lite:
+        try:
+            extra["tree"] = tree_summary(quick=args.quick)
+        except Exception as ex:
+            extra["tree"] = {"error": repr(ex)}
     if args.serve and rank == 0 and not args.lite:
         import importlib.util
         if importlib.util.find_spec("rebound_gb300.serve") is not None:
@@ -333,6 +338,84 @@ def run_gb300(args):
     return 0
 
 
+def tree_summary(quick=False, steps=3):
+    """Configuration-3 ring patch: SEI, tree gravity (opening angle 0.5, 25 ghost
+    boxes), shear boundary, tree collision search + hardsphere (epsilon 0.5).
+    Device-timed full steps, a split of gravity / collision time, and the oracle
+    (port of the reference's OpenMP tree walk) on a row sample of the same
+    particles for the CPU baseline."""
+    import numpy as np
+    import rebound_gb300 as R
+    from oracle import oracle as O
+    L = R.load()
+    box = 400.0 if quick else 2300.0
+    p = R.ics.ring_patch(box, seed=7)
+    n_root = int(box / 20.0)
+    omega = 1.3143527e-4
+
+    def make():
+        sim = R.Simulation()
+        sim.G, sim.OMEGA, sim.softening = 6.674e-11, omega, 0.1
+        sim.dt = 1e-3 * 2 * np.pi / omega
+        sim.configure_box(20.0, n_root, n_root, 1)
+        sim.configure_ghostboxes(2, 2, 0)
+        sim.opening_angle2 = 0.25
+        sim.boundary, sim.gravity, sim.integrator = "shear", "tree", "sei"
+        sim.collision, sim.collision_resolve = "tree", "hardsphere"
+        sim.coefficient_of_restitution = 0.5
+        sim.add(p)
+        return sim
+
+    sim = make()
+    h = sim.handle
+    ms = ctypes.c_double(0)
+    R._lib.check(L.rgpu_sim_time_steps(h, 1, ctypes.byref(ms)), h)        # warm-up
+    times = []
+    for _ in range(steps):
+        R._lib.check(L.rgpu_sim_time_steps(h, 1, ctypes.byref(ms)), h)
+        times.append(ms.value)
+    step_s = sum(times) / len(times) / 1e3
+    g = make()
+    g.collision = "none"
+    gh = g.handle
+    t0 = time.perf_counter()
+    R._lib.check(L.rgpu_update_acceleration(gh), gh)
+    grav_s = time.perf_counter() - t0
+    c = make()
+    ch = c.handle
+    n = ctypes.c_size_t(0)
+    out = np.zeros(max(1024, 4 * len(p)), dtype=R.COLLISION_DTYPE)
+    t0 = time.perf_counter()
+    R._lib.check(L.rgpu_collision_search(ch, out.ctypes.data, len(out), ctypes.byref(n)), ch)
+    coll_s = time.perf_counter() - t0
+    # CPU baseline: oracle tree walk (OpenMP over particles) on a row sample
+    orc = O.Sim(p, G=6.674e-11, softening=0.1, boundary="shear", root_size=20.0, N_root=(n_root, n_root, 1),
+                N_ghost=(2, 2, 0), OMEGA=omega, opening_angle2=0.25)
+    rows = 64 if quick else 256
+    t0 = time.perf_counter()
+    O.lib().orc_gravity_tree_rows(orc.ref, 0, rows)
+    cpu_rows_s = time.perf_counter() - t0
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    cpu_grav_step_s = cpu_rows_s / rows * len(p)
+    return {"workload": f"ring patch {box:.0f} m box, N={len(p)}, 25 ghost boxes, {n_root * n_root} roots",
+            "N": len(p), "gpu_step_s": step_s, "gpu_tree_gravity_s": grav_s, "gpu_collision_search_s": coll_s,
+            "pairs_found": int(n.value), "steps_per_s": 1.0 / step_s,
+            "cpu_baseline": {"tree_gravity_s_per_step_est": cpu_grav_step_s, "cores": cores, "kind": "port",
+                             "sample": f"{rows} of {len(p)} particles walked (oracle tree, OpenMP), scaled to N"},
+            "gravity_speedup_vs_cpu": cpu_grav_step_s / grav_s}
+
+
+def ensemble_only(args):
+    from rebound_gb300 import ensemble as E
+    import numpy as np
+    systems, periods = __import__("rebound_gb300").ics.planetary_systems(args.ens_systems, seed=3)
+    ens = E.Ensemble(systems, periods / 20.0, exact=bool(args.ens_exact))
+    ens.set_launch(args.ens_block, args.ens_steps)
+    ms = ens.time_steps(args.ens_steps)
+    return {"systems": args.ens_systems, "steps": args.ens_steps, "block": args.ens_block,
+            "system_steps_per_s": args.ens_systems * args.ens_steps / (ms * 1e-3)}
+
+
 def profiled_traffic():
     """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if present."""
     path = os.path.join(REPO, "profiles", "direct_basic_fp64.md")
@@ -356,7 +439,14 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=3.0)
     ap.add_argument("--no-ensemble", dest="ensemble", action="store_false")
     ap.add_argument("--no-serve", dest="serve", action="store_false")
+    ap.add_argument("--no-tree", dest="tree", action="store_false")
     ap.add_argument("--quick", action="store_true")
+    ap.add_argument("--only", choices=["tree", "ensemble", "serve"], default=None,
+                    help="run one secondary workload alone and print its summary")
+    ap.add_argument("--ens-systems", type=int, default=8192)
+    ap.add_argument("--ens-steps", type=int, default=20)
+    ap.add_argument("--ens-block", type=int, default=128)
+    ap.add_argument("--ens-exact", type=int, default=0)
     ap.add_argument("--lite", action="store_true",
                     help="headline FP64 step only (no other forms, ensemble or serving), for profiling runs")
     args = ap.parse_args()
@@ -364,6 +454,17 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.only:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        if args.only == "tree":
+            print(json.dumps({"tree": tree_summary(quick=args.quick)}), flush=True)
+        elif args.only == "ensemble":
+            print(json.dumps({"ensemble": ensemble_only(args)}), flush=True)
+        else:
+            from rebound_gb300 import serve as S
+            print(json.dumps({"serving": S.bench_summary(quick=args.quick)}), flush=True)
+        return 0
     return run_gb300(args)
 
 

@@ -219,7 +219,7 @@ int  rgpu_ensemble_create(rgpu_ensemble** out, const void* particles, size_t str
                           size_t n_systems, const double* dts, double G, int exact);
 void rgpu_ensemble_free(rgpu_ensemble* ens);
 const char* rgpu_ensemble_last_error(const rgpu_ensemble* ens);
-/* CTA size (32/64/128/256) and steps fused per kernel launch. */
+/* CTA size (32/64/128) of the persistent grid and steps fused per kernel launch. */
 int  rgpu_ensemble_set_launch(rgpu_ensemble* ens, int block, int64_t steps_per_launch);
 /* Advance every system by n steps (CUDA-graph replays of fused chunks). */
 int  rgpu_ensemble_steps(rgpu_ensemble* ens, int64_t n);

@@ -3,12 +3,13 @@
 // advanced together on one GPU.
 //
 // Systems are grouped into buckets by body count; each bucket is a
-// structure-of-arrays block [field][body][system] in HBM and is advanced by its
-// own kernel instantiation (one thread per system, fully unrolled over bodies).
-// Buckets run concurrently on separate streams; a chunk of `steps_per_launch`
-// steps per kernel is captured once into a CUDA graph (fork/join over the
-// bucket streams) and replayed.  An autotuner picks the CTA size and the steps
-// per launch by timing short runs.
+// structure-of-arrays block [field][body][system] in HBM.  One thread advances
+// one system (fully unrolled over bodies).  A persistent grid sized to the
+// GPU's resident capacity drains a queue of 32-system work units ordered
+// largest body count first, so every SM stays busy until the cheapest units at
+// the end.  A chunk of `steps_per_launch` steps (counter reset + persistent
+// launch) is captured once into a CUDA graph and replayed.  An autotuner picks
+// the CTA size by timing short runs.
 #define ENSEMBLE_NS ens_fast
 #include "ensemble_kernels.cuh"
 #include <algorithm>
@@ -17,7 +18,7 @@
 #include <new>
 #include <vector>
 
-void* ensemble_exact_steps_fn(int nb);
+void* ensemble_exact_persistent_fn();
 void* ensemble_exact_energy_fn(int nb);
 
 struct EnsBucket {
@@ -42,6 +43,9 @@ struct rgpu_ensemble {
     uint32_t* d_status = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr, fork = nullptr;
     std::vector<cudaEvent_t> joins;
+    ens_fast::Unit* d_units = nullptr;   // work units, largest body count first
+    int n_units = 0;
+    unsigned int* d_counter = nullptr;
     cudaGraphExec_t graph = nullptr;
     int64_t graph_steps = -1;
     int graph_block = -1;
@@ -59,29 +63,37 @@ int ens_err(rgpu_ensemble* e, int code, const std::string& m) {
     return ens_err((e), _x == cudaErrorMemoryAllocation ? RGPU_ERR_NOMEM : RGPU_ERR_CUDA, \
                    std::string(#expr) + ": " + cudaGetErrorString(_x)); } } while (0)
 
-typedef void (*StepsFn)(double*, const double*, double*, int, int, double, uint32_t*);
 typedef void (*EnergyFn)(const double*, int, double, double*);
 
-StepsFn steps_fn(const rgpu_ensemble* e, int nb) {
-    return e->exact ? (StepsFn)ensemble_exact_steps_fn(nb) : ens_fast::steps_for(nb);
-}
 EnergyFn energy_fn(const rgpu_ensemble* e, int nb) {
     return e->exact ? (EnergyFn)ensemble_exact_energy_fn(nb) : ens_fast::energy_for(nb);
 }
 
-// Enqueue one chunk of `n` steps for every bucket (fork/join over bucket streams).
+typedef void (*PersistentFn)(const ens_fast::Unit*, int, int, double, unsigned int*, uint32_t*);
+
+PersistentFn persistent_fn(const rgpu_ensemble* e) {
+    return e->exact ? (PersistentFn)ensemble_exact_persistent_fn() : ens_fast::persistent_kernel;
+}
+
+// Enqueue one chunk of `n` steps for every system: the unit counter is reset and
+// a persistent grid (all SMs, occupancy-limited) drains the unit queue.
 int enqueue_chunk(rgpu_ensemble* e, int n) {
-    ENS_CUDA(e, cudaEventRecord(e->fork, e->stream));
-    for (size_t k = 0; k < e->b.size(); k++) {
-        EnsBucket& B = e->b[k];
-        ENS_CUDA(e, cudaStreamWaitEvent(B.stream, e->fork, 0));
-        StepsFn f = steps_fn(e, B.nb);
-        const unsigned grid = (unsigned)((B.count + e->block - 1) / e->block);
-        f<<<grid, e->block, 0, B.stream>>>(B.st, B.dt, B.t, B.count, n, e->G, e->d_status);
-        g_launches++;
-        ENS_CUDA(e, cudaEventRecord(e->joins[k], B.stream));
-        ENS_CUDA(e, cudaStreamWaitEvent(e->stream, e->joins[k], 0));
+    PersistentFn f = persistent_fn(e);
+    int dev = 0, nsm = 1, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, e->block, 0) != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
     }
+    const int warps_needed = e->n_units;
+    int grid = nsm * per_sm;
+    const int warps_per_block = e->block / 32;
+    grid = std::max(1, std::min(grid, (warps_needed + warps_per_block - 1) / warps_per_block));
+    ENS_CUDA(e, cudaMemsetAsync(e->d_counter, 0, sizeof(unsigned int), e->stream));
+    f<<<grid, e->block, 0, e->stream>>>(e->d_units, e->n_units, n, e->G, e->d_counter, e->d_status);
+    g_launches++;
+    ENS_CUDA(e, cudaGetLastError());
     return RGPU_OK;
 }
 
@@ -189,6 +201,19 @@ int rgpu_ensemble_create(rgpu_ensemble** out, const void* particles, size_t stri
         cudaEventCreateWithFlags(&j, cudaEventDisableTiming);
         e->joins.push_back(j);
     }
+    if (!rc) {
+        std::vector<ens_fast::Unit> units;
+        for (auto it = e->b.rbegin(); it != e->b.rend(); ++it)          // largest body count first
+            for (int f = 0; f < it->count; f += 32)
+                units.push_back(ens_fast::Unit{it->st, it->dt, it->t, it->count, it->nb, f, 0});
+        e->n_units = (int)units.size();
+        if (cudaMalloc(&e->d_units, sizeof(ens_fast::Unit) * units.size()) != cudaSuccess ||
+            cudaMalloc(&e->d_counter, sizeof(unsigned int)) != cudaSuccess) {
+            rc = RGPU_ERR_NOMEM;
+        } else {
+            cudaMemcpy(e->d_units, units.data(), sizeof(ens_fast::Unit) * units.size(), cudaMemcpyHostToDevice);
+        }
+    }
     if (rc) { rgpu_ensemble_free(e); return rc; }
     *out = e;
     return RGPU_OK;
@@ -204,6 +229,8 @@ void rgpu_ensemble_free(rgpu_ensemble* e) {
         if (B.stream) cudaStreamDestroy(B.stream);
     }
     for (auto j : e->joins) cudaEventDestroy(j);
+    cudaFree(e->d_units);
+    cudaFree(e->d_counter);
     if (e->fork) cudaEventDestroy(e->fork);
     if (e->e0) cudaEventDestroy(e->e0);
     if (e->e1) cudaEventDestroy(e->e1);
@@ -215,7 +242,7 @@ void rgpu_ensemble_free(rgpu_ensemble* e) {
 const char* rgpu_ensemble_last_error(const rgpu_ensemble* e) { return e ? e->msg.c_str() : "null handle"; }
 
 int rgpu_ensemble_set_launch(rgpu_ensemble* e, int block, int64_t steps_per_launch) {
-    if (!e || (block != 32 && block != 64 && block != 128 && block != 256) || steps_per_launch < 1) return RGPU_ERR_ARG;
+    if (!e || (block != 32 && block != 64 && block != 128) || steps_per_launch < 1) return RGPU_ERR_ARG;
     e->block = block;
     e->steps_per_launch = steps_per_launch;
     return RGPU_OK;
@@ -246,10 +273,10 @@ int rgpu_ensemble_time_steps(rgpu_ensemble* e, int64_t n, double* ms) {
 int rgpu_ensemble_autotune(rgpu_ensemble* e, int64_t probe_steps, int64_t max_steps_per_launch,
                            int* best_block, double* best_ms_per_step) {
     if (!e || probe_steps < 1 || max_steps_per_launch < 1) return RGPU_ERR_ARG;
-    const int blocks[4] = {32, 64, 128, 256};
+    const int blocks[3] = {32, 64, 128};
     double best = 1e300;
     int bb = e->block;
-    for (int k = 0; k < 4; k++) {
+    for (int k = 0; k < 3; k++) {
         e->block = blocks[k];
         e->steps_per_launch = probe_steps;
         double ms = 0.;

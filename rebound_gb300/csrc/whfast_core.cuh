@@ -231,7 +231,10 @@ template <int NB>
 __device__ __forceinline__ void kepler_step(Jacobi<NB>& j, double m0, double G, double dt, int N, int Na,
                                             uint32_t* status) {
     double eta = m0;
-#pragma unroll
+    // Rolled on purpose: one copy of the solver per instantiation keeps code
+    // size and compile time bounded (the Jacobi arrays then live in L1-cached
+    // local memory, cheap next to the solver's FP64 work).
+#pragma unroll 1
     for (int i = 1; i < NB; i++) {
         if (i >= N) break;
         if (i < Na) eta += j.m[i];
