@@ -377,10 +377,30 @@ def tree_summary(quick=False, steps=3):
     step_s = sum(times) / len(times) / 1e3
     g = make()
     g.collision = "none"
-    gh = g.handle
     t0 = time.perf_counter()
-    R._lib.check(L.rgpu_update_acceleration(gh), gh)
+    g.update_acceleration()                 # returns after the device status is read (synchronous)
     grav_s = time.perf_counter() - t0
+    # split mode: exact near-window walk + mixed-precision far-root sweep
+    sp = make()
+    sp.gravity = "tree_split"
+    sp.collision = "none"
+    sp.update_acceleration()
+    t0 = time.perf_counter()
+    sp.update_acceleration()
+    split_s = time.perf_counter() - t0
+    a_split = R.accelerations(sp)
+    a_exact = R.accelerations(g)
+    den = np.linalg.norm(a_exact, axis=1)
+    split_err = np.linalg.norm(a_split - a_exact, axis=1) / np.where(den > 0, den, 1)
+    sp2 = make()
+    sp2.gravity = "tree_split"
+    h2 = sp2.handle
+    R._lib.check(L.rgpu_sim_time_steps(h2, 1, ctypes.byref(ms)), h2)
+    split_step = []
+    for _ in range(steps):
+        R._lib.check(L.rgpu_sim_time_steps(h2, 1, ctypes.byref(ms)), h2)
+        split_step.append(ms.value)
+    split_step_s = sum(split_step) / len(split_step) / 1e3
     c = make()
     ch = c.handle
     n = ctypes.c_size_t(0)
@@ -399,10 +419,15 @@ def tree_summary(quick=False, steps=3):
     cpu_grav_step_s = cpu_rows_s / rows * len(p)
     return {"workload": f"ring patch {box:.0f} m box, N={len(p)}, 25 ghost boxes, {n_root * n_root} roots",
             "N": len(p), "gpu_step_s": step_s, "gpu_tree_gravity_s": grav_s, "gpu_collision_search_s": coll_s,
+            "split_mode": {"gpu_step_s": split_step_s, "gpu_tree_gravity_s": split_s,
+                           "steps_per_s": 1.0 / split_step_s,
+                           "median_rel_diff_vs_exact_walk": float(np.median(split_err)),
+                           "max_rel_diff_vs_exact_walk": float(split_err.max())},
             "pairs_found": int(n.value), "steps_per_s": 1.0 / step_s,
             "cpu_baseline": {"tree_gravity_s_per_step_est": cpu_grav_step_s, "cores": cores, "kind": "port",
                              "sample": f"{rows} of {len(p)} particles walked (oracle tree, OpenMP), scaled to N"},
-            "gravity_speedup_vs_cpu": cpu_grav_step_s / grav_s}
+            "gravity_speedup_vs_cpu": cpu_grav_step_s / grav_s,
+            "split_gravity_speedup_vs_cpu": cpu_grav_step_s / split_s}
 
 
 def ensemble_only(args):

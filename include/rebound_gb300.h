@@ -46,7 +46,12 @@ enum { RGPU_GRAVITY_NONE = 0, RGPU_GRAVITY_BASIC = 1, RGPU_GRAVITY_COMPENSATED =
        /* GB300 additions: FP64 displacement, FP32 rsqrt/force, compensated FP32-pair
         * accumulation (MIXED); the same with the FP64 displacement formed exactly
         * from a two-float split of each coordinate (MIXED_SPLIT). */
-       RGPU_GRAVITY_MIXED = 64, RGPU_GRAVITY_MIXED_SPLIT = 65 };
+       RGPU_GRAVITY_MIXED = 64, RGPU_GRAVITY_MIXED_SPLIT = 65,
+       /* TREE with the work split: roots within ceil(1/theta)+1 root widths of a
+        * particle are walked exactly as the reference does; every other root is
+        * provably never opened and its monopole is summed by a tiled sweep in
+        * mixed precision (FP64 displacement via two-float splits, FP32 force). */
+       RGPU_GRAVITY_TREE_SPLIT = 66 };
 enum { RGPU_COLLISION_NONE = 0, RGPU_COLLISION_DIRECT = 1, RGPU_COLLISION_TREE = 2 };
 enum { RGPU_BOUNDARY_NONE = 0, RGPU_BOUNDARY_OPEN = 1, RGPU_BOUNDARY_PERIODIC = 2, RGPU_BOUNDARY_SHEAR = 3 };
 enum { RGPU_INTEGRATOR_LEAPFROG = 0, RGPU_INTEGRATOR_SEI = 1, RGPU_INTEGRATOR_WHFAST = 2 };

@@ -27,7 +27,7 @@ ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: 
           5: "non-finite particle", 6: "particle outside box", 7: "duplicate positions in tree",
           8: "tree too deep", 9: "output overflow", 10: "capacity exceeded", 11: "timeout"}
 
-GRAVITY = {"none": 0, "basic": 1, "compensated": 2, "tree": 3, "mixed": 64, "mixed_split": 65}
+GRAVITY = {"none": 0, "basic": 1, "compensated": 2, "tree": 3, "mixed": 64, "mixed_split": 65, "tree_split": 66}
 COLLISION = {"none": 0, "direct": 1, "tree": 2}
 BOUNDARY = {"none": 0, "open": 1, "periodic": 2, "shear": 3}
 INTEGRATOR = {"leapfrog": 0, "sei": 1, "whfast": 2}

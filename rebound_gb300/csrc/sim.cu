@@ -266,6 +266,7 @@ int update_acceleration(rgpu_sim* s) {
         case RGPU_GRAVITY_MIXED_SPLIT:
             return direct_accel(s, s->cfg.gravity);
         case RGPU_GRAVITY_TREE:
+        case RGPU_GRAVITY_TREE_SPLIT:
             return tree_accel(s);
         default:
             return set_error(s, RGPU_ERR_ARG, "Gravity module not found.");
@@ -402,7 +403,7 @@ const char* rgpu_sim_last_error(const rgpu_sim* s) { return s ? s->msg.c_str() :
 
 int rgpu_sim_configure(rgpu_sim* s, const rgpu_config* c) {
     if (!s || !c) return RGPU_ERR_ARG;
-    if (c->gravity == RGPU_GRAVITY_TREE || c->collision == RGPU_COLLISION_TREE) {
+    if (c->gravity == RGPU_GRAVITY_TREE || c->gravity == RGPU_GRAVITY_TREE_SPLIT || c->collision == RGPU_COLLISION_TREE) {
         if (c->root_size <= 0.0)
             return set_error(s, RGPU_ERR_ARG, "Set root_size to a finite value to use a tree based gravity or collision solver.");
     }

@@ -51,6 +51,8 @@ struct TreeBuffers {
     rgpu_collision* pairs = nullptr;
     size_t pairs_cap = 0;
     double* r_top = nullptr;        // per-block top-2 radii
+    void* sweep = nullptr;          // split mode: per-root monopole records
+    size_t sweep_cap = 0;
 };
 
 namespace {
@@ -359,6 +361,136 @@ __global__ void __launch_bounds__(128) walk_exact(ParticlesSoA p, int N, CellArr
         }
     }
     p.ax[i] = ax; p.ay[i] = ay; p.az[i] = az;
+}
+
+// --- split mode: near-window walk + far-root monopole sweep ----------------------------
+// A root whose index differs from the shifted particle's (virtual) root index by
+// more than K = ceil(1/theta) + 1 in any direction lies at least K-1 >= 1/theta
+// root widths away, so the opening test w^2 > theta^2 r^2 (src/tree.c:285) fails
+// for it and the reference uses exactly its monopole.  The split mode walks the
+// window |offset| <= K with the reference's FP64 descent and sweeps all other
+// roots as monopoles in a tiled kernel: FP64 displacement formed from two-float
+// splits, FP32 force, compensated FP32 accumulation.
+struct RootSweep {
+    float4 hi;      // COM (hi split) and G m (float)
+    float4 lo;      // COM (lo split)
+    int4 meta;      // root ix, iy, iz, leaf particle index (or -1)
+};
+
+__global__ void build_root_sweep(CellArrays c, int n_root, BoxGeom g, double G, RootSweep* __restrict__ out) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_root) return;
+    const bool empty = c.pt[r] == INT_MIN;
+    const double mx = empty ? 0. : c.mx[r], my = empty ? 0. : c.my[r], mz = empty ? 0. : c.mz[r];
+    const double gm = empty ? 0. : G * c.m[r];
+    const float hx = (float)mx, hy = (float)my, hz = (float)mz;
+    RootSweep s;
+    s.hi = make_float4(hx, hy, hz, (float)gm);
+    s.lo = make_float4((float)(mx - (double)hx), (float)(my - (double)hy), (float)(mz - (double)hz), 0.f);
+    s.meta = make_int4(r % g.nx, (r / g.nx) % g.ny, r / (g.nx * g.ny), (!empty && c.pt[r] >= 0) ? c.pt[r] : -1);
+    out[r] = s;
+}
+
+__device__ __forceinline__ void virtual_root(const BoxGeom& g, double sx, double sy, double sz, int& ix, int& iy,
+                                             int& iz) {
+    ix = (int)floor((sx + g.bx / 2.) / g.root_size);
+    iy = (int)floor((sy + g.by / 2.) / g.root_size);
+    iz = (int)floor((sz + g.bz / 2.) / g.root_size);
+}
+
+__global__ void __launch_bounds__(128) walk_near(ParticlesSoA p, int N, CellArrays c, BoxGeom geo,
+                                                 const GhostArr* __restrict__ gh, double G, double eps2, double oa2,
+                                                 int K, uint32_t* status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    int stack[kStack];
+    double ax = 0., ay = 0., az = 0.;
+    const double px = p.x[i], py = p.y[i], pz = p.z[i];
+    for (int g = 0; g < gh->n; g++) {
+        const double sx = gh->off[g][0] + px, sy = gh->off[g][1] + py, sz = gh->off[g][2] + pz;
+        int ixv, iyv, izv;
+        virtual_root(geo, sx, sy, sz, ixv, iyv, izv);
+        const int x0 = max(0, ixv - K), x1 = min(geo.nx - 1, ixv + K);
+        const int y0 = max(0, iyv - K), y1 = min(geo.ny - 1, iyv + K);
+        const int z0 = max(0, izv - K), z1 = min(geo.nz - 1, izv + K);
+        for (int rk = z0; rk <= z1; rk++)
+        for (int rj = y0; rj <= y1; rj++)
+        for (int ri = x0; ri <= x1; ri++) {
+            const int r = (rk * geo.ny + rj) * geo.nx + ri;
+            if (c.pt[r] == INT_MIN) continue;
+            int sp = 0;
+            stack[sp++] = r;
+            while (sp > 0) {
+                const int q = stack[--sp];
+                const double dx = sx - c.mx[q], dy = sy - c.my[q], dz = sz - c.mz[q];
+                const double r2 = dx * dx + dy * dy + dz * dz;
+                const int pt = c.pt[q];
+                if (pt < 0) {
+                    const double w = c.w[q];
+                    if (w * w > oa2 * r2) {
+                        const int f = c.first[q], n = c.nchild[q];
+                        if (sp + n > kStack) { atomicOr(status, DEV_ERR_STACK); sp = 0; break; }
+                        for (int k = n - 1; k >= 0; k--) stack[sp++] = f + k;
+                        continue;
+                    }
+                } else if (pt == i) {
+                    continue;
+                }
+                const double rr = sqrt(r2 + eps2);
+                const double pf = -G / (rr * rr * rr) * c.m[q];
+                ax += pf * dx; ay += pf * dy; az += pf * dz;
+            }
+        }
+    }
+    p.ax[i] = ax; p.ay[i] = ay; p.az[i] = az;
+}
+
+constexpr int kSweepTile = 256;
+
+__global__ void __launch_bounds__(kSweepTile) sweep_far(ParticlesSoA p, int N, const RootSweep* __restrict__ roots,
+                                                        int n_root, BoxGeom geo, const GhostArr* __restrict__ gh,
+                                                        double eps2, int K) {
+    __shared__ RootSweep tile[kSweepTile];
+    const int i = blockIdx.x * kSweepTile + threadIdx.x;
+    const bool live = i < N;
+    const double px = live ? p.x[i] : 0., py = live ? p.y[i] : 0., pz = live ? p.z[i] : 0.;
+    const float e2 = (float)eps2;
+    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+    for (int rt = 0; rt < n_root; rt += kSweepTile) {
+        __syncthreads();
+        const int rl = rt + threadIdx.x;
+        if (rl < n_root) tile[threadIdx.x] = roots[rl];
+        __syncthreads();
+        const int nt = min(kSweepTile, n_root - rt);
+        for (int g = 0; g < gh->n; g++) {
+            const double gx = gh->off[g][0] + px, gy = gh->off[g][1] + py, gz = gh->off[g][2] + pz;
+            int ixv, iyv, izv;
+            virtual_root(geo, gx, gy, gz, ixv, iyv, izv);
+            const float hx = (float)gx, hy = (float)gy, hz = (float)gz;
+            const float lx = (float)(gx - (double)hx), ly = (float)(gy - (double)hy), lz = (float)(gz - (double)hz);
+            for (int k = 0; k < nt; k++) {
+                const RootSweep R = tile[k];
+                const bool near = abs(R.meta.x - ixv) <= K && abs(R.meta.y - iyv) <= K && abs(R.meta.z - izv) <= K;
+                const bool self = R.meta.w == i;          // a single-particle root holding i itself
+                // displacement root - particle (the force on i points along it)
+                const float dx = (R.hi.x - hx) + (R.lo.x - lx);
+                const float dy = (R.hi.y - hy) + (R.lo.y - ly);
+                const float dz = (R.hi.z - hz) + (R.lo.z - lz);
+                const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, e2)));
+                const float ri = rsqrtf(r2);
+                float s = R.hi.w * ri * ri * ri;
+                s = (near || self) ? 0.f : s;
+                float t, y;
+                y = fmaf(s, dx, -cx); t = sx + y; cx = (t - sx) - y; sx = t;
+                y = fmaf(s, dy, -cy); t = sy + y; cy = (t - sy) - y; sy = t;
+                y = fmaf(s, dz, -cz); t = sz + y; cz = (t - sz) - y; sz = t;
+            }
+        }
+    }
+    if (!live) return;
+    p.ax[i] += (double)sx - (double)cx;
+    p.ay[i] += (double)sy - (double)cy;
+    p.az[i] += (double)sz - (double)cz;
 }
 
 // --- collision search (src/collision.c:197-269, :422-503) ----------------------------
@@ -670,11 +802,38 @@ int tree_accel(rgpu_sim* s) {
     RGPU_TRY(read_status(s));
     const rgpu_config& cf = s->cfg;
     RGPU_TRY(upload_ghosts(s, cf.N_ghost_x, cf.N_ghost_y, cf.N_ghost_z));
+    TreeBuffers* t = s->tree;
+    const double eps2 = cf.softening * cf.softening;
+    if (cf.gravity != RGPU_GRAVITY_TREE_SPLIT) {
+        ktimer_begin(s);
+        walk_exact<<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, arrays(t), t->n_root, g_ghosts, cf.G, eps2,
+                                                             cf.opening_angle2, s->d_status);
+        ktimer_end(s);
+        g_launches++;
+        RGPU_CUDA(s, cudaGetLastError());
+        return RGPU_OK;
+    }
+    // Split mode: near-window walk (reference semantics) + far-root monopole sweep.
+    if (!(cf.opening_angle2 > 0.))
+        return set_error(s, RGPU_ERR_ARG, "split tree mode needs opening_angle2 > 0");
+    const int K = (int)ceil(1.0 / sqrt(cf.opening_angle2)) + 1;
+    int n_root = 0;
+    const BoxGeom geo = geometry(cf, &n_root);
+    if ((size_t)n_root > t->sweep_cap) {
+        cudaFree(t->sweep);
+        t->sweep = nullptr;
+        t->sweep_cap = 0;
+        RGPU_CUDA(s, cudaMalloc(&t->sweep, sizeof(RootSweep) * n_root));
+        t->sweep_cap = (size_t)n_root;
+    }
+    RootSweep* sw = (RootSweep*)t->sweep;
+    build_root_sweep<<<grid_for(n_root, kB), kB, 0, s->stream>>>(arrays(t), n_root, geo, cf.G, sw);
+    walk_near<<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, arrays(t), geo, g_ghosts, cf.G, eps2,
+                                                        cf.opening_angle2, K, s->d_status);
     ktimer_begin(s);
-    walk_exact<<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, arrays(s->tree), s->tree->n_root, g_ghosts, cf.G,
-                                                         cf.softening * cf.softening, cf.opening_angle2, s->d_status);
+    sweep_far<<<grid_for(N, kSweepTile), kSweepTile, 0, s->stream>>>(s->p, N, sw, n_root, geo, g_ghosts, eps2, K);
     ktimer_end(s);
-    g_launches++;
+    g_launches += 3;
     RGPU_CUDA(s, cudaGetLastError());
     return RGPU_OK;
 }
@@ -735,7 +894,7 @@ void tree_free(rgpu_sim* s) {
     free_cells(t);
     cudaFree(t->keys); cudaFree(t->keys_alt); cudaFree(t->idx); cudaFree(t->idx_alt);
     cudaFree(t->hist); cudaFree(t->counter); cudaFree(t->pair_count); cudaFree(t->pair_off);
-    cudaFree(t->pairs); cudaFree(t->r_top);
+    cudaFree(t->pairs); cudaFree(t->r_top); cudaFree(t->sweep);
     delete t;
     s->tree = nullptr;
 }
