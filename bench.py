@@ -338,7 +338,7 @@ def run_gb300(args):
     return 0
 
 
-def tree_summary(quick=False, steps=3):
+def tree_summary(quick=False, steps=2):
     """Configuration-3 ring patch: SEI, tree gravity (opening angle 0.5, 25 ghost
     boxes), shear boundary, tree collision search + hardsphere (epsilon 0.5).
     Device-timed full steps, a split of gravity / collision time, and the oracle

@@ -94,6 +94,7 @@ SIGNATURES = {
     "rgpu_sim_time_steps": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.POINTER(ctypes.c_double)]),
     "rgpu_l2_flush": (ctypes.c_int, [_P, ctypes.c_size_t]),
     "rgpu_set_kernel_variant": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+    "rgpu_set_displacement_mode": (ctypes.c_int, [ctypes.c_int]),
     "rgpu_probe_rate": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "rgpu_direct_accel_noalloc": (ctypes.c_int, [_P] * 7 + [ctypes.c_int64, ctypes.c_double, ctypes.c_double,
                                                             ctypes.c_int, _P]),

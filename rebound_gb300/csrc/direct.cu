@@ -21,6 +21,7 @@
 //   (1-h)^(-3/2) = 1 + 3/2 h + 15/8 h^2 + O(h^3),   h = 1 - r^2 y0^2,
 // |h| < 2^-21, so the dropped 35/16 h^3 term is below 2^-62.
 #include "rgpu_internal.cuh"
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -102,6 +103,63 @@ struct GhostList {
     double off[125][3];
 };
 
+// --- FP64 displacement on the integer pipe --------------------------------------
+// Positions are held as 64-bit fixed point with scale 2^s, s chosen per force
+// evaluation so the largest |coordinate| is below 2^61 (differences then fit in
+// int64).  Every coordinate with |x| >= 2^-8 max|x| is representable exactly, so
+// the integer difference rounded once to double equals the FP64 subtraction
+// bit for bit; smaller coordinates are rounded to the 2^-s grid (an absolute
+// error below 2^-61 max|x|).
+struct __align__(32) FixBody {
+    long long x, y, z;
+    double gm;
+};
+
+// int64 * 2^-s -> double, round to nearest even, integer pipe only; ebias =
+// 1086 - s.  The caller keeps s <= 1022 so every nonzero result is a normal number.
+__device__ __forceinline__ double fix_to_double(long long v, int ebias) {
+    const unsigned long long sign = (unsigned long long)(v >> 63);
+    const unsigned long long a = ((unsigned long long)v ^ sign) - sign;          // |v|
+    const unsigned hi = (unsigned)(a >> 32), lo = (unsigned)a;
+    const int lz = hi ? __clz((int)hi) : 32 + __clz((int)lo);                    // 64 when a == 0
+    const unsigned long long n = a << (lz & 63);                                  // bit 63 set
+    const unsigned long long r = n + 0x3FFull + ((n >> 11) & 1ull);              // half an ulp, ties to even
+    const int carry = r < n;                                                      // rounded up to 2^64
+    const unsigned long long frac = carry ? 0ull : ((r >> 11) & 0xFFFFFFFFFFFFFull);
+    const unsigned long long e = (unsigned long long)(ebias - lz + carry);
+    const unsigned long long bits = (e << 52) | frac | (sign << 63);
+    return a ? __longlong_as_double((long long)bits) : 0.0;
+}
+
+__global__ void max_abs_coord(ParticlesSoA p, int N, unsigned long long* __restrict__ out) {
+    __shared__ double red[256];
+    double m = 0.;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+        m = fmax(m, fmax(fabs(p.x[i]), fmax(fabs(p.y[i]), fabs(p.z[i]))));
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicMax(out, (unsigned long long)__double_as_longlong(red[0]));  // positive doubles order as integers
+}
+
+__global__ void pack_fix(ParticlesSoA p, int N, double G, const unsigned long long* __restrict__ dmax,
+                         int* __restrict__ shift_out, FixBody* __restrict__ out) {
+    const double mx = __longlong_as_double((long long)*dmax);
+    const int s = (mx > 0. && isfinite(mx)) ? min(60 - ilogb(mx), 1022) : 60;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) *shift_out = s;
+    if (i >= N) return;
+    FixBody b;
+    b.x = __double2ll_rn(scalbn(p.x[i], s));
+    b.y = __double2ll_rn(scalbn(p.y[i], s));
+    b.z = __double2ll_rn(scalbn(p.z[i], s));
+    b.gm = G * p.m[i];
+    out[i] = b;
+}
+
 struct DirectArgs {
     const double4_32a* __restrict__ jpos;      // (x, y, z, G*m)
     const float4* __restrict__ jsplit;     // 2 per body: (xh, yh, zh, Gm_f), (xl, yl, zl, 0)
@@ -116,6 +174,7 @@ struct DirectArgs {
     double* __restrict__ az;
     double* __restrict__ partial;          // [split][3][cap] (splits > 1)
     size_t cap;
+    const int* __restrict__ fix_shift;     // non-null: jpos holds FixBody records at scale 2^shift
 };
 
 // j-range of particle i (src/gravity.c:215-233 and :258-277): active
@@ -130,7 +189,7 @@ __device__ __forceinline__ bool pair_skipped(const DirectArgs& a, int i, int j) 
     return false;
 }
 
-template <int MODE, bool GENERAL, int RV, bool CVT>
+template <int MODE, bool GENERAL, int RV, bool CVT, bool FIX = false>
 __global__ void __launch_bounds__(kBlock) direct_kernel(DirectArgs a, const GhostList* __restrict__ ghosts) {
     __shared__ double4_32a tile[(MODE == kMixedSplit) ? 1 : kBlock];
     __shared__ float4 tile_s[(MODE == kMixedSplit) ? 2 * kBlock : 1];
@@ -147,6 +206,10 @@ __global__ void __launch_bounds__(kBlock) direct_kernel(DirectArgs a, const Ghos
         const double4_32a p = a.jpos[i];
         xi = p.x; yi = p.y; zi = p.z;
     }
+    // FIX: the records are FixBody bit patterns; the displacement is the int64
+    // difference converted once (exactly the FP64 subtraction, see FixBody).
+    const long long xfi = __double_as_longlong(xi), yfi = __double_as_longlong(yi), zfi = __double_as_longlong(zi);
+    const int ebias = FIX ? 1086 - *a.fix_shift : 0;
     double sx = 0., sy = 0., sz = 0., cx = 0., cy = 0., cz = 0.;
     float fsx = 0.f, fsy = 0.f, fsz = 0.f, fcx = 0.f, fcy = 0.f, fcz = 0.f;
     const float eps2f = (float)a.eps2;
@@ -185,7 +248,14 @@ __global__ void __launch_bounds__(kBlock) direct_kernel(DirectArgs a, const Ghos
                 if (GENERAL) skip = skip || j >= jend_i || pair_skipped(a, i, j);
                 if (MODE == kBasic || MODE == kComp) {
                     const double4_32a q = tile[k];
-                    const double dx = q.x - gxi, dy = q.y - gyi, dz = q.z - gzi;
+                    double dx, dy, dz;
+                    if (FIX) {
+                        dx = fix_to_double(__double_as_longlong(q.x) - xfi, ebias);
+                        dy = fix_to_double(__double_as_longlong(q.y) - yfi, ebias);
+                        dz = fix_to_double(__double_as_longlong(q.z) - zfi, ebias);
+                    } else {
+                        dx = q.x - gxi; dy = q.y - gyi; dz = q.z - gzi;
+                    }
                     const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, a.eps2)));
                     double s = m_rinv3<RV>(r2, q.w);
                     s = skip ? 0.0 : s;
@@ -364,9 +434,16 @@ int choose_splits(int nbi, int jmax) {
 GhostList* g_ghost_dev = nullptr;
 int g_rinv_variant = kRinvSeriesInt;
 bool g_mixed_cvt = false;
+bool g_fix_disp = true;
 
 template <int MODE, bool GEN>
 void launch_mode(dim3 grid, cudaStream_t st, const DirectArgs& a) {
+    if constexpr ((MODE == kBasic || MODE == kComp) && !GEN) {
+        if (a.fix_shift) {
+            direct_kernel<MODE, false, kRinvSeriesInt, true, true><<<grid, kBlock, 0, st>>>(a, g_ghost_dev);
+            return;
+        }
+    }
     if (MODE == kBasic || MODE == kComp) {
         switch (g_rinv_variant) {
             case kRinvLib: direct_kernel<MODE, GEN, kRinvLib, true><<<grid, kBlock, 0, st>>>(a, g_ghost_dev); break;
@@ -387,6 +464,12 @@ extern "C" int rgpu_set_kernel_variant(int rinv_variant, int mixed_cvt) {
     if (rinv_variant < 0 || rinv_variant > 3) return RGPU_ERR_ARG;
     g_rinv_variant = rinv_variant;
     g_mixed_cvt = mixed_cvt != 0;
+    return RGPU_OK;
+}
+
+extern "C" int rgpu_set_displacement_mode(int mode) {
+    if (mode != 0 && mode != 1) return RGPU_ERR_ARG;
+    g_fix_disp = mode == 1;
     return RGPU_OK;
 }
 
@@ -434,21 +517,37 @@ int direct_accel(rgpu_sim* s, int gravity) {
         RGPU_CUDA(s, cudaMemcpyAsync(g_ghost_dev, &gl, sizeof(GhostList), cudaMemcpyHostToDevice, s->stream));
     }
 
-    pack_j<<<grid_for(N, 256), 256, 0, s->stream>>>(s->p, N, c.G, s->jpos, mode == kMixedSplit ? s->jsplit : nullptr);
-    g_launches++;
+    // BASIC and COMPENSATED without ghosts or pair exclusions form the
+    // displacement on the integer pipe from fixed-point positions; the two
+    // device words (max |coordinate|, scale) live in the unused jsplit buffer.
+    const bool fix = g_fix_disp && (mode == kBasic || mode == kComp) && !general;
+    int* fix_shift = nullptr;
+    if (fix) {
+        unsigned long long* dmax = reinterpret_cast<unsigned long long*>(s->jsplit);
+        fix_shift = reinterpret_cast<int*>(dmax + 1);
+        RGPU_CUDA(s, cudaMemsetAsync(dmax, 0, sizeof(unsigned long long), s->stream));
+        max_abs_coord<<<std::min<int>(grid_for(N, 256), 2 * 152), 256, 0, s->stream>>>(s->p, N, dmax);
+        pack_fix<<<grid_for(N, 256), 256, 0, s->stream>>>(s->p, N, c.G, dmax, fix_shift,
+                                                          reinterpret_cast<FixBody*>(s->jpos));
+        g_launches += 2;
+    } else {
+        pack_j<<<grid_for(N, 256), 256, 0, s->stream>>>(s->p, N, c.G, s->jpos, mode == kMixedSplit ? s->jsplit : nullptr);
+        g_launches++;
+    }
 
     const int nbi = (N + kBlock - 1) / kBlock;
     const int jmax = c.testparticle_type ? N : Na;
     const int splits = choose_splits(nbi, jmax);
     if (splits > 1) RGPU_TRY(ensure_partial(s, (size_t)splits));
 
-    DirectArgs a;
+    DirectArgs a{};
     a.jpos = s->jpos; a.jsplit = s->jsplit;
     a.N = N; a.Na = Na; a.tp = c.testparticle_type; a.ign = c.gravity_ignore_terms;
     a.eps2 = c.softening * c.softening;
     a.splits = splits;
     a.ax = s->p.ax; a.ay = s->p.ay; a.az = s->p.az;
     a.partial = s->partial; a.cap = s->cap;
+    a.fix_shift = fix_shift;
     const dim3 grid(nbi, splits);
 
     ktimer_begin(s);
@@ -581,7 +680,7 @@ extern "C" int rgpu_direct_accel_noalloc(const double* x, const double* y, const
     const int nbi = (N + kBlock - 1) / kBlock;
     int splits = choose_splits(nbi, N);
     if (splits > kNoAllocMaxSplits) splits = kNoAllocMaxSplits;
-    DirectArgs a;
+    DirectArgs a{};
     a.jpos = jpos; a.jsplit = jsplit;
     a.N = N; a.Na = N; a.tp = 0; a.ign = 0;
     a.eps2 = softening * softening;

@@ -28,8 +28,10 @@ def gpu_accel(R, particles, gravity, **cfg):
 
 @pytest.mark.parametrize("variant", [0, 1, 2, 3])
 def test_basic_plummer_4096_matches_reference(gpu, variant):
+    # m/r^3 variants with the FP64-subtraction displacement
     L = gpu.load()
     assert L.rgpu_set_kernel_variant(variant, 1) == 0
+    assert L.rgpu_set_displacement_mode(0) == 0
     try:
         g = golden("gravity_plummer.npz")
         a = gpu_accel(gpu, g["particles"], "basic", softening=0.01)
@@ -39,6 +41,60 @@ def test_basic_plummer_4096_matches_reference(gpu, variant):
         assert rel_err_vec(a, g["acc_compensated"]).max() <= FP64_TOL
     finally:
         L.rgpu_set_kernel_variant(3, 0)
+        L.rgpu_set_displacement_mode(1)
+
+
+@pytest.mark.parametrize("gravity", ["basic", "compensated"])
+def test_fixed_point_displacement_matches_reference(gpu, gravity):
+    # default form: int64 fixed-point positions, displacement on the integer pipe
+    g = golden("gravity_plummer.npz")
+    a = gpu_accel(gpu, g["particles"], gravity, softening=0.01)
+    assert rel_err_vec(a, g["acc_" + gravity]).max() <= FP64_TOL
+    assert rel_err_vec(a, g["acc_compensated"]).max() <= FP64_TOL
+
+
+def _both_displacements(gpu, parts, gravity, **cfg):
+    L = gpu.load()
+    a_fix = gpu_accel(gpu, parts, gravity, **cfg)
+    assert L.rgpu_set_displacement_mode(0) == 0
+    try:
+        a_sub = gpu_accel(gpu, parts, gravity, **cfg)
+    finally:
+        L.rgpu_set_displacement_mode(1)
+    return a_fix, a_sub
+
+
+@pytest.mark.parametrize("gravity", ["basic", "compensated"])
+@pytest.mark.parametrize("offset", [0.0, 1e6, -3.5e-3])
+def test_fixed_point_displacement_is_the_fp64_subtraction(gpu, gravity, offset):
+    # Every coordinate within a factor 2^8 of the largest is exact in the fixed-point
+    # form, so the integer-pipe displacement equals the FP64 subtraction bit for bit
+    # and the whole sum is bit-identical.  Coordinates lie in +-[4, 8] (+ offset).
+    rng = np.random.default_rng(11)
+    n = 3000
+    parts = np.zeros(n, dtype=O.PARTICLE_DTYPE)
+    mag = 4.0 + 4.0 * rng.random((n, 3))
+    pos = np.where(rng.random((n, 3)) < 0.5, -mag, mag)
+    if offset:
+        pos = offset + pos * (abs(offset) * 1e-3 if abs(offset) > 1 else 1.0)
+    parts["x"], parts["y"], parts["z"] = pos[:, 0], pos[:, 1], pos[:, 2]
+    parts["m"] = rng.random(n) / n
+    a_fix, a_sub = _both_displacements(gpu, parts, gravity, softening=0.0)
+    assert np.array_equal(a_fix, a_sub)
+
+
+def test_fixed_point_displacement_small_coordinates(gpu):
+    # Coordinates far below the largest are rounded to the 2^-s grid (absolute error
+    # < 2^-61 max|x|): a cluster at the origin next to one distant body.
+    rng = np.random.default_rng(12)
+    n = 2048
+    parts = np.zeros(n, dtype=O.PARTICLE_DTYPE)
+    parts["x"], parts["y"], parts["z"] = (rng.standard_normal((3, n)) * 1e-2)
+    parts["x"][0] = 1e3
+    parts["m"] = 1.0 / n
+    a_fix, a_sub = _both_displacements(gpu, parts, "basic", softening=0.0)
+    err = rel_err_vec(a_fix, a_sub)
+    assert err.max() <= 1e-11, err.max()
 
 
 def test_compensated_plummer_4096_matches_reference(gpu):
