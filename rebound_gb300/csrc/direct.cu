@@ -21,6 +21,7 @@
 //   (1-h)^(-3/2) = 1 + 3/2 h + 15/8 h^2 + O(h^3),   h = 1 - r^2 y0^2,
 // |h| < 2^-21, so the dropped 35/16 h^3 term is below 2^-62.
 #include "rgpu_internal.cuh"
+#include "fixpair.cuh"
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -103,33 +104,25 @@ struct GhostList {
     double off[125][3];
 };
 
-// --- FP64 displacement on the integer pipe --------------------------------------
+// --- Fixed-point positions for the integer-pipe pair forms ---------------------
 // Positions are held as 64-bit fixed point with scale 2^s, s chosen per force
 // evaluation so the largest |coordinate| is below 2^61 (differences then fit in
-// int64).  Every coordinate with |x| >= 2^-8 max|x| is representable exactly, so
-// the integer difference rounded once to double equals the FP64 subtraction
-// bit for bit; smaller coordinates are rounded to the 2^-s grid (an absolute
-// error below 2^-61 max|x|).
+// int64) and eps^2 2^2s below 2^124.  Every coordinate with |x| >= 2^-8 max|x|
+// is representable exactly, so the integer difference rounded once to double
+// equals the FP64 subtraction bit for bit; smaller coordinates are rounded to
+// the 2^-s grid (an absolute error below 2^-61 max|x|).
 struct __align__(32) FixBody {
     long long x, y, z;
     double gm;
 };
 
-// int64 * 2^-s -> double, round to nearest even, integer pipe only; ebias =
-// 1086 - s.  The caller keeps s <= 1022 so every nonzero result is a normal number.
-__device__ __forceinline__ double fix_to_double(long long v, int ebias) {
-    const unsigned long long sign = (unsigned long long)(v >> 63);
-    const unsigned long long a = ((unsigned long long)v ^ sign) - sign;          // |v|
-    const unsigned hi = (unsigned)(a >> 32), lo = (unsigned)a;
-    const int lz = hi ? __clz((int)hi) : 32 + __clz((int)lo);                    // 64 when a == 0
-    const unsigned long long n = a << (lz & 63);                                  // bit 63 set
-    const unsigned long long r = n + 0x3FFull + ((n >> 11) & 1ull);              // half an ulp, ties to even
-    const int carry = r < n;                                                      // rounded up to 2^64
-    const unsigned long long frac = carry ? 0ull : ((r >> 11) & 0xFFFFFFFFFFFFFull);
-    const unsigned long long e = (unsigned long long)(ebias - lz + carry);
-    const unsigned long long bits = (e << 52) | frac | (sign << 63);
-    return a ? __longlong_as_double((long long)bits) : 0.0;
-}
+// Per-evaluation scale words, written by pack_fix and read by every pair thread.
+struct __align__(16) FixScale {
+    unsigned long long dmax;               // max |coordinate| as double bits (atomicMax target)
+    int shift;                             // s
+    int two_s;                             // 2 s
+    unsigned long long e2hi, e2lo;         // eps^2 2^2s as a 128-bit integer
+};
 
 __global__ void max_abs_coord(ParticlesSoA p, int N, unsigned long long* __restrict__ out) {
     __shared__ double red[256];
@@ -145,12 +138,29 @@ __global__ void max_abs_coord(ParticlesSoA p, int N, unsigned long long* __restr
     if (threadIdx.x == 0) atomicMax(out, (unsigned long long)__double_as_longlong(red[0]));  // positive doubles order as integers
 }
 
-__global__ void pack_fix(ParticlesSoA p, int N, double G, const unsigned long long* __restrict__ dmax,
-                         int* __restrict__ shift_out, FixBody* __restrict__ out) {
-    const double mx = __longlong_as_double((long long)*dmax);
-    const int s = (mx > 0. && isfinite(mx)) ? min(60 - ilogb(mx), 1022) : 60;
+__global__ void pack_fix(ParticlesSoA p, int N, double G, double eps2, FixScale* __restrict__ sc,
+                         FixBody* __restrict__ out) {
+    const double mx = __longlong_as_double((long long)sc->dmax);
+    int s = (mx > 0. && isfinite(mx)) ? 60 - ilogb(mx) : 60;
+    if (eps2 > 0. && isfinite(eps2)) s = min(s, (123 - ilogb(eps2)) >> 1);
+    s = min(s, 1022);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) *shift_out = s;
+    if (i == 0) {
+        unsigned long long hi = 0, lo = 0;
+        if (eps2 > 0. && isfinite(eps2)) {
+            int ee;
+            const double fr = frexp(eps2, &ee);                        // eps2 = fr 2^ee, fr in [0.5, 1)
+            const unsigned long long m53 = (unsigned long long)scalbn(fr, 53);
+            const int sh = ee - 53 + 2 * s;                             // eps2 2^2s = m53 2^sh < 2^124
+            if (sh >= 64) { hi = m53 << (sh - 64); }
+            else if (sh > 0) { hi = m53 >> (64 - sh); lo = m53 << sh; }
+            else if (sh > -64) { lo = m53 >> (-sh); }
+        }
+        sc->shift = s;
+        sc->two_s = 2 * s;
+        sc->e2hi = hi;
+        sc->e2lo = lo;
+    }
     if (i >= N) return;
     FixBody b;
     b.x = __double2ll_rn(scalbn(p.x[i], s));
@@ -174,7 +184,7 @@ struct DirectArgs {
     double* __restrict__ az;
     double* __restrict__ partial;          // [split][3][cap] (splits > 1)
     size_t cap;
-    const int* __restrict__ fix_shift;     // non-null: jpos holds FixBody records at scale 2^shift
+    const FixScale* __restrict__ fix;      // non-null: jpos holds FixBody records (FIX kernels)
 };
 
 // j-range of particle i (src/gravity.c:215-233 and :258-277): active
@@ -189,7 +199,10 @@ __device__ __forceinline__ bool pair_skipped(const DirectArgs& a, int i, int j) 
     return false;
 }
 
-template <int MODE, bool GENERAL, int RV, bool CVT, bool FIX = false>
+// FIX: 0 = FP64 positions; 1 = fixed-point positions, displacement converted on
+// the integer pipe, FP64 m/r^3; 2 = fixed-point positions and m/r^3 on the
+// integer pipes (fixpair::rinv3), FP64 only for G m f and the accumulation.
+template <int MODE, bool GENERAL, int RV, bool CVT, int FIX = 0>
 __global__ void __launch_bounds__(kBlock) direct_kernel(DirectArgs a, const GhostList* __restrict__ ghosts) {
     __shared__ double4_32a tile[(MODE == kMixedSplit) ? 1 : kBlock];
     __shared__ float4 tile_s[(MODE == kMixedSplit) ? 2 * kBlock : 1];
@@ -209,7 +222,15 @@ __global__ void __launch_bounds__(kBlock) direct_kernel(DirectArgs a, const Ghos
     // FIX: the records are FixBody bit patterns; the displacement is the int64
     // difference converted once (exactly the FP64 subtraction, see FixBody).
     const long long xfi = __double_as_longlong(xi), yfi = __double_as_longlong(yi), zfi = __double_as_longlong(zi);
-    const int ebias = FIX ? 1086 - *a.fix_shift : 0;
+    int ebias = 0, fbias = 0, two_s = 0;
+    unsigned long long e2hi = 0, e2lo = 0;
+    if (FIX) {
+        ebias = 1086 - a.fix->shift;
+        fbias = 190 - a.fix->shift;
+        two_s = a.fix->two_s;
+        e2hi = a.fix->e2hi;
+        e2lo = a.fix->e2lo;
+    }
     double sx = 0., sy = 0., sz = 0., cx = 0., cy = 0., cz = 0.;
     float fsx = 0.f, fsy = 0.f, fsz = 0.f, fcx = 0.f, fcy = 0.f, fcz = 0.f;
     const float eps2f = (float)a.eps2;
@@ -248,16 +269,26 @@ __global__ void __launch_bounds__(kBlock) direct_kernel(DirectArgs a, const Ghos
                 if (GENERAL) skip = skip || j >= jend_i || pair_skipped(a, i, j);
                 if (MODE == kBasic || MODE == kComp) {
                     const double4_32a q = tile[k];
-                    double dx, dy, dz;
+                    double dx, dy, dz, s;
                     if (FIX) {
-                        dx = fix_to_double(__double_as_longlong(q.x) - xfi, ebias);
-                        dy = fix_to_double(__double_as_longlong(q.y) - yfi, ebias);
-                        dz = fix_to_double(__double_as_longlong(q.z) - zfi, ebias);
+                        unsigned long long sgx, sgy, sgz;
+                        const unsigned long long ux = fixpair::abs64(__double_as_longlong(q.x) - xfi, &sgx);
+                        const unsigned long long uy = fixpair::abs64(__double_as_longlong(q.y) - yfi, &sgy);
+                        const unsigned long long uz = fixpair::abs64(__double_as_longlong(q.z) - zfi, &sgz);
+                        dx = fixpair::abs_to_double(ux, sgx, ebias);
+                        dy = fixpair::abs_to_double(uy, sgy, ebias);
+                        dz = fixpair::abs_to_double(uz, sgz, ebias);
+                        if (FIX == 2) {
+                            s = q.w * fixpair::rinv3(ux, uy, uz, e2hi, e2lo, two_s);
+                        } else {
+                            const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, a.eps2)));
+                            s = m_rinv3<RV>(r2, q.w);
+                        }
                     } else {
                         dx = q.x - gxi; dy = q.y - gyi; dz = q.z - gzi;
+                        const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, a.eps2)));
+                        s = m_rinv3<RV>(r2, q.w);
                     }
-                    const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, a.eps2)));
-                    double s = m_rinv3<RV>(r2, q.w);
                     s = skip ? 0.0 : s;
                     if (MODE == kBasic) {
                         tx = fma(s, dx, tx); ty = fma(s, dy, ty); tz = fma(s, dz, tz);
@@ -270,7 +301,18 @@ __global__ void __launch_bounds__(kBlock) direct_kernel(DirectArgs a, const Ghos
                     }
                 } else {
                     float dxf, dyf, dzf, mf;
-                    if (MODE == kMixed) {
+                    if (MODE == kMixed && FIX) {
+                        // exact FP64 displacement from the fixed-point positions, rounded once to float
+                        const double4_32a q = tile[k];
+                        unsigned long long sgx, sgy, sgz;
+                        const unsigned long long ux = fixpair::abs64(__double_as_longlong(q.x) - xfi, &sgx);
+                        const unsigned long long uy = fixpair::abs64(__double_as_longlong(q.y) - yfi, &sgy);
+                        const unsigned long long uz = fixpair::abs64(__double_as_longlong(q.z) - zfi, &sgz);
+                        dxf = fixpair::abs_to_float(ux, sgx, fbias);
+                        dyf = fixpair::abs_to_float(uy, sgy, fbias);
+                        dzf = fixpair::abs_to_float(uz, sgz, fbias);
+                        mf = round_to_float(q.w);
+                    } else if (MODE == kMixed) {
                         const double4_32a q = tile[k];
                         const double dx = q.x - gxi, dy = q.y - gyi, dz = q.z - gzi;   // FP64 displacement
                         if (CVT) { dxf = (float)dx; dyf = (float)dy; dzf = (float)dz; mf = (float)q.w; }
@@ -434,13 +476,22 @@ int choose_splits(int nbi, int jmax) {
 GhostList* g_ghost_dev = nullptr;
 int g_rinv_variant = kRinvSeriesInt;
 bool g_mixed_cvt = false;
-bool g_fix_disp = true;
+int g_disp_mode = 2;
 
 template <int MODE, bool GEN>
 void launch_mode(dim3 grid, cudaStream_t st, const DirectArgs& a) {
     if constexpr ((MODE == kBasic || MODE == kComp) && !GEN) {
-        if (a.fix_shift) {
-            direct_kernel<MODE, false, kRinvSeriesInt, true, true><<<grid, kBlock, 0, st>>>(a, g_ghost_dev);
+        if (a.fix) {
+            if (g_disp_mode == 1)
+                direct_kernel<MODE, false, kRinvSeriesInt, true, 1><<<grid, kBlock, 0, st>>>(a, g_ghost_dev);
+            else
+                direct_kernel<MODE, false, kRinvSeriesInt, true, 2><<<grid, kBlock, 0, st>>>(a, g_ghost_dev);
+            return;
+        }
+    }
+    if constexpr (MODE == kMixed && !GEN) {
+        if (a.fix) {
+            direct_kernel<kMixed, false, kRinvSeries, false, 1><<<grid, kBlock, 0, st>>>(a, g_ghost_dev);
             return;
         }
     }
@@ -468,8 +519,8 @@ extern "C" int rgpu_set_kernel_variant(int rinv_variant, int mixed_cvt) {
 }
 
 extern "C" int rgpu_set_displacement_mode(int mode) {
-    if (mode != 0 && mode != 1) return RGPU_ERR_ARG;
-    g_fix_disp = mode == 1;
+    if (mode < 0 || mode > 2) return RGPU_ERR_ARG;
+    g_disp_mode = mode;
     return RGPU_OK;
 }
 
@@ -517,17 +568,16 @@ int direct_accel(rgpu_sim* s, int gravity) {
         RGPU_CUDA(s, cudaMemcpyAsync(g_ghost_dev, &gl, sizeof(GhostList), cudaMemcpyHostToDevice, s->stream));
     }
 
-    // BASIC and COMPENSATED without ghosts or pair exclusions form the
-    // displacement on the integer pipe from fixed-point positions; the two
-    // device words (max |coordinate|, scale) live in the unused jsplit buffer.
-    const bool fix = g_fix_disp && (mode == kBasic || mode == kComp) && !general;
-    int* fix_shift = nullptr;
+    // BASIC, COMPENSATED and MIXED without ghosts or pair exclusions form the
+    // displacement on the integer pipe from fixed-point positions; the scale
+    // words (FixScale) live in the jsplit buffer, which only MIXED_SPLIT uses.
+    const bool fix = g_disp_mode != 0 && (mode == kBasic || mode == kComp || mode == kMixed) && !general;
+    FixScale* fsc = nullptr;
     if (fix) {
-        unsigned long long* dmax = reinterpret_cast<unsigned long long*>(s->jsplit);
-        fix_shift = reinterpret_cast<int*>(dmax + 1);
-        RGPU_CUDA(s, cudaMemsetAsync(dmax, 0, sizeof(unsigned long long), s->stream));
-        max_abs_coord<<<std::min<int>(grid_for(N, 256), 2 * 152), 256, 0, s->stream>>>(s->p, N, dmax);
-        pack_fix<<<grid_for(N, 256), 256, 0, s->stream>>>(s->p, N, c.G, dmax, fix_shift,
+        fsc = reinterpret_cast<FixScale*>(s->jsplit);
+        RGPU_CUDA(s, cudaMemsetAsync(&fsc->dmax, 0, sizeof(unsigned long long), s->stream));
+        max_abs_coord<<<std::min<int>(grid_for(N, 256), 2 * 152), 256, 0, s->stream>>>(s->p, N, &fsc->dmax);
+        pack_fix<<<grid_for(N, 256), 256, 0, s->stream>>>(s->p, N, c.G, c.softening * c.softening, fsc,
                                                           reinterpret_cast<FixBody*>(s->jpos));
         g_launches += 2;
     } else {
@@ -547,7 +597,7 @@ int direct_accel(rgpu_sim* s, int gravity) {
     a.splits = splits;
     a.ax = s->p.ax; a.ay = s->p.ay; a.az = s->p.az;
     a.partial = s->partial; a.cap = s->cap;
-    a.fix_shift = fix_shift;
+    a.fix = fsc;
     const dim3 grid(nbi, splits);
 
     ktimer_begin(s);

@@ -41,37 +41,40 @@ def test_basic_plummer_4096_matches_reference(gpu, variant):
         assert rel_err_vec(a, g["acc_compensated"]).max() <= FP64_TOL
     finally:
         L.rgpu_set_kernel_variant(3, 0)
-        L.rgpu_set_displacement_mode(1)
+        L.rgpu_set_displacement_mode(2)
 
 
+@pytest.mark.parametrize("disp", [1, 2])
 @pytest.mark.parametrize("gravity", ["basic", "compensated"])
-def test_fixed_point_displacement_matches_reference(gpu, gravity):
-    # default form: int64 fixed-point positions, displacement on the integer pipe
-    g = golden("gravity_plummer.npz")
-    a = gpu_accel(gpu, g["particles"], gravity, softening=0.01)
-    assert rel_err_vec(a, g["acc_" + gravity]).max() <= FP64_TOL
-    assert rel_err_vec(a, g["acc_compensated"]).max() <= FP64_TOL
-
-
-def _both_displacements(gpu, parts, gravity, **cfg):
+def test_fixed_point_forms_match_reference(gpu, gravity, disp):
+    # 1: int64 fixed-point positions, displacement converted on the integer pipe;
+    # 2 (default): also r^2 and (r^2+eps^2)^(-3/2) on the integer pipes
     L = gpu.load()
-    a_fix = gpu_accel(gpu, parts, gravity, **cfg)
-    assert L.rgpu_set_displacement_mode(0) == 0
+    assert L.rgpu_set_displacement_mode(disp) == 0
     try:
-        a_sub = gpu_accel(gpu, parts, gravity, **cfg)
+        g = golden("gravity_plummer.npz")
+        a = gpu_accel(gpu, g["particles"], gravity, softening=0.01)
+        assert rel_err_vec(a, g["acc_" + gravity]).max() <= FP64_TOL
+        assert rel_err_vec(a, g["acc_compensated"]).max() <= FP64_TOL
     finally:
-        L.rgpu_set_displacement_mode(1)
-    return a_fix, a_sub
+        L.rgpu_set_displacement_mode(2)
 
 
-@pytest.mark.parametrize("gravity", ["basic", "compensated"])
-@pytest.mark.parametrize("offset", [0.0, 1e6, -3.5e-3])
-def test_fixed_point_displacement_is_the_fp64_subtraction(gpu, gravity, offset):
-    # Every coordinate within a factor 2^8 of the largest is exact in the fixed-point
-    # form, so the integer-pipe displacement equals the FP64 subtraction bit for bit
-    # and the whole sum is bit-identical.  Coordinates lie in +-[4, 8] (+ offset).
-    rng = np.random.default_rng(11)
-    n = 3000
+def _two_modes(gpu, parts, gravity, mode_a, mode_b, **cfg):
+    L = gpu.load()
+    out = []
+    try:
+        for m in (mode_a, mode_b):
+            assert L.rgpu_set_displacement_mode(m) == 0
+            out.append(gpu_accel(gpu, parts, gravity, **cfg))
+    finally:
+        L.rgpu_set_displacement_mode(2)
+    return out
+
+
+def _shell_box(n, offset, seed):
+    # coordinates in +-[4, 8] (scaled and shifted for an offset cluster)
+    rng = np.random.default_rng(seed)
     parts = np.zeros(n, dtype=O.PARTICLE_DTYPE)
     mag = 4.0 + 4.0 * rng.random((n, 3))
     pos = np.where(rng.random((n, 3)) < 0.5, -mag, mag)
@@ -79,8 +82,48 @@ def test_fixed_point_displacement_is_the_fp64_subtraction(gpu, gravity, offset):
         pos = offset + pos * (abs(offset) * 1e-3 if abs(offset) > 1 else 1.0)
     parts["x"], parts["y"], parts["z"] = pos[:, 0], pos[:, 1], pos[:, 2]
     parts["m"] = rng.random(n) / n
-    a_fix, a_sub = _both_displacements(gpu, parts, gravity, softening=0.0)
+    return parts
+
+
+@pytest.mark.parametrize("gravity", ["basic", "compensated"])
+@pytest.mark.parametrize("offset", [0.0, 1e6, -3.5e-3])
+def test_fixed_point_displacement_is_the_fp64_subtraction(gpu, gravity, offset):
+    # Every coordinate within a factor 2^8 of the largest is exact in the fixed-point
+    # form, so the integer-pipe displacement equals the FP64 subtraction bit for bit
+    # and the whole sum is bit-identical.
+    parts = _shell_box(3000, offset, 11)
+    a_fix, a_sub = _two_modes(gpu, parts, gravity, 1, 0, softening=0.0)
     assert np.array_equal(a_fix, a_sub)
+
+
+@pytest.mark.parametrize("gravity", ["basic", "compensated"])
+@pytest.mark.parametrize("offset,soft", [(0.0, 0.0), (0.0, 0.3), (1e6, 0.0), (-3.5e-3, 1e-4), (0.0, 40.0)])
+def test_integer_pair_factor_matches_fp64(gpu, gravity, offset, soft):
+    # (r^2 + eps^2)^(-3/2) on the integer pipes against the FP64 form, including a
+    # softening larger than the whole box (the fixed-point scale then follows eps).
+    # Error measured against each particle's force scale sum_j m_j / (r^2+eps^2)
+    # (the net force of a box interior nearly cancels): each pair factor is good to
+    # about one ulp, so the difference stays within a few ulps of that scale.
+    parts = _shell_box(3000, offset, 13)
+    a_int, a_fp = _two_modes(gpu, parts, gravity, 2, 0, softening=soft)
+    pos = np.stack([parts["x"], parts["y"], parts["z"]], axis=1)
+    d = pos[None, :, :] - pos[:, None, :]
+    r2 = (d * d).sum(axis=2) + soft * soft
+    np.fill_diagonal(r2, np.inf)
+    scale = (parts["m"][None, :] / r2).sum(axis=1)
+    err = np.linalg.norm(a_int - a_fp, axis=1) / scale
+    assert err.max() <= 4e-15, err.max()
+    assert rel_err_vec(a_int, a_fp).max() <= FP64_TOL
+
+
+@pytest.mark.parametrize("offset", [0.0, 1e6])
+def test_mixed_fixed_point_displacement(gpu, offset):
+    # MIXED rounds the exact displacement straight to float; the FP64 form rounds
+    # twice (double, then float).  They differ only in rare double-rounding cases.
+    parts = _shell_box(3000, offset, 17)
+    a_fix, a_sub = _two_modes(gpu, parts, "mixed", 2, 0, softening=0.01)
+    err = rel_err_vec(a_fix, a_sub)
+    assert np.median(err) <= 1e-7 and err.max() <= 1e-5, (np.median(err), err.max())
 
 
 def test_fixed_point_displacement_small_coordinates(gpu):
@@ -92,9 +135,10 @@ def test_fixed_point_displacement_small_coordinates(gpu):
     parts["x"], parts["y"], parts["z"] = (rng.standard_normal((3, n)) * 1e-2)
     parts["x"][0] = 1e3
     parts["m"] = 1.0 / n
-    a_fix, a_sub = _both_displacements(gpu, parts, "basic", softening=0.0)
-    err = rel_err_vec(a_fix, a_sub)
-    assert err.max() <= 1e-11, err.max()
+    for mode in (1, 2):
+        a_fix, a_sub = _two_modes(gpu, parts, "basic", mode, 0, softening=0.0)
+        err = rel_err_vec(a_fix, a_sub)
+        assert err.max() <= 1e-11, (mode, err.max())
 
 
 def test_compensated_plummer_4096_matches_reference(gpu):
