@@ -236,8 +236,14 @@ def run_gb300(args):
     fp64_peak = 2 * rate.value / 1e12
     L.rgpu_probe_rate(1, ctypes.byref(rate))
     fp32_peak = 2 * rate.value / 1e12
-    achieved = FLOPS_PER_PAIR * pairs / (kernel_ms * 1e-3) / 1e12
-    traffic = profiled_traffic()
+    L.rgpu_probe_rate(4, ctypes.byref(rate))
+    alu_peak = rate.value / 1e12
+    pair_rate = pairs / (kernel_ms * 1e-3)
+    prof = profiled_counts()
+    traffic = prof.get("traffic_bytes_per_launch")
+    alu_ipp = prof.get("alu_inst_per_pair")
+    fp64_ipp = prof.get("fp64_inst_per_pair")
+    fp64_equiv = FLOPS_PER_PAIR * pair_rate / 1e12
 
     # Accuracy and speed of the other forms (force evaluation at step 0).
     forms = {}
@@ -321,12 +327,8 @@ def run_gb300(args):
                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Plummer sphere)",
                "config": config_block(n, world),
                "e2e": e2e, "gpu_launches": int(launches),
-               "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                            "frac": achieved / fp64_peak if fp64_peak else None, "traffic": traffic,
-                            "kernel": "direct_kernel<BASIC> (FP64 pair sum)", "kernel_ms": kernel_ms,
-                            "flops_per_pair": FLOPS_PER_PAIR,
-                            "peak_source": "live DFMA probe on this GPU (rgpu_probe_rate); measured-peaks file has no FP64 figure",
-                            "fp32_peak_tflops": fp32_peak},
+               "roofline": roofline_block(alu_ipp, fp64_ipp, pair_rate, alu_peak, fp64_peak, fp32_peak,
+                                          fp64_equiv, traffic, kernel_ms),
                "forms": forms,
                "cpu_baseline": {"value": cpu_val, "unit": "Gpair-int/s", "cores": cores, "kind": "port",
                                 "sample": sample},
@@ -441,16 +443,51 @@ def ensemble_only(args):
             "system_steps_per_s": args.ens_systems * args.ens_steps / (ms * 1e-3)}
 
 
-def profiled_traffic():
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if present."""
+def profiled_counts():
+    """Per-launch DRAM bytes and per-pair instruction counts of the dominant kernel,
+    from the committed ncu summary (key: value lines)."""
     path = os.path.join(REPO, "profiles", "direct_basic_fp64.md")
+    out = {}
     try:
         for line in open(path):
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":")[1])
+            k, sep, v = line.partition(":")
+            if sep and k in ("traffic_bytes_per_launch", "alu_inst_per_pair", "inst_per_pair", "fp64_inst_per_pair"):
+                out[k] = float(v)
     except OSError:
         pass
-    return None
+    return out
+
+
+def roofline_block(alu_ipp, fp64_ipp, pair_rate, alu_peak, fp64_peak, fp32_peak, fp64_equiv, traffic, kernel_ms):
+    """Roofline of the FP64 pair kernel against the pipe that binds it.  The kernel
+    issues fp64_ipp FP64 instructions and alu_ipp integer-ALU instructions per pair
+    (ncu counts, size-independent); each pipe's achieved rate is that count times the
+    live pair rate, against its live probe (rgpu_probe_rate 0 and 4).  FP64 rates are
+    in DFMA-equivalent TFLOP/s (2 flops per pipe instruction).  The plain-FP64 view
+    (20 flops per pair at the DFMA peak) rides alongside."""
+    pipes = {}
+    if fp64_ipp and fp64_peak:
+        a = 2 * fp64_ipp * pair_rate / 1e12
+        pipes["fp64"] = {"achieved": a, "peak": fp64_peak, "unit": "TFLOP/s (DFMA-equivalent)",
+                         "frac": a / fp64_peak, "inst_per_pair": fp64_ipp,
+                         "peak_source": "live DFMA probe (rgpu_probe_rate 0); measured-peaks file has no FP64 figure"}
+    if alu_ipp and alu_peak:
+        a = alu_ipp * pair_rate / 1e12
+        pipes["alu"] = {"achieved": a, "peak": alu_peak, "unit": "Tinst/s (integer ALU lane-ops)",
+                        "frac": a / alu_peak, "inst_per_pair": alu_ipp,
+                        "peak_source": "live integer-ALU probe (rgpu_probe_rate 4)"}
+    plain = {"flops_per_pair": FLOPS_PER_PAIR, "equivalent_tflops": fp64_equiv, "fp64_peak_tflops": fp64_peak,
+             "equivalent_over_peak": fp64_equiv / fp64_peak if fp64_peak else None}
+    if not pipes:
+        return {"bound": "fp64", "achieved": fp64_equiv, "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": fp64_equiv / fp64_peak if fp64_peak else None, "traffic": traffic,
+                "kernel": "direct_kernel<BASIC>", "kernel_ms": kernel_ms, "plain_fp64_view": plain}
+    bound = max(pipes, key=lambda k: pipes[k]["frac"])
+    b = pipes[bound]
+    return {"bound": bound, "achieved": b["achieved"], "peak": b["peak"], "unit": b["unit"], "frac": b["frac"],
+            "traffic": traffic, "kernel": "direct_kernel<BASIC> (int64 fixed-point pair, FP64 accumulate)",
+            "kernel_ms": kernel_ms, "pair_rate_per_s": pair_rate, "pipes": pipes, "plain_fp64_view": plain,
+            "fp32_peak_tflops": fp32_peak}
 
 
 def main():

@@ -176,19 +176,19 @@ int rgpu_l2_flush(rgpu_sim* sim, size_t bytes);
  * rounds the FP64 displacement to FP32 (1: conversion instruction; 0 (default):
  * integer-pipe rounding).  All variants meet the FP64 / mixed tolerances. */
 int rgpu_set_kernel_variant(int rinv_variant, int mixed_cvt);
-/* Pair arithmetic of BASIC/COMPENSATED direct summation without ghost boxes
- * or pair exclusions: 2 (default) = int64 fixed-point positions at a scale
- * chosen per evaluation, displacement, r^2 and (r^2+eps^2)^(-3/2) on the
- * integer pipes, FP64 for G m f and the sums; 1 = fixed-point displacement
- * (equal to the FP64 subtraction for coordinates >= 2^-8 of the largest) with
- * FP64 r^2 and m/r^3; 0 = FP64 throughout.  No reference counterpart (tuning
- * only). */
+/* Pair arithmetic of BASIC/COMPENSATED (and the displacement of MIXED) in
+ * direct summation without ghost boxes or pair exclusions: 2 (default) =
+ * int64 fixed-point positions at a scale chosen per evaluation, displacement
+ * and (r^2+eps^2)^(-3/2) on the integer pipes, FP64 for G m f and the sums;
+ * 1 = fixed-point displacement (equal to the FP64 subtraction for coordinates
+ * >= 2^-8 of the largest) with FP64 r^2 and m/r^3; 0 = FP64 throughout.
+ * No reference counterpart (tuning only). */
 int rgpu_set_displacement_mode(int mode);
 /* Count of this library's kernel launches since load. */
 int64_t rgpu_launch_count(void);
 /* Measured sustained lane-operation rate (ops/s) of one instruction class on
  * the current device: 0 = FP64 FMA, 1 = FP32 FMA, 2 = FP64<->FP32 conversion,
- * 3 = FP32 rsqrt (MUFU). */
+ * 3 = FP32 rsqrt (MUFU), 4 = integer ALU (3-input logic op). */
 int rgpu_probe_rate(int which, double* ops_per_s);
 
 /* Kepler drift of n independent bodies with gravitational parameters mu[i]

@@ -121,8 +121,9 @@ struct __align__(16) FixScale {
     unsigned long long dmax;               // max |coordinate| as double bits (atomicMax target)
     int shift;                             // s
     int two_s;                             // 2 s
-    unsigned long long e2hi, e2lo;         // eps^2 2^2s as a 128-bit integer
+    unsigned long long e0, e1, e2;         // eps^2 2^2s = e0 + e1 2^32 + e2 2^62 (e0 < 2^32, e1 < 2^30)
 };
+static_assert(sizeof(FixScale) <= 256 * 2 * sizeof(float4), "FixScale lives in the jsplit buffer (>= 256 bodies)");
 
 __global__ void max_abs_coord(ParticlesSoA p, int N, unsigned long long* __restrict__ out) {
     __shared__ double red[256];
@@ -158,8 +159,9 @@ __global__ void pack_fix(ParticlesSoA p, int N, double G, double eps2, FixScale*
         }
         sc->shift = s;
         sc->two_s = 2 * s;
-        sc->e2hi = hi;
-        sc->e2lo = lo;
+        sc->e0 = lo & 0xFFFFFFFFull;
+        sc->e1 = (lo >> 32) & 0x3FFFFFFFull;
+        sc->e2 = (lo >> 62) | (hi << 2);
     }
     if (i >= N) return;
     FixBody b;
@@ -200,8 +202,10 @@ __device__ __forceinline__ bool pair_skipped(const DirectArgs& a, int i, int j) 
 }
 
 // FIX: 0 = FP64 positions; 1 = fixed-point positions, displacement converted on
-// the integer pipe, FP64 m/r^3; 2 = fixed-point positions and m/r^3 on the
-// integer pipes (fixpair::rinv3), FP64 only for G m f and the accumulation.
+// the integer pipe (exactly the FP64 subtraction), FP64 r^2 and m/r^3; 2 =
+// fixed-point positions, displacement and (r^2+eps^2)^(-3/2) on the integer
+// pipes (fixpair::limbs_to_double, fixpair::rinv3_limbs), FP64 only for
+// G m f and the accumulation.
 template <int MODE, bool GENERAL, int RV, bool CVT, int FIX = 0>
 __global__ void __launch_bounds__(kBlock) direct_kernel(DirectArgs a, const GhostList* __restrict__ ghosts) {
     __shared__ double4_32a tile[(MODE == kMixedSplit) ? 1 : kBlock];
@@ -223,13 +227,14 @@ __global__ void __launch_bounds__(kBlock) direct_kernel(DirectArgs a, const Ghos
     // difference converted once (exactly the FP64 subtraction, see FixBody).
     const long long xfi = __double_as_longlong(xi), yfi = __double_as_longlong(yi), zfi = __double_as_longlong(zi);
     int ebias = 0, fbias = 0, two_s = 0;
-    unsigned long long e2hi = 0, e2lo = 0;
+    unsigned long long e0 = 0, e1 = 0, e2 = 0;
     if (FIX) {
         ebias = 1086 - a.fix->shift;
         fbias = 190 - a.fix->shift;
         two_s = a.fix->two_s;
-        e2hi = a.fix->e2hi;
-        e2lo = a.fix->e2lo;
+        e0 = a.fix->e0;
+        e1 = a.fix->e1;
+        e2 = a.fix->e2;
     }
     double sx = 0., sy = 0., sz = 0., cx = 0., cy = 0., cz = 0.;
     float fsx = 0.f, fsy = 0.f, fsz = 0.f, fcx = 0.f, fcy = 0.f, fcz = 0.f;
@@ -270,7 +275,16 @@ __global__ void __launch_bounds__(kBlock) direct_kernel(DirectArgs a, const Ghos
                 if (MODE == kBasic || MODE == kComp) {
                     const double4_32a q = tile[k];
                     double dx, dy, dz, s;
-                    if (FIX) {
+                    if (FIX == 2) {
+                        unsigned xh, xl, yh, yl, zh, zl, sx_, sy_, sz_;
+                        fixpair::sub_abs(__double_as_longlong(q.x), xfi, xh, xl, sx_);
+                        fixpair::sub_abs(__double_as_longlong(q.y), yfi, yh, yl, sy_);
+                        fixpair::sub_abs(__double_as_longlong(q.z), zfi, zh, zl, sz_);
+                        dx = fixpair::limbs_to_double(xh, xl, sx_, ebias - 1);
+                        dy = fixpair::limbs_to_double(yh, yl, sy_, ebias - 1);
+                        dz = fixpair::limbs_to_double(zh, zl, sz_, ebias - 1);
+                        s = q.w * fixpair::rinv3_limbs<true>(xh, xl, yh, yl, zh, zl, e0, e1, e2, two_s);
+                    } else if (FIX) {
                         unsigned long long sgx, sgy, sgz;
                         const unsigned long long ux = fixpair::abs64(__double_as_longlong(q.x) - xfi, &sgx);
                         const unsigned long long uy = fixpair::abs64(__double_as_longlong(q.y) - yfi, &sgy);
@@ -278,12 +292,8 @@ __global__ void __launch_bounds__(kBlock) direct_kernel(DirectArgs a, const Ghos
                         dx = fixpair::abs_to_double(ux, sgx, ebias);
                         dy = fixpair::abs_to_double(uy, sgy, ebias);
                         dz = fixpair::abs_to_double(uz, sgz, ebias);
-                        if (FIX == 2) {
-                            s = q.w * fixpair::rinv3(ux, uy, uz, e2hi, e2lo, two_s);
-                        } else {
-                            const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, a.eps2)));
-                            s = m_rinv3<RV>(r2, q.w);
-                        }
+                        const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, a.eps2)));
+                        s = m_rinv3<RV>(r2, q.w);
                     } else {
                         dx = q.x - gxi; dy = q.y - gyi; dz = q.z - gzi;
                         const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, a.eps2)));

@@ -58,10 +58,32 @@ __global__ void probe_rsqrt(float* out, float a) {
     if (s == 1234.5678f) out[0] = s;
 }
 
+// Integer ALU pipe: dependent 3-input logic ops (one LOP3 each, written as
+// inline PTX so the compiler can neither fold nor move them to another pipe).
+__device__ __forceinline__ unsigned lop3_xor(unsigned a, unsigned b, unsigned c) {
+    unsigned d;
+    asm volatile("lop3.b32 %0, %1, %2, %3, 0x96;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+
+__global__ void probe_alu(unsigned* out, unsigned m) {
+    unsigned u[kChains], v[kChains];
+    for (int c = 0; c < kChains; c++) { u[c] = threadIdx.x * 7u + c; v[c] = c * 31u + m; }
+    for (int it = 0; it < kIters / 2; it++)
+#pragma unroll
+        for (int c = 0; c < kChains; c++) {
+            u[c] = lop3_xor(u[c], v[c], m);
+            v[c] = lop3_xor(v[c], u[c], it);
+        }
+    unsigned t = 0;
+    for (int c = 0; c < kChains; c++) t += u[c] + v[c];
+    if (t == 12345u) out[0] = t;
+}
+
 }  // namespace
 
 extern "C" int rgpu_probe_rate(int which, double* ops_per_s) {
-    if (!ops_per_s || which < 0 || which > 3) return RGPU_ERR_ARG;
+    if (!ops_per_s || which < 0 || which > 4) return RGPU_ERR_ARG;
     int dev = 0, nsm = 1;
     if (cudaGetDevice(&dev) != cudaSuccess) return RGPU_ERR_CUDA;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -79,6 +101,7 @@ extern "C" int rgpu_probe_rate(int which, double* ops_per_s) {
             case 0: probe_dfma<<<blocks, threads>>>((double*)buf, 0.999999, 1e-7); break;
             case 1: probe_ffma<<<blocks, threads>>>((float*)buf, 0.999999f, 1e-7f); break;
             case 2: probe_cvt<<<blocks, threads>>>((double*)buf, 0.5); break;
+            case 4: probe_alu<<<blocks, threads>>>((unsigned*)buf, 3u); break;
             default: probe_rsqrt<<<blocks, threads>>>((float*)buf, 0.5f); break;
         }
         g_launches++;
