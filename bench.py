@@ -45,6 +45,22 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x, dist, device):
+    """Max of a per-rank time over all ranks: the job is as slow as its slowest rank."""
+    if not dist:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank_step, steps, world, total_ms):
+    """Whole-job throughput: every rank processes its own units (replicas, weak
+    scaling), so the job's units over the slowest rank's time."""
+    return units_per_rank_step * steps * world / (total_ms * 1e-3)
+
+
 class Clocks:
     """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -221,12 +237,9 @@ def run_gb300(args):
     launches = L.rgpu_launch_count() - launches0
     kms, kn = ctypes.c_double(0.), ctypes.c_int64(0)
     L.rgpu_sim_kernel_time(h, ctypes.byref(kms), ctypes.byref(kn))
-    if dist:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, dist, "cuda")
     pairs = n * (n - 1)
-    value = pairs * args.steps * world / (total_ms * 1e-3) / 1e9
+    value = job_rate(pairs, args.steps, world, total_ms) / 1e9
     ms_step = total_ms / args.steps
     kernel_ms = kms.value / max(1, kn.value)
 
@@ -295,8 +308,8 @@ def run_gb300(args):
         R._lib.check(L.rgpu_steps(h, 1), h)
         R._lib.check(L.rgpu_sim_get_particles(h, host.data_ptr(), n, 112), h)
     barrier()
-    e2e_s = time.perf_counter() - t0
-    e2e = {"value": pairs * e2e_steps * world / e2e_s / 1e9, "unit": "Gpair-int/s",
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist, "cuda")
+    e2e = {"value": job_rate(pairs, e2e_steps, world, e2e_s * 1e3) / 1e9, "unit": "Gpair-int/s",
            "h2d_bytes_per_step": n * 112, "d2h_bytes_per_step": n * 88}
 
     extra = {}
