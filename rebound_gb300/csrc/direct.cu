@@ -226,11 +226,15 @@ __global__ void __launch_bounds__(kBlock) direct_kernel(DirectArgs a, const Ghos
     // FIX: the records are FixBody bit patterns; the displacement is the int64
     // difference converted once (exactly the FP64 subtraction, see FixBody).
     const long long xfi = __double_as_longlong(xi), yfi = __double_as_longlong(yi), zfi = __double_as_longlong(zi);
-    int ebias = 0, fbias = 0, two_s = 0;
+    int ebias = 0, two_s = 0;
+    float sc_hi = 0.f, sc_lo = 0.f;                 // 2^(32 - s), 2^-s (MIXED)
     unsigned long long e0 = 0, e1 = 0, e2 = 0;
     if (FIX) {
         ebias = 1086 - a.fix->shift;
-        fbias = 190 - a.fix->shift;
+        if (MODE == kMixed) {
+            sc_hi = __uint_as_float((unsigned)max(1, min(254, 127 + 32 - a.fix->shift)) << 23);
+            sc_lo = __uint_as_float((unsigned)max(1, min(254, 127 - a.fix->shift)) << 23);
+        }
         two_s = a.fix->two_s;
         e0 = a.fix->e0;
         e1 = a.fix->e1;
@@ -312,15 +316,15 @@ __global__ void __launch_bounds__(kBlock) direct_kernel(DirectArgs a, const Ghos
                 } else {
                     float dxf, dyf, dzf, mf;
                     if (MODE == kMixed && FIX) {
-                        // exact FP64 displacement from the fixed-point positions, rounded once to float
+                        // the exact displacement D (int64, from the fixed-point positions) to float
+                        // as hi 2^32 + lo with two 32-bit conversions and one FFMA (<= 1.5 ulp)
                         const double4_32a q = tile[k];
-                        unsigned long long sgx, sgy, sgz;
-                        const unsigned long long ux = fixpair::abs64(__double_as_longlong(q.x) - xfi, &sgx);
-                        const unsigned long long uy = fixpair::abs64(__double_as_longlong(q.y) - yfi, &sgy);
-                        const unsigned long long uz = fixpair::abs64(__double_as_longlong(q.z) - zfi, &sgz);
-                        dxf = fixpair::abs_to_float(ux, sgx, fbias);
-                        dyf = fixpair::abs_to_float(uy, sgy, fbias);
-                        dzf = fixpair::abs_to_float(uz, sgz, fbias);
+                        const long long Dx = __double_as_longlong(q.x) - xfi;
+                        const long long Dy = __double_as_longlong(q.y) - yfi;
+                        const long long Dz = __double_as_longlong(q.z) - zfi;
+                        dxf = fmaf(__int2float_rn((int)(Dx >> 32)), sc_hi, __uint2float_rn((unsigned)Dx) * sc_lo);
+                        dyf = fmaf(__int2float_rn((int)(Dy >> 32)), sc_hi, __uint2float_rn((unsigned)Dy) * sc_lo);
+                        dzf = fmaf(__int2float_rn((int)(Dz >> 32)), sc_hi, __uint2float_rn((unsigned)Dz) * sc_lo);
                         mf = round_to_float(q.w);
                     } else if (MODE == kMixed) {
                         const double4_32a q = tile[k];

@@ -111,21 +111,6 @@ FIX_HD double abs_to_double(u64 a, u64 sign, int ebias) {
     return a ? bits_double(bits) : 0.0;
 }
 
-// sign * a * 2^-s as a float, round to nearest even; fbias = 190 - s.  Results
-// outside the float range flush to zero or saturate to infinity.
-FIX_HD float abs_to_float(u64 a, u64 sign, int fbias) {
-    const int lz = clz64(a);
-    const u64 n = a << (lz & 63);
-    const u64 r = n + 0x7FFFFFFFFFull + ((n >> 40) & 1ull);          // half an ulp at bit 40, ties to even
-    const int carry = r < n;
-    const u32 frac = carry ? 0u : (u32)((r >> 40) & 0x7FFFFFull);
-    int e = fbias - lz + carry;
-    u32 bits = ((u32)e << 23) | frac;
-    bits = e <= 0 ? 0u : (e >= 255 ? 0x7F800000u : bits);
-    bits |= (u32)sign & 0x80000000u;
-    return a ? bits_float(bits) : 0.0f;
-}
-
 // Seed y0 ~ x^(-1/2) for x in [1, 4) given as float bits.  The device uses the
 // hardware approximation (relative error below 2^-21); the host uses the
 // correctly rounded value, optionally perturbed by a caller-given factor to
