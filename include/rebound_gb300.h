@@ -190,6 +190,11 @@ int64_t rgpu_launch_count(void);
  * the current device: 0 = FP64 FMA, 1 = FP32 FMA, 2 = FP64<->FP32 conversion,
  * 3 = FP32 rsqrt (MUFU), 4 = integer ALU (3-input logic op). */
 int rgpu_probe_rate(int which, double* ops_per_s);
+/* Self-check of the integer-pipe IEEE FP64 division and square root used by the
+ * exact tree walk: n pseudo-random operand sets from `seed`, each compared bit
+ * for bit with the hardware a / b and sqrt(x); *mismatches counts differences.
+ * No reference counterpart. */
+int rgpu_selftest_exactfp(long long n, unsigned long long seed, long long* mismatches);
 
 /* Kepler drift of n independent bodies with gravitational parameters mu[i]
  * over dt[i] (universal variables, Stumpff series, Newton / quartic solver

@@ -3,6 +3,7 @@
 // holds only HBM and BF16-tensor figures).  Each thread runs independent
 // dependency chains so the pipe, not latency, limits the rate.
 #include "rgpu_internal.cuh"
+#include "exactfp.cuh"
 
 namespace {
 
@@ -80,7 +81,59 @@ __global__ void probe_alu(unsigned* out, unsigned m) {
     if (t == 12345u) out[0] = t;
 }
 
+// Self-check of the integer-pipe IEEE division and square root against the
+// hardware operations on pseudo-random normal operands (splitmix64 stream).
+__device__ __forceinline__ unsigned long long splitmix(unsigned long long& s) {
+    unsigned long long z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ double random_double(unsigned long long& s, int emin, int span) {
+    const unsigned long long r = splitmix(s), f = splitmix(s);
+    const int e = emin + (int)(r % (unsigned)span);
+    unsigned long long frac = f & 0xFFFFFFFFFFFFFull;
+    const int pat = (int)((r >> 32) & 7);
+    if (pat == 0) frac = 0;
+    if (pat == 1) frac = 0xFFFFFFFFFFFFFull;
+    if (pat == 2) frac &= 0xFFFFull;
+    if (pat == 3) frac = 0xFFFFFFFFFFFFFull - (frac & 0xFFFFull);
+    const unsigned long long sign = (r >> 40) & 1ull;
+    return __longlong_as_double((long long)((sign << 63) | ((unsigned long long)(e + 1023) << 52) | frac));
+}
+
+__global__ void exactfp_check(long long n, unsigned long long seed, unsigned long long* bad) {
+    unsigned long long local = 0;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        unsigned long long s = seed ^ (0x632BE59BD9B4E019ull * (unsigned long long)(k + 1));
+        const double a = random_double(s, -300, 601), b = random_double(s, -300, 601);
+        const double x = fabs(random_double(s, -1000, 2001));
+        if (__double_as_longlong(exactfp::div_rn(a, b)) != __double_as_longlong(a / b)) local++;
+        if (__double_as_longlong(exactfp::sqrt_rn(x)) != __double_as_longlong(sqrt(x))) local++;
+    }
+    if (local) atomicAdd(bad, local);
+}
+
 }  // namespace
+
+extern "C" int rgpu_selftest_exactfp(long long n, unsigned long long seed, long long* mismatches) {
+    if (!mismatches || n < 0) return RGPU_ERR_ARG;
+    unsigned long long* d = nullptr;
+    if (cudaMalloc(&d, sizeof(unsigned long long)) != cudaSuccess) return RGPU_ERR_NOMEM;
+    cudaMemset(d, 0, sizeof(unsigned long long));
+    int dev = 0, nsm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    exactfp_check<<<nsm * 8, 256>>>(n, seed, d);
+    g_launches++;
+    unsigned long long h = 0;
+    cudaError_t err = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (err != cudaSuccess) return RGPU_ERR_CUDA;
+    *mismatches = (long long)h;
+    return RGPU_OK;
+}
 
 extern "C" int rgpu_probe_rate(int which, double* ops_per_s) {
     if (!ops_per_s || which < 0 || which > 4) return RGPU_ERR_ARG;

@@ -17,6 +17,7 @@
 // 0..7, depth first) with an explicit stack, so accelerations are
 // bit-identical to the reference's serial build.
 #include "rgpu_internal.cuh"
+#include "exactfp.cuh"
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -354,8 +355,9 @@ __global__ void __launch_bounds__(128) walk_exact(ParticlesSoA p, int N, CellArr
                 } else if (pt == i) {
                     continue;
                 }
-                const double rr = sqrt(r2 + eps2);
-                const double pf = -G / (rr * rr * rr) * c.m[q];
+                // IEEE sqrt and division, bit-identical, on the integer pipes (exactfp)
+                const double rr = exactfp::sqrt_rn(r2 + eps2);
+                const double pf = exactfp::div_rn(-G, rr * rr * rr) * c.m[q];
                 ax += pf * dx; ay += pf * dy; az += pf * dz;
             }
         }
@@ -436,8 +438,9 @@ __global__ void __launch_bounds__(128) walk_near(ParticlesSoA p, int N, CellArra
                 } else if (pt == i) {
                     continue;
                 }
-                const double rr = sqrt(r2 + eps2);
-                const double pf = -G / (rr * rr * rr) * c.m[q];
+                // IEEE sqrt and division, bit-identical, on the integer pipes (exactfp)
+                const double rr = exactfp::sqrt_rn(r2 + eps2);
+                const double pf = exactfp::div_rn(-G, rr * rr * rr) * c.m[q];
                 ax += pf * dx; ay += pf * dy; az += pf * dz;
             }
         }
