@@ -269,7 +269,8 @@ typedef struct rgpu_server_config {
     int32_t slots_per_bucket;        /* WHFast slots per body count (default 16,384) */
     int32_t pool_particles;          /* cluster particle pool (default 4,194,304) */
     int32_t cluster_steps_per_tick;  /* default 8 */
-    int32_t reserved;
+    int32_t thread_per_system;       /* 0 (default): one warp per WHFast system, lanes = bodies
+                                        (lowest latency); 1: one thread per system */
 } rgpu_server_config;
 typedef struct rgpu_server_stats {
     int64_t completed, waiting, resident, ticks;

@@ -62,6 +62,189 @@ __global__ void __launch_bounds__(128) wh_slots_kernel(double* __restrict__ st, 
     remaining[sid] = rem - n;
 }
 
+// --- warp per system ---------------------------------------------------------------
+// The same WHFast step (safe_mode = 1, Jacobi coordinates, DEFAULT kernel) with
+// lane i of a warp holding body i, for latency: the Kepler drifts of all bodies
+// and each body's row of pair forces run side by side, and the Jacobi transforms
+// become mass-weighted prefix / suffix sums across lanes.  With C_i the centre of
+// mass of bodies 0..i-1, eta_i their mass and X the centre of mass of all bodies:
+//     q_i = x_i - C_i,    x_i = q_i + X - sum_{k >= i} (m_k / eta_{k+1}) q_k,
+// the closed forms of the recurrences of src/transformations.c:34-81 and :178-226
+// (summed in tree order here, so results agree with the serial form to rounding).
+constexpr unsigned kFull = 0xffffffffu;
+
+template <int NB>
+__device__ __forceinline__ double lane_prefix(double v, int lane) {     // inclusive, lanes >= NB hold 0
+#pragma unroll
+    for (int d = 1; d < NB; d <<= 1) {
+        const double t = __shfl_up_sync(kFull, v, d);
+        if (lane >= d) v += t;
+    }
+    return v;
+}
+
+template <int NB>
+__device__ __forceinline__ double lane_suffix(double v, int lane) {     // inclusive, lanes >= NB hold 0
+#pragma unroll
+    for (int d = 1; d < NB; d <<= 1) {
+        const double t = __shfl_down_sync(kFull, v, d);
+        if (lane + d < 32) v += t;
+    }
+    return v;
+}
+
+template <int NB>
+__device__ __forceinline__ double lane_exclusive(double v, int lane) {  // sum over lanes < lane
+    const double e = __shfl_up_sync(kFull, lane_prefix<NB>(v, lane), 1);
+    return lane == 0 ? 0. : e;
+}
+
+// Advance WHFast slot `sid` of one bucket by up to `chunk` steps; called by a whole warp.
+template <int NB>
+__device__ __noinline__ void warp_advance(double* __restrict__ st, const double* __restrict__ dt,
+                                          int64_t* __restrict__ remaining, int cap, int sid, int chunk, double G,
+                                          uint32_t* status) {
+    const int lane = (int)(threadIdx.x & 31);
+    const int64_t rem = remaining[sid];
+    if (rem <= 0) return;
+    const int nsteps = (int)(rem < chunk ? rem : chunk);
+    const size_t f = (size_t)NB * cap;
+    const bool on = lane < NB;
+    const size_t o = (size_t)(on ? lane : 0) * cap + sid;
+    double x = 0., y = 0., z = 0., vx = 0., vy = 0., vz = 0., m = 0.;
+    if (on) {
+        x = st[o]; y = st[f + o]; z = st[2 * f + o];
+        vx = st[3 * f + o]; vy = st[4 * f + o]; vz = st[5 * f + o]; m = st[6 * f + o];
+    }
+    const double h = dt[sid], h2 = h / 2.;
+    // masses are constant over a request: the prefix masses once
+    const double eta_in = lane_prefix<NB>(m, lane);                  // sum_{k <= i} m_k
+    const double up = __shfl_up_sync(kFull, eta_in, 1);                // every lane takes part in the shuffle
+    const double eta_ex = lane == 0 ? 0. : up;
+    const double Mi = 1. / __shfl_sync(kFull, eta_in, NB - 1);
+    const bool jac = on && lane > 0;                                 // lanes holding a Jacobi body
+    const double ei = jac ? 1. / eta_ex : 0.;
+    const double wf = jac ? m / eta_in : 0.;
+    const double mu = G * eta_in;
+    double mj[NB];
+#pragma unroll
+    for (int j = 0; j < NB; j++) mj[j] = __shfl_sync(kFull, m, j);
+    for (int k = 0; k < nsteps; k++) {
+        // inertial -> Jacobi (lane 0: centre of mass)
+        double qx, qy, qz, ux, uy, uz;
+        {
+            const double Px = lane_prefix<NB>(m * x, lane), Py = lane_prefix<NB>(m * y, lane),
+                         Pz = lane_prefix<NB>(m * z, lane);
+            const double Pvx = lane_prefix<NB>(m * vx, lane), Pvy = lane_prefix<NB>(m * vy, lane),
+                         Pvz = lane_prefix<NB>(m * vz, lane);
+            const double Ex = __shfl_up_sync(kFull, Px, 1), Ey = __shfl_up_sync(kFull, Py, 1),
+                         Ez = __shfl_up_sync(kFull, Pz, 1);
+            const double Evx = __shfl_up_sync(kFull, Pvx, 1), Evy = __shfl_up_sync(kFull, Pvy, 1),
+                         Evz = __shfl_up_sync(kFull, Pvz, 1);
+            const double Tx = __shfl_sync(kFull, Px, NB - 1), Ty = __shfl_sync(kFull, Py, NB - 1),
+                         Tz = __shfl_sync(kFull, Pz, NB - 1);
+            const double Tvx = __shfl_sync(kFull, Pvx, NB - 1), Tvy = __shfl_sync(kFull, Pvy, NB - 1),
+                         Tvz = __shfl_sync(kFull, Pvz, NB - 1);
+            if (lane == 0) {
+                qx = Tx * Mi; qy = Ty * Mi; qz = Tz * Mi; ux = Tvx * Mi; uy = Tvy * Mi; uz = Tvz * Mi;
+            } else {
+                qx = x - Ex * ei; qy = y - Ey * ei; qz = z - Ez * ei;
+                ux = vx - Evx * ei; uy = vy - Evy * ei; uz = vz - Evz * ei;
+            }
+        }
+        // drift dt/2: Kepler per Jacobi body, free drift of the centre of mass
+        if (jac) wh::kepler_solver(qx, qy, qz, ux, uy, uz, mu, h2, status);
+        else if (lane == 0) { qx += h2 * ux; qy += h2 * uy; qz += h2 * uz; }
+        // Jacobi -> inertial positions
+        {
+            const double Xc = __shfl_sync(kFull, qx, 0), Yc = __shfl_sync(kFull, qy, 0), Zc = __shfl_sync(kFull, qz, 0);
+            const double Wx = lane_suffix<NB>(wf * qx, lane), Wy = lane_suffix<NB>(wf * qy, lane),
+                         Wz = lane_suffix<NB>(wf * qz, lane);
+            x = (jac ? qx : 0.) + Xc - Wx; y = (jac ? qy : 0.) + Yc - Wy; z = (jac ? qz : 0.) + Zc - Wz;
+        }
+        // inertial accelerations, all pairs except (0, 1), no softening (src/gravity.c:195-257)
+        double ax = 0., ay = 0., az = 0.;
+#pragma unroll
+        for (int j = 0; j < NB; j++) {
+            const double xj = __shfl_sync(kFull, x, j), yj = __shfl_sync(kFull, y, j), zj = __shfl_sync(kFull, z, j);
+            if (on && j != lane && lane + j != 1) {
+                const double dx = x - xj, dy = y - yj, dz = z - zj;
+                const double r = sqrt(dx * dx + dy * dy + dz * dz);
+                const double pfj = -(G / (r * r * r)) * mj[j];
+                ax += pfj * dx; ay += pfj * dy; az += pfj * dz;
+            }
+        }
+        // kick in Jacobi coordinates (src/transformations.c:147-176, src/integrator_whfast.c:447-472)
+        {
+            const double Sx = lane_exclusive<NB>(m * ax, lane), Sy = lane_exclusive<NB>(m * ay, lane),
+                         Sz = lane_exclusive<NB>(m * az, lane);
+            if (jac) {
+                ux += h * (ax - Sx * ei); uy += h * (ay - Sy * ei); uz += h * (az - Sz * ei);
+                if (lane > 1) {
+                    const double rj2i = 1. / (qx * qx + qy * qy + qz * qz);
+                    const double pf = h * (sqrt(rj2i) * rj2i * G * eta_in);
+                    ux += pf * qx; uy += pf * qy; uz += pf * qz;
+                }
+            }
+        }
+        // drift dt/2
+        if (jac) wh::kepler_solver(qx, qy, qz, ux, uy, uz, mu, h2, status);
+        else if (lane == 0) { qx += h2 * ux; qy += h2 * uy; qz += h2 * uz; }
+        // Jacobi -> inertial positions and velocities
+        {
+            const double Xc = __shfl_sync(kFull, qx, 0), Yc = __shfl_sync(kFull, qy, 0), Zc = __shfl_sync(kFull, qz, 0);
+            const double Vx = __shfl_sync(kFull, ux, 0), Vy = __shfl_sync(kFull, uy, 0), Vz = __shfl_sync(kFull, uz, 0);
+            const double Wx = lane_suffix<NB>(wf * qx, lane), Wy = lane_suffix<NB>(wf * qy, lane),
+                         Wz = lane_suffix<NB>(wf * qz, lane);
+            const double Wvx = lane_suffix<NB>(wf * ux, lane), Wvy = lane_suffix<NB>(wf * uy, lane),
+                         Wvz = lane_suffix<NB>(wf * uz, lane);
+            x = (jac ? qx : 0.) + Xc - Wx; y = (jac ? qy : 0.) + Yc - Wy; z = (jac ? qz : 0.) + Zc - Wz;
+            vx = (jac ? ux : 0.) + Vx - Wvx; vy = (jac ? uy : 0.) + Vy - Wvy; vz = (jac ? uz : 0.) + Vz - Wvz;
+        }
+        if (!on) { x = y = z = vx = vy = vz = 0.; }
+    }
+    if (on) {
+        st[o] = x; st[f + o] = y; st[2 * f + o] = z;
+        st[3 * f + o] = vx; st[4 * f + o] = vy; st[5 * f + o] = vz;
+    }
+    if (lane == 0) remaining[sid] = rem - nsteps;
+}
+
+// One launch per tick over the live slots of every bucket: a unit is up to four
+// consecutive slots of one bucket, one block of four warps.  (Per-bucket launches
+// on concurrent streams stacked their few blocks on the same SMs.)
+struct WarpUnit {
+    double* st;
+    const double* dt;
+    int64_t* remaining;
+    int cap, nb, slot0, nslots;
+};
+
+__global__ void __launch_bounds__(128) wh_warp_units(const WarpUnit* __restrict__ units, int chunk, double G,
+                                                     uint32_t* status) {
+    const WarpUnit U = units[blockIdx.x];
+    const int w = (int)(threadIdx.x >> 5);
+    if (w >= U.nslots) return;                       // whole warps exit together
+    const int sid = U.slot0 + w;
+    switch (U.nb) {
+        case 2: warp_advance<2>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
+        case 3: warp_advance<3>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
+        case 4: warp_advance<4>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
+        case 5: warp_advance<5>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
+        case 6: warp_advance<6>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
+        case 7: warp_advance<7>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
+        case 8: warp_advance<8>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
+        case 9: warp_advance<9>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
+        case 10: warp_advance<10>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
+        case 11: warp_advance<11>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
+        case 12: warp_advance<12>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
+        case 13: warp_advance<13>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
+        case 14: warp_advance<14>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
+        case 15: warp_advance<15>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
+        default: warp_advance<16>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
+    }
+}
+
 typedef void (*WhSlotsFn)(double*, const double*, int64_t*, int, int, double, uint32_t*);
 
 WhSlotsFn wh_slots_for(int nb) {
@@ -211,6 +394,7 @@ struct Request {
 
 struct WhBucket {
     int nb = 0, cap = 0, live = 0;
+    int hw = 0;                     // slots in [hw, cap) have never been used
     double* st = nullptr;           // 7 * nb * cap
     double* dt = nullptr;
     int64_t* remaining = nullptr;
@@ -241,6 +425,12 @@ struct rgpu_server {
     std::unordered_map<int64_t, Request> req;
     std::vector<int64_t> resident[3];
     cudaStream_t kstream[3] = {nullptr, nullptr, nullptr};
+    // one stream per WHFast body count, so the buckets of a tick run side by side
+    // (a tick then lasts as long as its slowest bucket, not the sum of them)
+    cudaStream_t bstream[wh::kMaxBodies + 1] = {};
+    WarpUnit* d_units = nullptr;     // per-tick unit table of the warp-per-system kernel
+    int units_cap = 0;
+    std::vector<WarpUnit> units;
     int64_t next_id = 1;
     size_t bytes_in_use = 0;
     bool stop = false;
@@ -315,6 +505,7 @@ int admit_whfast(rgpu_server* s, Request& r) {
     B.free_slots.pop_back();
     B.owner[q] = r.id;
     B.live++;
+    B.hw = std::max(B.hw, q + 1);
     r.bucket = n;
     r.slot = q;
     r.remaining = r.steps;
@@ -386,16 +577,40 @@ void whfast_worker(rgpu_server* s) {
         std::vector<WhBucket*> live;
         for (auto& kv : s->buckets) if (kv.second.cap && kv.second.live) live.push_back(&kv.second);
         lk.unlock();
-        for (WhBucket* B : live) {
-            wh_slots_for(B->nb)<<<(B->cap + 127) / 128, 128, 0, st>>>(B->st, B->dt, B->remaining, B->cap, chunk,
-                                                                      1.0, s->d_status);
-            g_launches++;
+        if (s->cfg.thread_per_system) {
+            for (WhBucket* B : live) {
+                cudaStream_t bs = s->bstream[B->nb];
+                wh_slots_for(B->nb)<<<(B->hw + 127) / 128, 128, 0, bs>>>(B->st, B->dt, B->remaining, B->cap, chunk,
+                                                                         1.0, s->d_status);
+                g_launches++;
+                B->rem_host.resize(B->cap);
+                cudaMemcpyAsync(B->rem_host.data(), B->remaining, sizeof(int64_t) * B->hw, cudaMemcpyDeviceToHost, bs);
+            }
+            for (WhBucket* B : live) cudaStreamSynchronize(s->bstream[B->nb]);
+        } else {
+            s->units.clear();
+            for (WhBucket* B : live)
+                for (int q0 = 0; q0 < B->hw; q0 += 4)
+                    s->units.push_back(WarpUnit{B->st, B->dt, B->remaining, B->cap, B->nb, q0, std::min(4, B->hw - q0)});
+            const int nu = (int)s->units.size();
+            if (nu > s->units_cap) {
+                cudaFree(s->d_units);
+                s->d_units = nullptr;
+                s->units_cap = 0;
+                if (cudaMalloc(&s->d_units, sizeof(WarpUnit) * (size_t)nu * 2) == cudaSuccess) s->units_cap = nu * 2;
+                else cudaGetLastError();
+            }
+            if (nu && nu <= s->units_cap) {
+                cudaMemcpyAsync(s->d_units, s->units.data(), sizeof(WarpUnit) * nu, cudaMemcpyHostToDevice, st);
+                wh_warp_units<<<nu, 128, 0, st>>>(s->d_units, chunk, 1.0, s->d_status);
+                g_launches++;
+            }
+            for (WhBucket* B : live) {
+                B->rem_host.resize(B->cap);
+                cudaMemcpyAsync(B->rem_host.data(), B->remaining, sizeof(int64_t) * B->hw, cudaMemcpyDeviceToHost, st);
+            }
+            cudaStreamSynchronize(st);
         }
-        for (WhBucket* B : live) {
-            B->rem_host.resize(B->cap);
-            cudaMemcpyAsync(B->rem_host.data(), B->remaining, sizeof(int64_t) * B->cap, cudaMemcpyDeviceToHost, st);
-        }
-        cudaStreamSynchronize(st);
         lk.lock();
         s->ticks++;
         std::vector<int64_t> still, fin;
@@ -575,6 +790,8 @@ int rgpu_server_create(rgpu_server** out, const rgpu_server_config* cfg) {
     bool ok = cudaStreamCreateWithFlags(&s->kstream[RGPU_SERVE_WHFAST], cudaStreamNonBlocking) == cudaSuccess &&
               cudaStreamCreateWithFlags(&s->kstream[RGPU_SERVE_CLUSTER], cudaStreamNonBlocking) == cudaSuccess &&
               cudaMalloc(&s->d_status, 4) == cudaSuccess && cudaMemset(s->d_status, 0, 4) == cudaSuccess;
+    for (int nb = 2; ok && nb <= wh::kMaxBodies; nb++)
+        ok = cudaStreamCreateWithFlags(&s->bstream[nb], cudaStreamNonBlocking) == cudaSuccess;
     for (int k = 0; ok && k < 10; k++) ok = cudaMalloc(f[k], sizeof(double) * P) == cudaSuccess;
     ok = ok && cudaMalloc(&s->pool.split, sizeof(float4) * 2 * (size_t)P) == cudaSuccess;
     if (!ok) { cudaGetLastError(); rgpu_server_free(s); return RGPU_ERR_NOMEM; }
@@ -594,6 +811,7 @@ void rgpu_server_free(rgpu_server* s) {
     s->cv_work.notify_all();
     for (auto& w : s->worker) if (w.joinable()) w.join();
     for (cudaStream_t st : s->kstream) if (st) cudaStreamSynchronize(st);
+    for (cudaStream_t st : s->bstream) if (st) cudaStreamSynchronize(st);
     for (auto& kv : s->buckets) { cudaFree(kv.second.st); cudaFree(kv.second.dt); cudaFree(kv.second.remaining); }
     double* f[10] = {s->pool.x, s->pool.y, s->pool.z, s->pool.vx, s->pool.vy, s->pool.vz,
                      s->pool.ax, s->pool.ay, s->pool.az, s->pool.m};
@@ -601,8 +819,10 @@ void rgpu_server_free(rgpu_server* s) {
     cudaFree(s->pool.split);
     cudaFree(s->d_items);
     cudaFree(s->d_slots);
+    cudaFree(s->d_units);
     cudaFree(s->d_status);
     for (cudaStream_t st : s->kstream) if (st) cudaStreamDestroy(st);
+    for (cudaStream_t st : s->bstream) if (st) cudaStreamDestroy(st);
     delete s;
 }
 

@@ -21,13 +21,13 @@ WHFAST, CLUSTER = 1, 2
 
 class Server:
     def __init__(self, hbm_budget_bytes=None, steps_per_launch=None, slots_per_bucket=None, pool_particles=None,
-                 cluster_steps_per_tick=None):
+                 cluster_steps_per_tick=None, thread_per_system=None):
         self._L = _lib.load()
         cfg = ServerConfig()
         self._L.rgpu_server_config_default(ctypes.byref(cfg))
         for k, v in dict(hbm_budget_bytes=hbm_budget_bytes, steps_per_launch=steps_per_launch,
                          slots_per_bucket=slots_per_bucket, pool_particles=pool_particles,
-                         cluster_steps_per_tick=cluster_steps_per_tick).items():
+                         cluster_steps_per_tick=cluster_steps_per_tick, thread_per_system=thread_per_system).items():
             if v is not None:
                 setattr(cfg, k, v)
         h = ctypes.c_void_p()

@@ -36,10 +36,15 @@ def test_results_identical_alone_and_in_the_mix(gpu):
         assert same(out, mixed[q]), q
 
 
-def test_results_track_plain_path(gpu):
-    from rebound_gb300.serve import run_stream, WHFAST
+@pytest.mark.parametrize("thread_per_system", [0, 1])
+def test_results_track_plain_path(gpu, thread_per_system):
+    # 0: warp per WHFast system (lanes = bodies, prefix-sum Jacobi transforms);
+    # 1: thread per system (the serial restatement)
+    from rebound_gb300.serve import Server, run_stream, WHFAST
     reqs = small_stream(gpu, 12)
-    _, res, _, _ = run_stream(reqs, rate=1000.0)
+    srv = Server(thread_per_system=thread_per_system)
+    _, res, _, _ = run_stream(reqs, rate=1000.0, server=srv)
+    srv.close()
     checked = {1: 0, 2: 0}
     for (kind, p, dt, steps, G, soft), out in zip(reqs, res):
         sim = gpu.Simulation()
