@@ -287,7 +287,13 @@ __global__ void __launch_bounds__(kBlock) direct_kernel(DirectArgs a, const Ghos
                         dx = fixpair::limbs_to_double(xh, xl, sx_, ebias - 1);
                         dy = fixpair::limbs_to_double(yh, yl, sy_, ebias - 1);
                         dz = fixpair::limbs_to_double(zh, zl, sz_, ebias - 1);
-                        s = q.w * fixpair::rinv3_limbs<true>(xh, xl, yh, yl, zh, zl, e0, e1, e2, two_s);
+                        // COMPENSATED is FP64-bound (Kahan terms): G m folded into the integer
+                        // factor saves its DMUL; BASIC is integer-bound: the DMUL is cheaper there.
+                        if (MODE == kComp)
+                            s = fixpair::rinv3m_limbs<true>(xh, xl, yh, yl, zh, zl, e0, e1, e2, two_s,
+                                                            (unsigned long long)__double_as_longlong(q.w));
+                        else
+                            s = q.w * fixpair::rinv3_limbs<true>(xh, xl, yh, yl, zh, zl, e0, e1, e2, two_s);
                     } else if (FIX) {
                         unsigned long long sgx, sgy, sgz;
                         const unsigned long long ux = fixpair::abs64(__double_as_longlong(q.x) - xfi, &sgx);

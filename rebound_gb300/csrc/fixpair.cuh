@@ -200,10 +200,11 @@ FIX_HD double limbs_to_double(u32 ah, u32 al, u32 sg, int ebias1) {
 
 // The factor (r^2 + eps^2)^(-3/2) from the limbs of |dx|, |dy|, |dz| (< 2^62
 // each), with eps^2 2^2s pre-split as e0 + e1 2^32 + e2 2^62 (e0 < 2^32,
-// e1 < 2^30, e2 < 2^62).  UNIFORM: all 32 lanes of the warp call it together
-// (lets the common normalisation take a warp-uniform branch).
+// e1 < 2^30, e2 < 2^62), as F 2^(e3 - 59) with F in [2^58, 2^62).  Returns false
+// for a zero radius.  UNIFORM: all 32 lanes of the warp call it together (lets
+// the common normalisation take a warp-uniform branch).
 template <bool UNIFORM>
-FIX_HD double rinv3_limbs(u32 xh, u32 xl, u32 yh, u32 yl, u32 zh, u32 zl, u64 e0, u64 e1, u64 e2, int two_s) {
+FIX_HD bool rinv3_core(u32 xh, u32 xl, u32 yh, u32 yl, u32 zh, u32 zl, u64 e0, u64 e1, u64 e2, int two_s, u64& F, int& e3) {
     // 1. r^2 + eps^2 = S2 2^62 + S1 2^32 + S0 with a 31-bit split b = bh 2^31 + bl:
     //    b^2 = bh^2 2^62 + bh bl 2^32 + bl^2, each product < 2^62, no carries.
     u64 S0 = e0, S1 = e1, S2 = e2;
@@ -237,7 +238,7 @@ FIX_HD double rinv3_limbs(u32 xh, u32 xl, u32 yh, u32 yl, u32 zh, u32 zl, u64 e0
         Tl = shf_l(r1, r2, lz - 1);
     } else {
         const u64 hi = m2, lo = ((u64)r1 << 32) | (u32)S0;
-        if ((hi | lo) == 0) return bits_double(0x7FF0000000000000ull);
+        if ((hi | lo) == 0) return false;
         u64 T;
         if (hi) {
             lz = clz64(hi);
@@ -280,17 +281,59 @@ FIX_HD double rinv3_limbs(u32 xh, u32 xl, u32 yh, u32 yl, u32 zh, u32 zl, u64 e0
     const u64 Y2s = wide(Y8, Y8);
     const u64 Y3 = mad_wide((u32)(Y2s >> 32), Y8, (u64)mulhi32((u32)Y2s, Y8));
     const u32 Y3h = (u32)(Y3 >> 32), Y3l = (u32)Y3, Mh = (u32)(M1 >> 32), Ml = (u32)M1;
-    const u64 F = mad_wide(Y3h, Mh, (u64)mulhi32(Y3h, Ml) + mulhi32(Y3l, Mh));   // F 2^(3 ey - 59) = y0^3 (1+c)
-    // 5. (r^2)^(-3/2) = F 2^(3 ey - 59 - 3k), rounded to double
-    const u32 Fh = (u32)(F >> 32), Fl = (u32)F;
-    const int lzf = clz32(Fh);
-    const u32 nh = shf_l(Fl, Fh, lzf), nl = Fl << lzf;
-    const int be1 = 1026 - lzf + 3 * (ey - k);
-    const u32 bhi = ((u32)be1 << 20) + (nh >> 11);
+    F = mad_wide(Y3h, Mh, (u64)mulhi32(Y3h, Ml) + mulhi32(Y3l, Mh));   // F 2^(3 ey - 59) = y0^3 (1+c)
+    e3 = 3 * (ey - k);                                                // (r^2)^(-3/2) = F 2^(e3 - 59)
+    return true;
+}
+
+// sign-less n 2^(be1 + 1 - 1086) for a 64-bit n with bit 63 set, rounded to double.
+FIX_HD double assemble(u32 nh, u32 nl, int be1) {
+    const u32 bhi = ((u32)be1 << 20) + (nh >> 11);                    // the leading 1 adds the last exponent unit
     const u32 blo = shf_l(nl, nh, 21);
-    const u64 bits = (((u64)bhi << 32) | blo) + ((nl >> 10) & 1u);
+    const u64 bits = (((u64)bhi << 32) | blo) + ((nl >> 10) & 1u);   // round: carries into the exponent if needed
     if ((unsigned)be1 > 2045u) return be1 < 0 ? 0.0 : bits_double(0x7FF0000000000000ull);
     return bits_double(bits);
+}
+
+// 5. (r^2)^(-3/2) = F 2^(e3 - 59), rounded to double.
+FIX_HD double finish_f(u64 F, int e3) {
+    const u32 Fh = (u32)(F >> 32), Fl = (u32)F;
+    const int lzf = clz32(Fh);                                       // F >= 2^58: Fh != 0
+    return assemble(shf_l(Fl, Fh, lzf), Fl << lzf, 1026 - lzf + e3);
+}
+
+// 5'. G m (r^2)^(-3/2): the 53-bit mantissa of G m (double bits gm) multiplied in
+// before the one rounding (the high 64 bits of F 2^2 x mantissa 2^11; the
+// low-by-low partial product lies below the last kept bit).  A zero, subnormal
+// or non-finite G m takes an FP64 product.
+FIX_HD double finish_mf(u64 F, int e3, u64 gm) {
+    const int em = (int)((gm >> 52) & 0x7FF);
+    if ((unsigned)(em - 1) >= 2046u) return bits_double(gm) * finish_f(F, e3);
+    const u64 A = F << 2, B = (((gm & 0xFFFFFFFFFFFFFull) | (1ull << 52)) << 11);
+    const u32 ah = (u32)(A >> 32), al = (u32)A, bh = (u32)(B >> 32), bl = (u32)B;
+    const u64 P = mad_wide(ah, bh, (u64)mulhi32(ah, bl) + mulhi32(al, bh));   // F m 2^-51, in [2^59, 2^64)
+    const u32 Ph = (u32)(P >> 32), Pl = (u32)P;
+    const int lzp = clz32(Ph);
+    return assemble(shf_l(Pl, Ph, lzp), Pl << lzp, em + 2 - lzp + e3);
+}
+
+template <bool UNIFORM>
+FIX_HD double rinv3_limbs(u32 xh, u32 xl, u32 yh, u32 yl, u32 zh, u32 zl, u64 e0, u64 e1, u64 e2, int two_s) {
+    u64 F;
+    int e3;
+    if (!rinv3_core<UNIFORM>(xh, xl, yh, yl, zh, zl, e0, e1, e2, two_s, F, e3)) return bits_double(0x7FF0000000000000ull);
+    return finish_f(F, e3);
+}
+
+// G m / (r^2 + eps^2)^(3/2) with G m given as double bits.
+template <bool UNIFORM>
+FIX_HD double rinv3m_limbs(u32 xh, u32 xl, u32 yh, u32 yl, u32 zh, u32 zl, u64 e0, u64 e1, u64 e2, int two_s,
+                           u64 gm) {
+    u64 F;
+    int e3;
+    if (!rinv3_core<UNIFORM>(xh, xl, yh, yl, zh, zl, e0, e1, e2, two_s, F, e3))
+        return bits_double(gm) * bits_double(0x7FF0000000000000ull);          // as G m / 0
+    return finish_mf(F, e3, gm);
 }
 
 }  // namespace fixpair
