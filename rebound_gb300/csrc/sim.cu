@@ -186,22 +186,31 @@ __global__ void sei_second(ParticlesSoA p, int N, SeiCoef c) {
 
 struct BoxCoef { double bx, by, bz, offp1, offm1, dvy; int shear; };
 
-// src/boundary.c:78-135 (shear and periodic wrap).
-__global__ void boundary_wrap(ParticlesSoA p, int N, BoxCoef b) {
+// src/boundary.c:78-135 (shear and periodic wrap): the reference's repeated
+// whole-box shifts, each loop capped at kWrapCap shifts.  A coordinate further out
+// (or infinite) is left where it is and reported, instead of looping on it.
+constexpr int kWrapCap = 1024;
+
+__global__ void boundary_wrap(ParticlesSoA p, int N, BoxCoef b, uint32_t* status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     double x = p.x[i], y = p.y[i], z = p.z[i], vy = p.vy[i];
+    int nx = 0, ny = 0, nz = 0;
     if (b.shear) {
-        while (x > b.bx / 2.) { x -= b.bx; y += b.offp1; vy += b.dvy; }
-        while (x < -b.bx / 2.) { x += b.bx; y += b.offm1; vy -= b.dvy; }
+        for (; x > b.bx / 2. && nx < kWrapCap; nx++) { x -= b.bx; y += b.offp1; vy += b.dvy; }
+        for (; x < -b.bx / 2. && nx < kWrapCap; nx++) { x += b.bx; y += b.offm1; vy -= b.dvy; }
     } else {
-        while (x > b.bx / 2.) x -= b.bx;
-        while (x < -b.bx / 2.) x += b.bx;
+        for (; x > b.bx / 2. && nx < kWrapCap; nx++) x -= b.bx;
+        for (; x < -b.bx / 2. && nx < kWrapCap; nx++) x += b.bx;
     }
-    while (y > b.by / 2.) y -= b.by;
-    while (y < -b.by / 2.) y += b.by;
-    while (z > b.bz / 2.) z -= b.bz;
-    while (z < -b.bz / 2.) z += b.bz;
+    for (; y > b.by / 2. && ny < kWrapCap; ny++) y -= b.by;
+    for (; y < -b.by / 2. && ny < kWrapCap; ny++) y += b.by;
+    for (; z > b.bz / 2. && nz < kWrapCap; nz++) z -= b.bz;
+    for (; z < -b.bz / 2. && nz < kWrapCap; nz++) z += b.bz;
+    if (nx >= kWrapCap || ny >= kWrapCap || nz >= kWrapCap) {
+        atomicOr(status, DEV_ERR_OUT_OF_BOX);
+        return;
+    }
     p.x[i] = x; p.y[i] = y; p.z[i] = z; p.vy[i] = vy;
 }
 
@@ -325,7 +334,7 @@ int boundary_check(rgpu_sim* s) {
     b.offp1 = -fmod(-1.5 * c.OMEGA * b.bx * c.t + b.by / 2., b.by) - b.by / 2.;
     b.offm1 = -fmod(1.5 * c.OMEGA * b.bx * c.t - b.by / 2., b.by) + b.by / 2.;
     b.dvy = 3. / 2. * c.OMEGA * b.bx;
-    boundary_wrap<<<grid_for(N, 256), 256, 0, s->stream>>>(s->p, N, b);
+    boundary_wrap<<<grid_for(N, 256), 256, 0, s->stream>>>(s->p, N, b, s->d_status);
     g_launches++;
     return RGPU_OK;
 }
@@ -510,7 +519,9 @@ int rgpu_integrate(rgpu_sim* s, double tmax) {
             RGPU_TRY(rc);
             break;
         }
+        const double t_before = s->cfg.t;
         RGPU_TRY(rgpu_steps(s, 1));
+        if (s->cfg.t == t_before) return set_error(s, RGPU_ERR_ARG, "dt too small to advance t");
     }
     if (s->cfg.integrator == RGPU_INTEGRATOR_WHFAST) RGPU_TRY(whfast_synchronize(s));
     return read_status(s);

@@ -329,8 +329,78 @@ def fixture_sei_periodic():
     np.savez_compressed(os.path.join(HERE, "sei_shear.npz"), particles=p0, after20=state(sim), meta=meta)
 
 
+def fixture_reference_cases():
+    """Scenarios of the reference's own unit tests for this path (leapfrog and
+    WHFast energy thresholds, forward/backward reversibility), with the inputs the
+    reference builds (its "outer solar system" data set, orbital elements) and
+    the errors the reference itself reaches on them."""
+    import math
+    out = {}
+
+    def rel(a, b):
+        return abs((a - b) / b)
+
+    # outer solar system, moved to the centre of mass (rebound/tests/test_leapfrog.py:7-9)
+    sim = rebound.Simulation()
+    sim.add("outer solar system")
+    sim.move_to_com()
+    out["oss"] = state(sim)
+    sim.integrator = "leapfrog"
+    sim.dt = 1.
+    e0 = sim.energy()
+    sim.integrate(1e3)
+    out["oss_leapfrog_err"] = rel(e0, sim.energy())          # test_leapfrog.py:14-22 (bar 1e-3)
+    sim = rebound.Simulation()
+    sim.add("outer solar system")
+    sim.integrator = "whfast"
+    sim.dt = 0.005 * 12. * 2. * 3.1415
+    out["oss_raw"] = state(sim)
+    e0 = sim.energy()
+    sim.integrate(1000. * 2. * 3.1415)
+    out["oss_whfast_err"] = rel(e0, sim.energy())            # test_whfast.py:20-29 (bar 2.4e-8)
+    # hyperbolic orbit (test_whfast.py:43-54, bar 1e-14)
+    sim = rebound.Simulation()
+    sim.add(m=1.)
+    sim.add(m=1e-3, a=-1., e=2.5)
+    out["hyper"] = state(sim)
+    yr = -sim.particles[1].P
+    out["hyper_yr"] = yr
+    sim.integrator = "whfast"
+    sim.dt = 0.00512 * yr
+    e0 = sim.energy()
+    sim.integrate(1e2 * yr)
+    out["hyper_err"] = rel(e0, sim.energy())
+    # two planets (test_whfast.py:56-69, bar 1.2e-8)
+    sim = rebound.Simulation()
+    sim.add(m=1.)
+    sim.add(m=1e-3, a=1., e=.1)
+    sim.add(m=1e-3, a=3., e=0.1)
+    out["two"] = state(sim)
+    sim.integrator = "whfast"
+    sim.dt = 0.005123 * 2. * math.pi
+    e0 = sim.energy()
+    sim.integrate(1e3 * 2. * math.pi)
+    out["two_err"] = rel(e0, sim.energy())
+    # forward then backward (test_whfast.py:307-345, bars 1e-14 and 1e-13)
+    for name, kw, per_sign in (("bf_hyper", dict(a=-1., e=2.5, omega=0.3, Omega=0.4, inc=0.1), -1.),
+                               ("bf_ecc", dict(a=1.4, e=0.0125, omega=0.3, Omega=0.4, inc=0.1), 1.)):
+        sim = rebound.Simulation()
+        sim.add(m=1.)
+        sim.add(m=1e-3, **kw)
+        out[name] = state(sim)
+        yr = per_sign * sim.particles[1].P
+        sim.integrator = "whfast"
+        sim.dt = 0.0512 * yr
+        out[name + "_dt"] = sim.dt
+        sim.steps(100)
+        sim.dt *= -1
+        sim.steps(100)
+        out[name + "_end"] = state(sim)
+    np.savez_compressed(os.path.join(HERE, "reference_cases.npz"), **out)
+
+
 if __name__ == "__main__":
-    which = sys.argv[2:] or ["gravity_cases", "ring", "whfast", "sei", "gravity_plummer"]
+    which = sys.argv[2:] or ["gravity_cases", "ring", "whfast", "sei", "gravity_plummer", "reference_cases"]
     for w in which:
         print("generating", w, flush=True)
         globals()["fixture_" + w]() if w != "sei" else fixture_sei_periodic()
