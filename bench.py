@@ -317,6 +317,7 @@ def run_gb300(args):
         try:
             from rebound_gb300 import ensemble as E
             extra["ensemble"] = E.bench_summary(quick=args.quick)
+            extra["ensemble"]["cpu_baseline"] = ensemble_cpu_baseline(seconds=2.0 if args.quick else 8.0)
         except Exception as ex:  # reported, not hidden
             extra["ensemble"] = {"error": repr(ex)}
     if args.tree and rank == 0 and not args.lite:
@@ -454,6 +455,38 @@ def ensemble_only(args):
     ms = ens.time_steps(args.ens_steps)
     return {"systems": args.ens_systems, "steps": args.ens_steps, "block": args.ens_block,
             "system_steps_per_s": args.ens_systems * args.ens_steps / (ms * 1e-3)}
+
+
+def ensemble_cpu_baseline(seconds=8.0, seed=3):
+    """The oracle's port of the reference's single-simulation WHFast step
+    (src/integrator_whfast.c:1113-1259) on every host core, one system per thread
+    at a time, over a sample of the configuration-4 systems (same generator, same
+    dt = P_inner / 20).  ctypes releases the GIL during each foreign call, so the
+    threads run in parallel; each call advances one system by a whole sample."""
+    import concurrent.futures as cf
+    from oracle import oracle as O
+    from rebound_gb300 import ics
+    O.build()
+    L = O.lib()
+    cores = os.cpu_count() or 1
+    n_sys = 4 * cores
+    systems, periods = ics.planetary_systems(n_sys, seed=seed)
+    sims = [O.Sim(systems[q], dt=float(periods[q]) / 20.0) for q in range(n_sys)]
+    t0 = time.perf_counter()
+    L.orc_whfast_steps(sims[0].ref, 500)
+    per_step = max((time.perf_counter() - t0) / 500, 1e-7)
+    steps = max(200, int(seconds * cores / (n_sys * per_step)))
+
+    def run(q):
+        L.orc_whfast_steps(sims[q].ref, steps)
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=cores) as ex:
+        list(ex.map(run, range(n_sys)))
+    el = time.perf_counter() - t0
+    return {"value": n_sys * steps / el, "unit": "system-steps/s", "cores": cores, "kind": "port",
+            "sample": f"{n_sys} of the 65,536 systems (k in [2, 10]) x {steps} steps, oracle WHFast, "
+                      f"one thread per core ({el:.1f} s)"}
 
 
 def profiled_counts():

@@ -968,6 +968,11 @@ void orc_whfast_step(orc_sim* r) {                                /* :1113-1259 
     r->t += dt / 2.;
 }
 
+/* n WHFast steps in a row (one foreign call for a whole timing sample). */
+void orc_whfast_steps(orc_sim* r, long n) {
+    for (long k = 0; k < n; k++) orc_whfast_step(r);
+}
+
 /* ------------------------------------------------------------------------
  * Energy: src/tools.c:108-162 (no softening, test-particle aware).
  * ---------------------------------------------------------------------- */

@@ -95,6 +95,7 @@ size_t orc_collision_search_tree(orc_sim* r, orc_collision* out, size_t cap);
 void orc_leapfrog_step(orc_sim* r, int gravity);              /* order 2 DKD */
 void orc_sei_step(orc_sim* r, int gravity);
 void orc_whfast_step(orc_sim* r);                             /* Jacobi, DEFAULT kernel */
+void orc_whfast_steps(orc_sim* r, long n);                    /* n steps (timing) */
 void orc_whfast_synchronize(orc_sim* r);
 void orc_whfast_kepler_solver(orc_particle* p, double mu, double dt);
 void orc_inertial_to_jacobi_posvel(const orc_particle* ps, orc_particle* pj, const orc_particle* pm, size_t N, size_t N_active);

@@ -85,6 +85,8 @@ def lib():
         L.orc_gravity_basic_omp_rows.argtypes = [P, ctypes.c_size_t, ctypes.c_size_t]
         L.orc_gravity_compensated_omp_rows.argtypes = [P, ctypes.c_size_t, ctypes.c_size_t]
         L.orc_gravity_tree_rows.argtypes = [P, ctypes.c_size_t, ctypes.c_size_t]
+        L.orc_whfast_steps.argtypes = [P, ctypes.c_long]
+        L.orc_whfast_steps.restype = None
         L.orc_leapfrog_step.argtypes = [P, ctypes.c_int]
         L.orc_sei_step.argtypes = [P, ctypes.c_int]
         L.orc_collision_search_direct.argtypes = [P, ctypes.c_void_p, ctypes.c_size_t]
