@@ -653,6 +653,47 @@ void orc_leapfrog_step(orc_sim* r, int gravity) {
     lf_drift(r, dt * 0.5);
 }
 
+/* Orders 4, 6 and 8: src/integrator_leapfrog.c:68-70 (coefficients) and :111-196
+ * (stage sequences), restated as a drift, then per stage accelerations, kick and
+ * drift, with the same expression for every drift and kick length. */
+static const double orc_lf4_a = 0.675603595979828817023843904485;
+static const double orc_lf6_a[5] = {0.1867, 0.5554970237124784, 0.1294669489134754, -0.843265623387734,
+                                    0.9432033015235604};
+static const double orc_lf8_a[9] = {0.128865979381443, 0.581514087105251, -0.410175371469850, 0.1851469357165877,
+                                    -0.4095523434208514, 0.1444059410800120, 0.2783355003936797,
+                                    0.3149566839162949, -0.6269948254051343979};
+
+int orc_leapfrog_step_order(orc_sim* r, int gravity, int order) {
+    if (order == 2) { orc_leapfrog_step(r, gravity); return 0; }
+    r->gravity_ignore_terms = 0;
+    const double dt = r->dt;
+    if (order == 4) {
+        const double a = orc_lf4_a;
+        lf_drift(r, dt * a);
+        update_accel(r, gravity); lf_kick(r, dt * 2. * a); lf_drift(r, dt * (0.5 - a));
+        update_accel(r, gravity); lf_kick(r, dt * (1. - 4. * a)); lf_drift(r, dt * (0.5 - a));
+        update_accel(r, gravity); lf_kick(r, dt * 2. * a); lf_drift(r, dt * a);
+        return 0;
+    }
+    if (order != 6 && order != 8) return 1;
+    const double* a = order == 6 ? orc_lf6_a : orc_lf8_a;
+    const int m = order == 6 ? 5 : 9;
+    lf_drift(r, dt * a[0] * 0.5);
+    /* up the coefficient list and back down: kicks a0..a[m-1]..a0 */
+    for (int i = 0; i < m; i++) {
+        update_accel(r, gravity);
+        lf_kick(r, dt * a[i]);
+        if (i + 1 < m) lf_drift(r, dt * (a[i] + a[i + 1]) * 0.5);
+    }
+    for (int i = m - 2; i >= 0; i--) {
+        lf_drift(r, dt * (a[i] + a[i + 1]) * 0.5);
+        update_accel(r, gravity);
+        lf_kick(r, dt * a[i]);
+    }
+    lf_drift(r, dt * a[0] * 0.5);
+    return 0;
+}
+
 /* ------------------------------------------------------------------------
  * SEI: src/integrator_sei.c:86-174.
  * ---------------------------------------------------------------------- */

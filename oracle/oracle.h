@@ -94,6 +94,7 @@ size_t orc_collision_search_tree(orc_sim* r, orc_collision* out, size_t cap);
 /* Integrators. */
 void orc_leapfrog_step(orc_sim* r, int gravity);              /* order 2 DKD */
 void orc_sei_step(orc_sim* r, int gravity);
+int orc_leapfrog_step_order(orc_sim* r, int gravity, int order);   /* order 2, 4, 6, 8; nonzero: unsupported */
 void orc_whfast_step(orc_sim* r);                             /* Jacobi, DEFAULT kernel */
 void orc_whfast_steps(orc_sim* r, long n);                    /* n steps (timing) */
 void orc_whfast_synchronize(orc_sim* r);

@@ -88,6 +88,8 @@ def lib():
         L.orc_whfast_steps.argtypes = [P, ctypes.c_long]
         L.orc_whfast_steps.restype = None
         L.orc_leapfrog_step.argtypes = [P, ctypes.c_int]
+        L.orc_leapfrog_step_order.argtypes = [P, ctypes.c_int, ctypes.c_int]
+        L.orc_leapfrog_step_order.restype = ctypes.c_int
         L.orc_sei_step.argtypes = [P, ctypes.c_int]
         L.orc_collision_search_direct.argtypes = [P, ctypes.c_void_p, ctypes.c_size_t]
         L.orc_collision_search_direct.restype = ctypes.c_size_t
@@ -151,9 +153,10 @@ class Sim:
         fn(self.ref)
         return self.acc()
 
-    def leapfrog(self, steps, gravity="basic"):
+    def leapfrog(self, steps, gravity="basic", order=2):
         for _ in range(steps):
-            lib().orc_leapfrog_step(self.ref, GRAVITY[gravity])
+            if lib().orc_leapfrog_step_order(self.ref, GRAVITY[gravity], order):
+                raise ValueError("leapfrog order must be 2, 4, 6 or 8")
 
     def sei(self, steps, gravity="tree"):
         for _ in range(steps):

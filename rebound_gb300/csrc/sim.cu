@@ -282,16 +282,68 @@ int update_acceleration(rgpu_sim* s) {
     }
 }
 
+// Composition coefficients of the order-4, -6 and -8 leapfrog schemes
+// (src/integrator_leapfrog.c:68-70): the order-4 value is Yoshida's
+// 1 / (2 (2 - 2^(1/3))); the order-6 and -8 kick weights are the symmetric
+// composition coefficients the reference uses, kept digit for digit so that the
+// drift and kick lengths round exactly as there.
+constexpr double kLf4A = 0.675603595979828817023843904485;
+constexpr double kLf6A[5] = {0.1867, 0.5554970237124784, 0.1294669489134754, -0.843265623387734, 0.9432033015235604};
+constexpr double kLf8A[9] = {0.128865979381443, 0.581514087105251, -0.410175371469850, 0.1851469357165877,
+                             -0.4095523434208514, 0.1444059410800120, 0.2783355003936797, 0.3149566839162949,
+                             -0.6269948254051343979};
+
+// Drift lengths d[0..nk] and kick lengths k[0..nk-1] of one step: the scheme is
+// D(d0) [a K(k0) D(d1)] ... [a K(k_{nk-1}) D(d_nk)], with the reference's own
+// expressions for each length (src/integrator_leapfrog.c:97-203).
+int leapfrog_scheme(int order, double dt, double* d, double* k) {
+    switch (order) {
+        case 0:
+        case 2:
+            d[0] = dt * 0.5; k[0] = dt; d[1] = dt * 0.5;
+            return 1;
+        case 4:
+            d[0] = dt * kLf4A; k[0] = dt * 2. * kLf4A; d[1] = dt * (0.5 - kLf4A);
+            k[1] = dt * (1. - 4. * kLf4A); d[2] = dt * (0.5 - kLf4A); k[2] = dt * 2. * kLf4A; d[3] = dt * kLf4A;
+            return 3;
+        case 6:
+        case 8: {
+            const double* a = order == 6 ? kLf6A : kLf8A;
+            const int m = order == 6 ? 5 : 9;
+            const int nk = 2 * m - 1;                // kick weights a0 .. a_{m-1} .. a0
+            d[0] = dt * a[0] * 0.5;
+            for (int q = 0; q < nk; q++) {
+                const int ia = q < m ? q : nk - 1 - q;
+                k[q] = dt * a[ia];
+                if (q + 1 < nk) {
+                    const int ib = q + 1 < m ? q + 1 : nk - 2 - q;
+                    const int lo = ia < ib ? ia : ib, hi = ia < ib ? ib : ia;
+                    d[q + 1] = dt * (a[lo] + a[hi]) * 0.5;
+                }
+            }
+            d[nk] = dt * a[0] * 0.5;
+            return nk;
+        }
+        default:
+            return -1;
+    }
+}
+
 int leapfrog_step(rgpu_sim* s) {
-    // src/integrator_leapfrog.c:97-107 (order 2): D(dt/2) a K(dt) D(dt/2).
+    // src/integrator_leapfrog.c:97-203: drift, then (accelerations, kick, drift) per stage;
+    // the time advances with each drift as in the reference.
     const int N = (int)s->N;
-    const double dt = s->cfg.dt;
     s->cfg.gravity_ignore_terms = 0;
-    if (N) { lf_drift<<<grid_for(N, 256), 256, 0, s->stream>>>(s->p, N, dt * 0.5); g_launches++; }
-    s->cfg.t += dt * 0.5;
-    RGPU_TRY(update_acceleration(s));
-    if (N) { lf_kick_drift<<<grid_for(N, 256), 256, 0, s->stream>>>(s->p, N, dt, dt * 0.5); g_launches++; }
-    s->cfg.t += dt * 0.5;
+    double d[18], k[17];
+    const int nk = leapfrog_scheme(s->cfg.leapfrog_order, s->cfg.dt, d, k);
+    if (nk < 0) return set_error(s, RGPU_ERR_ARG, "leapfrog order must be 2, 4, 6 or 8");
+    if (N) { lf_drift<<<grid_for(N, 256), 256, 0, s->stream>>>(s->p, N, d[0]); g_launches++; }
+    s->cfg.t += d[0];
+    for (int q = 0; q < nk; q++) {
+        RGPU_TRY(update_acceleration(s));
+        if (N) { lf_kick_drift<<<grid_for(N, 256), 256, 0, s->stream>>>(s->p, N, k[q], d[q + 1]); g_launches++; }
+        s->cfg.t += d[q + 1];
+    }
     return RGPU_OK;
 }
 

@@ -399,8 +399,39 @@ def fixture_reference_cases():
     np.savez_compressed(os.path.join(HERE, "reference_cases.npz"), **out)
 
 
+def fixture_leapfrog_orders():
+    """Leapfrog orders 4, 6, 8 (src/integrator_leapfrog.c:97-203): 20 steps of a
+    softened 128-body Plummer sphere with BASIC gravity, and the outer-solar-system
+    energy errors of rebound/tests/test_leapfrog.py:24-56 (integrate(1e3), steps(1))."""
+    out = {}
+    p0 = plummer_truncated(128, seed=21)
+    out["particles"] = p0
+    for order in (4, 6, 8):
+        sim = rebound.Simulation()
+        load(sim, p0)
+        sim.softening = 0.01
+        sim.integrator = "leapfrog"
+        sim.integrator.order = order
+        sim.dt = 1e-3
+        sim.steps(20)
+        out["after20_o%d" % order] = state(sim)
+        out["t_o%d" % order] = sim.t
+        sim = rebound.Simulation()
+        sim.add("outer solar system")
+        sim.move_to_com()
+        sim.integrator = "leapfrog"
+        sim.integrator.order = order
+        sim.dt = 1
+        e0 = sim.energy()
+        sim.integrate(1e3)
+        sim.steps(1)
+        out["oss_err_o%d" % order] = abs((e0 - sim.energy()) / sim.energy())
+    np.savez_compressed(os.path.join(HERE, "leapfrog_orders.npz"), **out)
+
+
 if __name__ == "__main__":
-    which = sys.argv[2:] or ["gravity_cases", "ring", "whfast", "sei", "gravity_plummer", "reference_cases"]
+    which = sys.argv[2:] or ["gravity_cases", "ring", "whfast", "sei", "gravity_plummer", "reference_cases",
+                             "leapfrog_orders"]
     for w in which:
         print("generating", w, flush=True)
         globals()["fixture_" + w]() if w != "sei" else fixture_sei_periodic()

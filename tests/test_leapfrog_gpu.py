@@ -1,4 +1,4 @@
-"""Leapfrog (order 2) on the GPU: configuration 1 (Plummer N=4,096, softening
+"""Leapfrog on the GPU: orders 2, 4, 6, 8 (src/integrator_leapfrog.c:97-203), and configuration 1 (Plummer N=4,096, softening
 0.01, dt=1e-3, 1,000 steps, BASIC, FP64) against the reference.
 
 Bar: the relative energy error after 1,000 steps is within 2x of the
@@ -63,3 +63,42 @@ def test_integrate_exact_finish_time(gpu):
     sim = make(gpu, g["particles"][:256])
     sim.integrate(0.0105)
     assert sim.t == 0.0105
+
+
+@pytest.mark.parametrize("order", [4, 6, 8])
+def test_higher_orders_track_reference(gpu, order):
+    # 20 steps of the reference's composition schemes on a softened 128-body sphere
+    g = golden("leapfrog_orders.npz")
+    sim = make(gpu, g["particles"])
+    sim.leapfrog_order = order
+    sim.steps(20)
+    p, ref = sim.particles, g["after20_o%d" % order]
+    for f in ("x", "y", "z", "vx", "vy", "vz"):
+        scale = np.abs(ref[f]).max()
+        assert np.abs(p[f] - ref[f]).max() <= 1e-12 * scale, (order, f)
+    assert sim.t == float(g["t_o%d" % order])      # the same sequence of drift lengths
+
+
+@pytest.mark.parametrize("order,bar", [(4, 3e-6), (6, 1e-9), (8, 1e-9)])
+def test_higher_orders_outer_solar_system(gpu, order, bar):
+    # rebound/tests/test_leapfrog.py:24-56: integrate to t = 1e3 with dt = 1, one more step
+    g = golden("reference_cases.npz")
+    ref_err = float(golden("leapfrog_orders.npz")["oss_err_o%d" % order])
+    sim = gpu.Simulation()
+    sim.integrator = "leapfrog"
+    sim.leapfrog_order = order
+    sim.dt = 1.0
+    sim.add(g["oss"])
+    e0 = sim.energy()
+    sim.integrate(1e3)
+    sim.steps(1)
+    err = abs((e0 - sim.energy()) / sim.energy())
+    assert err < bar
+    assert err <= max(2 * ref_err, 1e-13), (err, ref_err)
+
+
+def test_unsupported_order_is_an_error(gpu):
+    sim = make(gpu, golden("leapfrog_orders.npz")["particles"])
+    sim.leapfrog_order = 3
+    with pytest.raises(gpu.RGPUError):
+        sim.steps(1)

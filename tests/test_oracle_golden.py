@@ -33,6 +33,16 @@ def test_oracle_leapfrog_trajectory():
     assert max_diff(s.p, g["after10"]) == 0.0
 
 
+@pytest.mark.parametrize("order", [4, 6, 8])
+def test_oracle_leapfrog_orders(order):
+    # src/integrator_leapfrog.c:97-203, bit for bit with the reference's own run
+    g = golden("leapfrog_orders.npz")
+    s = O.Sim(g["particles"], softening=0.01, dt=1e-3)
+    s.leapfrog(20, order=order)
+    assert max_diff(s.p, g["after20_o%d" % order]) == 0.0
+    assert s.s.t == float(g["t_o%d" % order])
+
+
 @pytest.mark.parametrize("case", ["plain", "testp0", "testp1", "ignore01", "ignore0", "ghost", "single", "two"])
 def test_oracle_gravity_cases(case):
     g = golden("gravity_cases.npz")
