@@ -83,7 +83,7 @@ typedef struct rgpu_config {
     int32_t status;            /* REB_STATUS_* value after a step (7 = collision halt) */
     int64_t collisions_log_n;  /* number of resolved hardsphere collisions */
     int32_t leapfrog_order;    /* 2 (default; 0 means 2), 4, 6 or 8: src/integrator_leapfrog.c:97-203 */
-    int32_t reserved;
+    int32_t whfast_coordinates; /* 0 Jacobi (default), 1 democratic heliocentric (src/integrator_whfast.h) */
 } rgpu_config;
 
 /* One overlapping, approaching pair: same layout as struct reb_collision

@@ -45,7 +45,7 @@ class Config(ctypes.Structure):
         ("gravity", ctypes.c_int32), ("collision", ctypes.c_int32), ("collision_resolve", ctypes.c_int32),
         ("boundary", ctypes.c_int32), ("integrator", ctypes.c_int32), ("whfast_safe_mode", ctypes.c_int32),
         ("rand_seed", ctypes.c_uint32), ("status", ctypes.c_int32), ("collisions_log_n", ctypes.c_int64),
-        ("leapfrog_order", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+        ("leapfrog_order", ctypes.c_int32), ("whfast_coordinates", ctypes.c_int32)]
 
 
 class ServerConfig(ctypes.Structure):

@@ -4,59 +4,11 @@
 // system's state lives in the handle's SoA arrays (inertial) plus a Jacobi
 // buffer for safe_mode = 0.  Compiled with --fmad=false: bit-identical to the
 // reference's serial build.
-#include "whfast_core.cuh"
-
-struct WhfastBuffers {
-    double* jac = nullptr;   // 7 * cap: x, y, z, vx, vy, vz, m (Jacobi, p_jh)
-    size_t cap = 0;
-};
+#include "whfast_plain.cuh"
 
 namespace {
 
-enum : int { kFromInertial = 1, kFirstHalf = 2, kSyncAtEnd = 4, kSyncOnly = 8 };
-
-template <int NB>
-__device__ void load_sys(wh::System<NB>& s, const ParticlesSoA& p, int N) {
-#pragma unroll
-    for (int i = 0; i < NB; i++) {
-        const bool on = i < N;
-        s.x[i] = on ? p.x[i] : 0.; s.y[i] = on ? p.y[i] : 0.; s.z[i] = on ? p.z[i] : 0.;
-        s.vx[i] = on ? p.vx[i] : 0.; s.vy[i] = on ? p.vy[i] : 0.; s.vz[i] = on ? p.vz[i] : 0.;
-        s.m[i] = on ? p.m[i] : 0.;
-    }
-}
-
-template <int NB>
-__device__ void store_pos_vel(const wh::System<NB>& s, ParticlesSoA& p, int N) {
-#pragma unroll
-    for (int i = 0; i < NB; i++) {
-        if (i >= N) break;
-        p.x[i] = s.x[i]; p.y[i] = s.y[i]; p.z[i] = s.z[i];
-        p.vx[i] = s.vx[i]; p.vy[i] = s.vy[i]; p.vz[i] = s.vz[i];
-    }
-}
-
-template <int NB>
-__device__ void load_jac(wh::Jacobi<NB>& j, const double* jac, size_t cap, int N) {
-#pragma unroll
-    for (int i = 0; i < NB; i++) {
-        const bool on = i < N;
-        j.x[i] = on ? jac[0 * cap + i] : 0.; j.y[i] = on ? jac[1 * cap + i] : 0.; j.z[i] = on ? jac[2 * cap + i] : 0.;
-        j.vx[i] = on ? jac[3 * cap + i] : 0.; j.vy[i] = on ? jac[4 * cap + i] : 0.; j.vz[i] = on ? jac[5 * cap + i] : 0.;
-        j.m[i] = on ? jac[6 * cap + i] : 0.;
-    }
-}
-
-template <int NB>
-__device__ void store_jac(const wh::Jacobi<NB>& j, double* jac, size_t cap, int N) {
-#pragma unroll
-    for (int i = 0; i < NB; i++) {
-        if (i >= N) break;
-        jac[0 * cap + i] = j.x[i]; jac[1 * cap + i] = j.y[i]; jac[2 * cap + i] = j.z[i];
-        jac[3 * cap + i] = j.vx[i]; jac[4 * cap + i] = j.vy[i]; jac[5 * cap + i] = j.vz[i];
-        jac[6 * cap + i] = j.m[i];
-    }
-}
+using namespace wh_plain;
 
 // One step (or a synchronize) of src/integrator_whfast.c for the handle's system.
 template <int NB>
@@ -66,36 +18,32 @@ __global__ void __launch_bounds__(32) whfast_plain(ParticlesSoA p, double* jac, 
     wh::System<NB> s;
     wh::Jacobi<NB> j;
     load_sys(s, p, N);
-    if (flags & kSyncOnly) {
-        // reb_integrator_whfast_synchronize (:1051-1111): Kepler(dt/2), COM, to inertial.
-        load_jac(j, jac, cap, N);
-        wh::kepler_step(j, s.m[0], G, dt / 2., N, Na, status);
-        wh::com_step(j, dt / 2.);
-        wh::to_inertial(s, j, N, Na);
-        store_pos_vel(s, p, N);
-        return;
-    }
-    if (flags & kFromInertial) wh::to_jacobi(s, j, N, Na);
+    const bool sync_only = (flags & kSyncOnly) != 0;
+    if (!sync_only && (flags & kFromInertial)) wh::to_jacobi(s, j, N, Na);
     else load_jac(j, jac, cap, N);
-    const double d1 = (flags & kFirstHalf) ? dt / 2. : dt;      // combined drift when unsynchronized
-    wh::kepler_step(j, s.m[0], G, d1, N, Na, status);
-    wh::com_step(j, d1);
-    wh::to_inertial(s, j, N, Na);
-    double ax[NB], ay[NB], az[NB];
-    wh::gravity_01(s, ax, ay, az, G, eps2, N, Na, tp);
-    wh::interaction_step(j, s, ax, ay, az, G, dt, N, Na);
-#pragma unroll
-    for (int i = 0; i < NB; i++) {
-        if (i >= N) break;
-        p.ax[i] = ax[i]; p.ay[i] = ay[i]; p.az[i] = az[i];
-    }
-    if (flags & kSyncAtEnd) {
-        wh::kepler_step(j, s.m[0], G, dt / 2., N, Na, status);
-        wh::com_step(j, dt / 2.);
+    // One drift call site (rolled passes) keeps one inlined copy of the Kepler solver:
+    // pass 0 = the opening drift (dt/2 when synchronized, dt when not) and the kick, or
+    // the synchronize drift; pass 1 = the closing drift of safe_mode.
+#pragma unroll 1
+    for (int pass = 0; pass < 2; pass++) {
+        if (pass == 1 && (sync_only || !(flags & kSyncAtEnd))) break;
+        const double d = (pass == 0 && !sync_only && !(flags & kFirstHalf)) ? dt : dt / 2.;
+        wh::kepler_step(j, s.m[0], G, d, N, Na, status);
+        wh::com_step(j, d);
         wh::to_inertial(s, j, N, Na);
+        if (pass == 0 && !sync_only) {
+            double ax[NB], ay[NB], az[NB];
+            wh::gravity_01(s, ax, ay, az, G, eps2, N, Na, tp);
+            wh::interaction_step(j, s, ax, ay, az, G, dt, N, Na);
+#pragma unroll
+            for (int i = 0; i < NB; i++) {
+                if (i >= N) break;
+                p.ax[i] = ax[i]; p.ay[i] = ay[i]; p.az[i] = az[i];
+            }
+        }
     }
     store_pos_vel(s, p, N);
-    store_jac(j, jac, cap, N);
+    if (!sync_only) store_jac(j, jac, cap, N);
 }
 
 typedef void (*PlainKernel)(ParticlesSoA, double*, size_t, int, int, int, double, double, double, int, uint32_t*);
@@ -134,9 +82,10 @@ int ensure_jac(rgpu_sim* s) {
 
 int launch(rgpu_sim* s, int flags) {
     const int N = (int)s->N;
+    RGPU_TRY(ensure_jac(s));
+    if (s->cfg.whfast_coordinates == 1) return launch_dh(s, flags);
     PlainKernel k = kernel_for(N);
     if (!k) return set_error(s, RGPU_ERR_UNSUPPORTED, "WHFast on the GPU supports 2..16 particles per simulation");
-    RGPU_TRY(ensure_jac(s));
     const rgpu_config& c = s->cfg;
     ktimer_begin(s);
     k<<<1, 32, 0, s->stream>>>(s->p, s->wh->jac, s->cap, N, (int)n_active(s), c.testparticle_type, c.G,
@@ -152,7 +101,9 @@ int launch(rgpu_sim* s, int flags) {
 int whfast_step(rgpu_sim* s) {
     if (s->N == 0) return RGPU_OK;
     rgpu_config& c = s->cfg;
-    c.gravity_ignore_terms = 1;                                  // :932-933
+    if (c.whfast_coordinates != 0 && c.whfast_coordinates != 1)
+        return set_error(s, RGPU_ERR_UNSUPPORTED, "WHFast coordinates: 0 (Jacobi) or 1 (democratic heliocentric)");
+    c.gravity_ignore_terms = c.whfast_coordinates == 1 ? 2 : 1;  // :929-938
     int flags = 0;
     if (c.whfast_safe_mode || s->did_modify) {
         if (!s->whfast_synchronized) RGPU_TRY(whfast_synchronize(s));
@@ -162,7 +113,8 @@ int whfast_step(rgpu_sim* s) {
     if (c.whfast_safe_mode) flags |= kSyncAtEnd;
     RGPU_TRY(launch(s, flags));
     s->whfast_synchronized = c.whfast_safe_mode != 0;
-    c.t += c.dt;
+    c.t += c.dt / 2.;                                            // two half steps, as :1186 and :1244
+    c.t += c.dt / 2.;
     return RGPU_OK;
 }
 

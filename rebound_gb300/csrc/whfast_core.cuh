@@ -252,7 +252,9 @@ __device__ __forceinline__ void com_step(Jacobi<NB>& j, double dt) {
 
 // BASIC gravity with gravity_ignore_terms = 1 (skip the 0-1 pair), serial
 // pairwise order (src/gravity.c:195-257, starti = 2, startj = 0).
-template <int NB>
+// STARTJ = 1: gravity_ignore_terms = 2, every term involving particle 0 skipped
+// (democratic heliocentric coordinates; src/gravity.c:180-181, startj = 1).
+template <int NB, int STARTJ = 0>
 __device__ __forceinline__ void gravity_01(const System<NB>& s, double ax[NB], double ay[NB], double az[NB],
                                            double G, double eps2, int N, int Na, int tp) {
 #pragma unroll
@@ -261,7 +263,7 @@ __device__ __forceinline__ void gravity_01(const System<NB>& s, double ax[NB], d
     for (int i = 2; i < NB; i++) {
         if (i >= Na) break;
 #pragma unroll
-        for (int jj = 0; jj < i; jj++) {
+        for (int jj = STARTJ; jj < i; jj++) {
             const double dx = (0. + s.x[i]) - s.x[jj];
             const double dy = (0. + s.y[i]) - s.y[jj];
             const double dz = (0. + s.z[i]) - s.z[jj];
@@ -278,7 +280,7 @@ __device__ __forceinline__ void gravity_01(const System<NB>& s, double ax[NB], d
     for (int i = 2; i < NB; i++) {
         if (i < st || i >= N) continue;
 #pragma unroll
-        for (int jj = 0; jj < NB; jj++) {
+        for (int jj = STARTJ; jj < NB; jj++) {
             if (jj >= Na) break;
             const double dx = (0. + s.x[i]) - s.x[jj];
             const double dy = (0. + s.y[i]) - s.y[jj];
@@ -339,6 +341,108 @@ __device__ __forceinline__ void interaction_step(Jacobi<NB>& j, const System<NB>
             j.vy[i] += pf * qy;
             j.vz[i] += pf * qz;
         }
+    }
+}
+
+// --- democratic heliocentric coordinates (Duncan, Levison & Lee 1998) -----------
+// h[0]: centre of mass (position and velocity) and total mass; h[i], i >= 1:
+// heliocentric position, barycentric velocity.
+
+// reb_transformations_inertial_to_democraticheliocentric_posvel (src/transformations.c:388-425).
+template <int NB>
+__device__ __forceinline__ void to_dh(const System<NB>& s, Jacobi<NB>& h, int N, int Na) {
+    double x0 = 0., y0 = 0., z0 = 0., vx0 = 0., vy0 = 0., vz0 = 0., m0 = 0.;
+#pragma unroll
+    for (int i = 0; i < NB; i++) {
+        if (i >= Na) break;
+        const double m = s.m[i];
+        x0 += s.x[i] * m; y0 += s.y[i] * m; z0 += s.z[i] * m;
+        vx0 += s.vx[i] * m; vy0 += s.vy[i] * m; vz0 += s.vz[i] * m;
+        m0 += m;
+    }
+    h.x[0] = x0 / m0; h.y[0] = y0 / m0; h.z[0] = z0 / m0;
+    h.vx[0] = vx0 / m0; h.vy[0] = vy0 / m0; h.vz[0] = vz0 / m0;
+    h.m[0] = m0;
+#pragma unroll
+    for (int i = 1; i < NB; i++) {
+        if (i >= N) break;
+        h.x[i] = s.x[i] - s.x[0]; h.y[i] = s.y[i] - s.y[0]; h.z[i] = s.z[i] - s.z[0];
+        h.vx[i] = s.vx[i] - h.vx[0]; h.vy[i] = s.vy[i] - h.vy[0]; h.vz[i] = s.vz[i] - h.vz[0];
+        h.m[i] = s.m[i];
+    }
+}
+
+// reb_transformations_democraticheliocentric_to_inertial_posvel (src/transformations.c:427-473).
+template <int NB>
+__device__ __forceinline__ void dh_to_inertial(System<NB>& s, const Jacobi<NB>& h, int N, int Na) {
+    const double mtot = h.m[0];
+    double x0 = 0., y0 = 0., z0 = 0.;
+#pragma unroll
+    for (int i = 1; i < NB; i++) {
+        if (i >= Na) break;
+        const double m = h.m[i];
+        x0 += h.x[i] * m / mtot; y0 += h.y[i] * m / mtot; z0 += h.z[i] * m / mtot;
+        s.m[i] = m;
+    }
+    s.x[0] = h.x[0] - x0; s.y[0] = h.y[0] - y0; s.z[0] = h.z[0] - z0;
+#pragma unroll
+    for (int i = 1; i < NB; i++) {
+        if (i >= N) break;
+        s.x[i] = h.x[i] + s.x[0]; s.y[i] = h.y[i] + s.y[0]; s.z[i] = h.z[i] + s.z[0];
+    }
+    const double m0 = s.m[0];
+#pragma unroll
+    for (int i = 1; i < NB; i++) {
+        if (i >= N) break;
+        s.vx[i] = h.vx[i] + h.vx[0]; s.vy[i] = h.vy[i] + h.vy[0]; s.vz[i] = h.vz[i] + h.vz[0];
+    }
+    double vx0 = 0., vy0 = 0., vz0 = 0.;
+#pragma unroll
+    for (int i = 1; i < NB; i++) {
+        if (i >= Na) break;
+        const double m = s.m[i];
+        vx0 += h.vx[i] * m / m0; vy0 += h.vy[i] * m / m0; vz0 += h.vz[i] * m / m0;
+    }
+    s.vx[0] = h.vx[0] - vx0; s.vy[0] = h.vy[0] - vy0; s.vz[0] = h.vz[0] - vz0;
+}
+
+// Kepler drift about the star alone, mu = G m_0 (src/integrator_whfast.c:611-616).
+template <int NB>
+__device__ __forceinline__ void kepler_step_dh(Jacobi<NB>& h, double m0, double G, double dt, int N,
+                                               uint32_t* status) {
+#pragma unroll 1
+    for (int i = 1; i < NB; i++) {
+        if (i >= N) break;
+        kepler_solver(h.x[i], h.y[i], h.z[i], h.vx[i], h.vy[i], h.vz[i], m0 * G, dt, status);
+    }
+}
+
+// Jump step: drift by the star's momentum share (src/integrator_whfast.c:536-553).
+template <int NB>
+__device__ __forceinline__ void jump_step_dh(Jacobi<NB>& h, const System<NB>& s, double dt, int N, int Na) {
+    const double m0 = s.m[0];
+    double px = 0., py = 0., pz = 0.;
+#pragma unroll
+    for (int i = 1; i < NB; i++) {
+        if (i >= Na) break;
+        const double m = s.m[i];
+        px += m * h.vx[i]; py += m * h.vy[i]; pz += m * h.vz[i];
+    }
+#pragma unroll
+    for (int i = 1; i < NB; i++) {
+        if (i >= N) break;
+        h.x[i] += dt * (px / m0); h.y[i] += dt * (py / m0); h.z[i] += dt * (pz / m0);
+    }
+}
+
+// Interaction kick with the planets' mutual accelerations (src/integrator_whfast.c:494-500).
+template <int NB>
+__device__ __forceinline__ void interaction_step_dh(Jacobi<NB>& h, const double ax[NB], const double ay[NB],
+                                                    const double az[NB], double dt, int N) {
+#pragma unroll
+    for (int i = 1; i < NB; i++) {
+        if (i >= N) break;
+        h.vx[i] += dt * ax[i]; h.vy[i] += dt * ay[i]; h.vz[i] += dt * az[i];
     }
 }
 

@@ -1,0 +1,62 @@
+// Pieces shared by the plain (one simulation per call) WHFast kernels in
+// Jacobi (whfast.cu) and democratic heliocentric (whfast_dh.cu) coordinates:
+// the handle's coordinate buffer, the step flags and the load / store helpers.
+#pragma once
+#include "whfast_core.cuh"
+
+struct WhfastBuffers {
+    double* jac = nullptr;   // 7 * cap: x, y, z, vx, vy, vz, m (Jacobi, p_jh)
+    size_t cap = 0;
+};
+
+namespace wh_plain {
+
+enum : int { kFromInertial = 1, kFirstHalf = 2, kSyncAtEnd = 4, kSyncOnly = 8 };
+
+template <int NB>
+__device__ void load_sys(wh::System<NB>& s, const ParticlesSoA& p, int N) {
+#pragma unroll
+    for (int i = 0; i < NB; i++) {
+        const bool on = i < N;
+        s.x[i] = on ? p.x[i] : 0.; s.y[i] = on ? p.y[i] : 0.; s.z[i] = on ? p.z[i] : 0.;
+        s.vx[i] = on ? p.vx[i] : 0.; s.vy[i] = on ? p.vy[i] : 0.; s.vz[i] = on ? p.vz[i] : 0.;
+        s.m[i] = on ? p.m[i] : 0.;
+    }
+}
+
+template <int NB>
+__device__ void store_pos_vel(const wh::System<NB>& s, ParticlesSoA& p, int N) {
+#pragma unroll
+    for (int i = 0; i < NB; i++) {
+        if (i >= N) break;
+        p.x[i] = s.x[i]; p.y[i] = s.y[i]; p.z[i] = s.z[i];
+        p.vx[i] = s.vx[i]; p.vy[i] = s.vy[i]; p.vz[i] = s.vz[i];
+    }
+}
+
+template <int NB>
+__device__ void load_jac(wh::Jacobi<NB>& j, const double* jac, size_t cap, int N) {
+#pragma unroll
+    for (int i = 0; i < NB; i++) {
+        const bool on = i < N;
+        j.x[i] = on ? jac[0 * cap + i] : 0.; j.y[i] = on ? jac[1 * cap + i] : 0.; j.z[i] = on ? jac[2 * cap + i] : 0.;
+        j.vx[i] = on ? jac[3 * cap + i] : 0.; j.vy[i] = on ? jac[4 * cap + i] : 0.; j.vz[i] = on ? jac[5 * cap + i] : 0.;
+        j.m[i] = on ? jac[6 * cap + i] : 0.;
+    }
+}
+
+template <int NB>
+__device__ void store_jac(const wh::Jacobi<NB>& j, double* jac, size_t cap, int N) {
+#pragma unroll
+    for (int i = 0; i < NB; i++) {
+        if (i >= N) break;
+        jac[0 * cap + i] = j.x[i]; jac[1 * cap + i] = j.y[i]; jac[2 * cap + i] = j.z[i];
+        jac[3 * cap + i] = j.vx[i]; jac[4 * cap + i] = j.vy[i]; jac[5 * cap + i] = j.vz[i];
+        jac[6 * cap + i] = j.m[i];
+    }
+}
+
+// Democratic heliocentric step / synchronize on the handle (whfast_dh.cu).
+int launch_dh(rgpu_sim* s, int flags);
+
+}  // namespace wh_plain

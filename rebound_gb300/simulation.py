@@ -24,7 +24,9 @@ _CFG_INTS = ("testparticle_type", "N_root_x", "N_root_y", "N_root_z", "N_ghost_x
 
 
 class WHFastSettings:
-    """Subset of rebound's ri_whfast used on the GPU path (safe_mode)."""
+    """Subset of rebound's ri_whfast used on the GPU path (safe_mode, coordinates)."""
+
+    COORDINATES = {"jacobi": 0, "democraticheliocentric": 1}
 
     def __init__(self, sim):
         self._sim = sim
@@ -36,6 +38,15 @@ class WHFastSettings:
     @safe_mode.setter
     def safe_mode(self, v):
         self._sim._cfg.whfast_safe_mode = int(v)
+
+    @property
+    def coordinates(self):
+        c = self._sim._cfg.whfast_coordinates
+        return next(k for k, v in self.COORDINATES.items() if v == c)
+
+    @coordinates.setter
+    def coordinates(self, name):
+        self._sim._cfg.whfast_coordinates = self.COORDINATES[name]
 
 
 class Simulation:

@@ -429,9 +429,73 @@ def fixture_leapfrog_orders():
     np.savez_compressed(os.path.join(HERE, "leapfrog_orders.npz"), **out)
 
 
+def fixture_whfast_dh():
+    """WHFast in democratic heliocentric coordinates (src/integrator_whfast.c with
+    coordinates = DEMOCRATICHELIOCENTRIC): the scenarios of
+    rebound/tests/test_whfast.py:212-305 with the reference's own errors, and a
+    100-step trajectory of the two-planet system (safe_mode 1 and 0)."""
+    import math
+    out = {}
+
+    def rel(a, b):
+        return abs((a - b) / b)
+
+    def dh(sim, dt, safe=1):
+        sim.integrator = "whfast"
+        sim.integrator.coordinates = "democraticheliocentric"
+        sim.integrator.safe_mode = safe
+        sim.dt = dt
+
+    sim = rebound.Simulation()
+    sim.add("outer solar system")
+    out["oss"] = state(sim)
+    dh(sim, 0.005 * 12. * 2. * 3.1415)
+    e0 = sim.energy()
+    sim.integrate(1000. * 2. * 3.1415)
+    out["oss_err"] = rel(e0, sim.energy())                   # bar 1.5e-8
+    sim = rebound.Simulation()
+    sim.add(m=1.)
+    sim.add(m=1e-3, a=-1., e=2.5)
+    out["hyper"] = state(sim)
+    yr = -sim.particles[1].P
+    out["hyper_yr"] = yr
+    dh(sim, 0.00512 * yr)
+    e0 = sim.energy()
+    sim.integrate(1e2 * yr)
+    out["hyper_err"] = rel(e0, sim.energy())                 # bar 4.5e-8
+    jupyr = 2. * math.pi
+    for safe in (1, 0):
+        sim = rebound.Simulation()
+        sim.add(m=1.)
+        sim.add(m=1e-3, a=1., e=.1)
+        sim.add(m=1e-3, a=3., e=0.1)
+        out["two"] = state(sim)
+        dh(sim, 0.005123 * jupyr, safe)
+        e0 = sim.energy()
+        sim.integrate(1e3 * jupyr)
+        out["two_err_safe%d" % safe] = rel(e0, sim.energy())  # bar 2.9e-8
+        sim = rebound.Simulation()
+        load(sim, out["two"])
+        dh(sim, 0.005123 * jupyr, safe)
+        sim.steps(100)
+        if not safe:
+            sim.integrator.synchronize() if hasattr(sim.integrator, "synchronize") else sim.synchronize()
+        out["two_after100_safe%d" % safe] = state(sim)
+    for tag, order in (("order12", (1., 3.)), ("order21", (3., 1.))):
+        sim = rebound.Simulation()
+        sim.add(m=1.)
+        for a in order:
+            sim.add(m=1e-3, a=a, e=0.1, primary=sim.particles[0])
+        out[tag] = state(sim)
+        dh(sim, 0.005123 * jupyr)
+        sim.integrate(1e0 * jupyr)
+        out[tag + "_end"] = state(sim)
+    np.savez_compressed(os.path.join(HERE, "whfast_dh.npz"), **out)
+
+
 if __name__ == "__main__":
     which = sys.argv[2:] or ["gravity_cases", "ring", "whfast", "sei", "gravity_plummer", "reference_cases",
-                             "leapfrog_orders"]
+                             "leapfrog_orders", "whfast_dh"]
     for w in which:
         print("generating", w, flush=True)
         globals()["fixture_" + w]() if w != "sei" else fixture_sei_periodic()
