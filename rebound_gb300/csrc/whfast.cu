@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(32) whfast_plain(ParticlesSoA p, double* jac, 
         }
     }
     store_pos_vel(s, p, N);
-    if (!sync_only) store_jac(j, jac, cap, N);
+    store_jac(j, jac, cap, N);               // synchronize keeps the drifted coordinates, as the reference
 }
 
 typedef void (*PlainKernel)(ParticlesSoA, double*, size_t, int, int, int, double, double, double, int, uint32_t*);

@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(32) whfast_plain_dh(ParticlesSoA p, double* bu
         }
     }
     store_pos_vel(s, p, N);
-    if (!sync_only) store_jac(h, buf, cap, N);
+    store_jac(h, buf, cap, N);               // synchronize keeps the drifted coordinates, as the reference
 }
 
 typedef void (*PlainKernel)(ParticlesSoA, double*, size_t, int, int, int, double, double, double, int, uint32_t*);

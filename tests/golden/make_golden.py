@@ -481,6 +481,17 @@ def fixture_whfast_dh():
         if not safe:
             sim.integrator.synchronize() if hasattr(sim.integrator, "synchronize") else sim.synchronize()
         out["two_after100_safe%d" % safe] = state(sim)
+    # safe_mode 0: steps, synchronize, more steps from the synchronized coordinates
+    for coords in ("jacobi", "democraticheliocentric"):
+        sim = rebound.Simulation()
+        load(sim, out["two"])
+        dh(sim, 0.005123 * jupyr, 0)
+        sim.integrator.coordinates = coords
+        sim.steps(50)
+        sim.synchronize()
+        sim.steps(50)
+        sim.synchronize()
+        out["two_sync_mid_" + coords] = state(sim)
     for tag, order in (("order12", (1., 3.)), ("order21", (3., 1.))):
         sim = rebound.Simulation()
         sim.add(m=1.)

@@ -98,3 +98,19 @@ def test_order_of_planets_does_not_matter(gpu):
     a, b = ends["order12"], ends["order21"]
     for f in ("x", "y"):
         assert abs(a[f][1] - b[f][2]) <= 1e-14 and abs(a[f][2] - b[f][1]) <= 1e-14
+
+
+@pytest.mark.parametrize("coords", ["jacobi", "democraticheliocentric"])
+def test_safe_mode_off_synchronize_mid_run(gpu, coords):
+    # safe_mode 0: 50 steps, synchronize, 50 more steps from the synchronized
+    # coordinates, synchronize: the reference's own trajectory bit for bit
+    g = golden("whfast_dh.npz")
+    sim = dh_sim(gpu, g["two"], 0.005123 * 2. * math.pi, 0)
+    sim.ri_whfast.coordinates = coords
+    sim.steps(50)
+    sim.synchronize()
+    sim.steps(50)
+    sim.synchronize()
+    out, ref = sim.particles, g["two_sync_mid_" + coords]
+    for f in XV:
+        assert np.array_equal(out[f], ref[f]), f
