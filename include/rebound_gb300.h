@@ -84,6 +84,13 @@ typedef struct rgpu_config {
     int64_t collisions_log_n;  /* number of resolved hardsphere collisions */
     int32_t leapfrog_order;    /* 2 (default; 0 means 2), 4, 6 or 8: src/integrator_leapfrog.c:97-203 */
     int32_t whfast_coordinates; /* 0 Jacobi (default), 1 democratic heliocentric (src/integrator_whfast.h) */
+    /* src/integrator_whfast.h:29-47 (Jacobi coordinates only where not 0): */
+    int32_t whfast_corrector;   /* first symplectic corrector order: 0 (off), 3, 5, 7, 11 or 17 */
+    int32_t whfast_corrector2;  /* 1: second symplectic corrector */
+    int32_t whfast_kernel;      /* 0 DEFAULT, 1 MODIFIEDKICK, 2 COMPOSITION, 3 LAZY */
+    int32_t whfast_keep_unsynchronized;  /* 1: synchronize leaves the integrator state unsynchronized */
+    int32_t exact_finish_time;  /* src/rebound.h: 1 (default) lands integrate exactly on tmax */
+    int32_t reserved0;
 } rgpu_config;
 
 /* One overlapping, approaching pair: same layout as struct reb_collision

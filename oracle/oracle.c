@@ -959,13 +959,16 @@ static void whfast_com_step(orc_sim* r, double dt) {              /* :638-651 */
 static void whfast_interaction_step(orc_sim* r, double dt) {      /* :431-492 */
     const size_t N = r->N, Na = n_active_of(r);
     orc_particle* pj = r->p_jh;
+    /* kernels MODIFIEDKICK and LAZY run with gravity = JACOBI: the Jacobi term is
+     * already in the accelerations (:458) */
+    const int jacobi_term = r->whfast_kernel != 1 && r->whfast_kernel != 3;
     inertial_to_jacobi_acc(r->particles, pj, r->particles, N, Na);
     double eta = r->particles[0].m;
     for (size_t i = 1; i < N; i++) {
         const orc_particle q = pj[i];
         if (i < Na) eta += q.m;
         pj[i].vx += dt * q.ax; pj[i].vy += dt * q.ay; pj[i].vz += dt * q.az;
-        if (i > 1) {
+        if (jacobi_term && i > 1) {
             const double rj2i = 1. / (q.x * q.x + q.y * q.y + q.z * q.z);
             const double rji = sqrt(rj2i);
             const double rj3iM = rji * rj2i * r->G * eta;
@@ -975,12 +978,181 @@ static void whfast_interaction_step(orc_sim* r, double dt) {      /* :431-492 */
     }
 }
 
+/* reb_gravity_jacobi_calculate_acceleration (src/gravity.c:108-162). */
+static void gravity_jacobi(orc_sim* r) {
+    orc_particle* const P = r->particles;
+    const size_t N = r->N;
+    const double G = r->G;
+    double Rx = 0., Ry = 0., Rz = 0., M = 0.;
+    for (size_t j = 0; j < N; j++) {
+        P[j].ax = 0.; P[j].ay = 0.; P[j].az = 0.;
+        for (size_t i = 0; i < j + 1; i++) {
+            if (j > 1) {
+                const double Qx = P[j].x - Rx / M, Qy = P[j].y - Ry / M, Qz = P[j].z - Rz / M;
+                const double dr = sqrt(Qx * Qx + Qy * Qy + Qz * Qz);
+                const double dQ = i < j ? -P[j].m : M;
+                const double pf = G * dQ / (dr * dr * dr);
+                P[i].ax += pf * Qx; P[i].ay += pf * Qy; P[i].az += pf * Qz;
+            }
+            if (i != j && (i != 0 || j != 1)) {
+                const double dx = P[i].x - P[j].x, dy = P[i].y - P[j].y, dz = P[i].z - P[j].z;
+                const double dr = sqrt(dx * dx + dy * dy + dz * dz);
+                const double pf = G / (dr * dr * dr);
+                const double pfi = pf * P[i].m, pfj = pf * P[j].m;
+                P[i].ax -= pfj * dx; P[i].ay -= pfj * dy; P[i].az -= pfj * dz;
+                P[j].ax += pfi * dx; P[j].ay += pfi * dy; P[j].az += pfi * dz;
+            }
+        }
+        Rx += P[j].m * P[j].x; Ry += P[j].m * P[j].y; Rz += P[j].m * P[j].z;
+        M += P[j].m;
+    }
+}
+
+/* reb_simulation_update_acceleration for WHFast: BASIC with the 0-1 pair
+ * skipped, or JACOBI for kernels MODIFIEDKICK and LAZY (:929-931). */
+static void whfast_update_acceleration(orc_sim* r) {
+    if (r->whfast_kernel == 1 || r->whfast_kernel == 3) gravity_jacobi(r);
+    else orc_gravity_basic_serial(r);
+}
+
+/* reb_integrator_whfast_calculate_jerk (:786-870) into jx, jy, jz. */
+static void whfast_jerk(const orc_sim* r, double* jx, double* jy, double* jz) {
+    const orc_particle* const P = r->particles;
+    const size_t N = r->N;
+    const double G = r->G;
+    double Rx = 0., Ry = 0., Rz = 0., M = 0., Ax = 0., Ay = 0., Az = 0.;
+    for (size_t j = 0; j < N; j++) {
+        jx[j] = 0.; jy[j] = 0.; jz[j] = 0.;
+        for (size_t i = 0; i < j + 1; i++) {
+            if (j > 1) {
+                const double dQ = i < j ? -P[j].m : M;
+                const double Qx = P[j].x - Rx / M, Qy = P[j].y - Ry / M, Qz = P[j].z - Rz / M;
+                const double dax = P[j].ax - Ax / M, day = P[j].ay - Ay / M, daz = P[j].az - Az / M;
+                const double dr = sqrt(Qx * Qx + Qy * Qy + Qz * Qz);
+                const double pf2 = G * dQ / (dr * dr * dr);
+                jx[i] += pf2 * dax; jy[i] += pf2 * day; jz[i] += pf2 * daz;
+                const double alpha = dax * Qx + day * Qy + daz * Qz;
+                const double pf1 = 3. * alpha * pf2 / (dr * dr);
+                jx[i] -= pf1 * Qx; jy[i] -= pf1 * Qy; jz[i] -= pf1 * Qz;
+            }
+            if (j != i && (i != 0 || j != 1)) {
+                const double dx = P[j].x - P[i].x, dy = P[j].y - P[i].y, dz = P[j].z - P[i].z;
+                const double dax = P[j].ax - P[i].ax, day = P[j].ay - P[i].ay, daz = P[j].az - P[i].az;
+                const double dr = sqrt(dx * dx + dy * dy + dz * dz);
+                const double alpha = dax * dx + day * dy + daz * dz;
+                const double pf2 = G / (dr * dr * dr);
+                const double pf2i = pf2 * P[i].m, pf2j = pf2 * P[j].m;
+                jx[j] -= dax * pf2i; jy[j] -= day * pf2i; jz[j] -= daz * pf2i;
+                jx[i] += dax * pf2j; jy[i] += day * pf2j; jz[i] += daz * pf2j;
+                const double pf1 = 3. * alpha * pf2 / (dr * dr);
+                const double pf1i = pf1 * P[i].m, pf1j = pf1 * P[j].m;
+                jx[j] += dx * pf1i; jy[j] += dy * pf1i; jz[j] += dz * pf1i;
+                jx[i] -= dx * pf1j; jy[i] -= dy * pf1j; jz[i] -= dz * pf1j;
+            }
+        }
+        Ax += P[j].ax * P[j].m; Ay += P[j].ay * P[j].m; Az += P[j].az * P[j].m;
+        Rx += P[j].x * P[j].m; Ry += P[j].y * P[j].m; Rz += P[j].z * P[j].m;
+        M += P[j].m;
+    }
+}
+
+/* Corrector coefficients (src/integrator_whfast.c:124-158). */
+static const double corr_a[9] = {0.,
+    0.41833001326703777398908601289259374469640768464934,
+    0.83666002653407554797817202578518748939281536929867,
+    1.2549900398011133219672580386777812340892230539480,
+    1.6733200530681510959563440515703749787856307385973,
+    2.0916500663351888699454300644629687234820384232467,
+    2.5099800796022266439345160773555624681784461078960,
+    2.9283100928692644179236020902481562128748537925454,
+    3.3466401061363021919126881031407499575712614771947};
+static const double corr_b3[1] = {-0.024900596027799867499350357910273437184309981229127};
+static const double corr_b5[2] = {-0.0083001986759332891664501193034244790614366604097090,
+                                  0.041500993379666445832250596517122395307183302048545};
+static const double corr_b7[3] = {0.0024926811426922105779030593952776964450539008582219,
+                                  -0.018270923246702131478062356884535264841652263842597,
+                                  0.053964399093127498721765893493510877532452806339655};
+static const double corr_b11[5] = {0.00020361579647854651301632818774633716473696537436847,
+                                   -0.0023487215292295354188307328851055489876255097419754,
+                                   0.012309078592019946317544564763237909911330686448336,
+                                   -0.038121613681288650508647613260247372125243616270670,
+                                   0.072593394748842738674253180742744961827622366521517};
+static const double corr_b17[8] = {-0.0000043347415473373580190650223498124944896789841432241,
+                                   0.000076436355227935738363241846979413475106795392377415,
+                                   -0.00063599983075817658983166881625078545864140848560259,
+                                   0.0033132577069380655655490196833451994080066801611459,
+                                   -0.012071760822342291062449751726959664253913904872527,
+                                   0.032422198864713580293681523029577130832258806467604,
+                                   -0.065192863576377893658290760803725762027864651086787,
+                                   0.093056103771425958591541059067553547100903397724386};
+static const double corr2_b = 0.03486083443891981449909050107438281205803;
+
+/* Jacobi -> inertial, then the accelerations, then a kick of dt. */
+static void whfast_evaluate_kick(orc_sim* r, double dt) {
+    orc_jacobi_to_inertial_posvel(r->particles, r->p_jh, r->particles, r->N, n_active_of(r));
+    whfast_update_acceleration(r);
+    whfast_interaction_step(r, dt);
+}
+
+static void corrector_z(orc_sim* r, double a, double b) {          /* :653-694 */
+    whfast_kepler_step(r, a);
+    whfast_evaluate_kick(r, -b);
+    whfast_kepler_step(r, -2. * a);
+    whfast_evaluate_kick(r, b);
+    whfast_kepler_step(r, a);
+}
+
+static void apply_corrector(orc_sim* r, double inv, int order) {   /* :696-751 */
+    const double dt = r->dt;
+    if (order == 3) {
+        corrector_z(r, corr_a[1] * dt, -inv * corr_b3[0] * dt);
+        corrector_z(r, -corr_a[1] * dt, inv * corr_b3[0] * dt);
+        return;
+    }
+    const double* b = order == 5 ? corr_b5 : order == 7 ? corr_b7 : order == 11 ? corr_b11 : corr_b17;
+    const int h = order == 5 ? 2 : order == 7 ? 3 : order == 11 ? 5 : 8;
+    for (int k = 0; k < h; k++) corrector_z(r, -corr_a[h - k] * dt, -inv * b[k] * dt);
+    for (int k = h - 1; k >= 0; k--) corrector_z(r, corr_a[h - k] * dt, inv * b[k] * dt);
+}
+
+static void operator_c(orc_sim* r, double a, double b) {           /* :753-768 */
+    whfast_kepler_step(r, a);
+    whfast_evaluate_kick(r, b);
+    whfast_kepler_step(r, -a);
+}
+static void operator_y(orc_sim* r, double a, double b) { operator_c(r, a, b); operator_c(r, -a, -b); }
+static void operator_u(orc_sim* r, double a, double b) {
+    whfast_kepler_step(r, a);
+    operator_y(r, a, b);
+    operator_y(r, a, -b);
+    whfast_kepler_step(r, -a);
+}
+static void apply_corrector2(orc_sim* r, double inv) {             /* :779-785 */
+    const double a = 0.5 * inv * r->dt;
+    const double b = corr2_b * inv * r->dt;
+    operator_u(r, a, b);
+    operator_u(r, -a, b);
+}
+
 void orc_whfast_synchronize(orc_sim* r) {                         /* :1051-1111 */
     if (r->whfast_is_synchronized == 0) {
-        whfast_kepler_step(r, r->dt / 2.);
-        whfast_com_step(r, r->dt / 2.);
+        orc_particle* keep = NULL;
+        if (r->whfast_keep_unsynchronized) {
+            keep = (orc_particle*)malloc(sizeof(orc_particle) * r->N);
+            memcpy(keep, r->p_jh, sizeof(orc_particle) * r->N);
+        }
+        const double d = r->whfast_kernel == 2 ? 3. * r->dt / 8. : r->dt / 2.;
+        whfast_kepler_step(r, d);
+        whfast_com_step(r, d);
+        if (r->whfast_corrector2) apply_corrector2(r, -1.);
+        if (r->whfast_corrector) apply_corrector(r, -1., r->whfast_corrector);
         orc_jacobi_to_inertial_posvel(r->particles, r->p_jh, r->particles, r->N, n_active_of(r));
-        r->whfast_is_synchronized = 1;
+        if (keep) {
+            memcpy(r->p_jh, keep, sizeof(orc_particle) * r->N);
+            free(keep);
+        } else {
+            r->whfast_is_synchronized = 1;
+        }
     }
 }
 
@@ -994,16 +1166,57 @@ void orc_whfast_step(orc_sim* r) {                                /* :1113-1259 
         r->whfast_did_modify = 0;
     }
     if (r->whfast_is_synchronized) {
-        whfast_kepler_step(r, dt / 2.);
-        whfast_com_step(r, dt / 2.);
+        if (r->whfast_corrector) apply_corrector(r, 1., r->whfast_corrector);
+        if (r->whfast_corrector2) apply_corrector2(r, 1.);
+        const double d = r->whfast_kernel == 2 ? 5. * dt / 8. : dt / 2.;
+        whfast_kepler_step(r, d);
+        whfast_com_step(r, d);
     } else {
         whfast_kepler_step(r, dt);
         whfast_com_step(r, dt);
     }
     orc_jacobi_to_inertial_posvel(r->particles, r->p_jh, r->particles, N, Na);
     r->t += dt / 2.;
-    orc_gravity_basic_serial(r);
-    whfast_interaction_step(r, dt);
+    whfast_update_acceleration(r);
+    switch (r->whfast_kernel) {
+        case 1: {                                                  /* MODIFIEDKICK (:1192-1203) */
+            double* j = (double*)malloc(sizeof(double) * 3 * N);
+            whfast_jerk(r, j, j + N, j + 2 * N);
+            const double pf = dt * dt / 12.;
+            for (size_t i = 0; i < N; i++) {
+                r->particles[i].ax += pf * j[i];
+                r->particles[i].ay += pf * j[N + i];
+                r->particles[i].az += pf * j[2 * N + i];
+            }
+            free(j);
+            whfast_interaction_step(r, dt);
+            break;
+        }
+        case 2:                                                    /* COMPOSITION (:1205-1231) */
+            whfast_interaction_step(r, -dt / 6.);
+            whfast_kepler_step(r, -dt / 4.); whfast_com_step(r, -dt / 4.);
+            whfast_evaluate_kick(r, dt / 6.);
+            whfast_kepler_step(r, dt / 8.); whfast_com_step(r, dt / 8.);
+            whfast_evaluate_kick(r, dt);
+            whfast_kepler_step(r, -dt / 8.); whfast_com_step(r, -dt / 8.);
+            whfast_evaluate_kick(r, -dt / 6.);
+            whfast_kepler_step(r, dt / 4.); whfast_com_step(r, dt / 4.);
+            whfast_evaluate_kick(r, dt / 6.);
+            break;
+        case 3: {                                                  /* LAZY (:1233-1247) */
+            const double pf = dt * dt / 12.;
+            for (size_t i = 1; i < N; i++) {
+                r->particles[i].x += pf * r->particles[i].ax;
+                r->particles[i].y += pf * r->particles[i].ay;
+                r->particles[i].z += pf * r->particles[i].az;
+            }
+            whfast_update_acceleration(r);
+            whfast_interaction_step(r, dt);
+            break;
+        }
+        default:                                                   /* DEFAULT */
+            whfast_interaction_step(r, dt);
+    }
     r->whfast_is_synchronized = 0;
     if (r->whfast_safe_mode) orc_whfast_synchronize(r);
     r->t += dt / 2.;

@@ -67,6 +67,11 @@ typedef struct orc_sim {
     orc_particle* p_jh;         /* WHFast Jacobi state, N entries (caller-owned) */
     double* cs;                 /* compensated-sum scratch, 3N (caller-owned) */
     double sei_lastdt, sei_sindt, sei_tandt, sei_sindtz, sei_tandtz;
+    /* WHFast options (src/integrator_whfast.h:29-50), Jacobi coordinates */
+    int whfast_corrector;       /* 0, 3, 5, 7, 11, 17 */
+    int whfast_corrector2;
+    int whfast_kernel;          /* 0 DEFAULT, 1 MODIFIEDKICK, 2 COMPOSITION, 3 LAZY */
+    int whfast_keep_unsynchronized;
 } orc_sim;
 
 /* Gravity (src/gravity.c). *_serial = the reference built without OpenMP;

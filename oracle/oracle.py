@@ -7,6 +7,7 @@ src/boundary.c, src/integrator_{leapfrog,sei,whfast}.c, src/transformations.c,
 src/tools.c) and is pinned against golden vectors of the unmodified reference.
 """
 import ctypes
+import math
 import os
 import subprocess
 import sysconfig
@@ -40,7 +41,9 @@ class OrcSim(ctypes.Structure):
         ("rand_seed", ctypes.c_uint), ("error", ctypes.c_int),
         ("particles", ctypes.c_void_p), ("p_jh", ctypes.c_void_p), ("cs", ctypes.c_void_p),
         ("sei_lastdt", ctypes.c_double), ("sei_sindt", ctypes.c_double), ("sei_tandt", ctypes.c_double),
-        ("sei_sindtz", ctypes.c_double), ("sei_tandtz", ctypes.c_double)]
+        ("sei_sindtz", ctypes.c_double), ("sei_tandtz", ctypes.c_double),
+        ("whfast_corrector", ctypes.c_int), ("whfast_corrector2", ctypes.c_int),
+        ("whfast_kernel", ctypes.c_int), ("whfast_keep_unsynchronized", ctypes.c_int)]
 
 
 def _elf_matches_host(path):
@@ -109,6 +112,7 @@ def lib():
 
 GRAVITY = {"none": 0, "basic": 1, "compensated": 2, "tree": 3, "basic_omp": 101, "compensated_omp": 102}
 BOUNDARY = {"none": 0, "open": 1, "periodic": 2, "shear": 3}
+WHFAST_KERNEL = {"default": 0, "modifiedkick": 1, "composition": 2, "lazy": 3}
 
 
 class Sim:
@@ -116,7 +120,8 @@ class Sim:
 
     def __init__(self, particles, G=1.0, softening=0.0, dt=0.0, t=0.0, N_active=None,
                  testparticle_type=0, boundary="none", root_size=-1.0, N_root=(1, 1, 1),
-                 N_ghost=(0, 0, 0), OMEGA=0.0, OMEGAZ=-1.0, opening_angle2=0.25, safe_mode=1):
+                 N_ghost=(0, 0, 0), OMEGA=0.0, OMEGAZ=-1.0, opening_angle2=0.25, safe_mode=1,
+                 corrector=0, corrector2=0, kernel=0, keep_unsynchronized=0):
         self.p = np.ascontiguousarray(particles, dtype=PARTICLE_DTYPE).copy()
         n = len(self.p)
         self.pj = np.zeros(n, dtype=PARTICLE_DTYPE)
@@ -133,6 +138,9 @@ class Sim:
         s.whfast_safe_mode = safe_mode
         s.whfast_is_synchronized = 1
         s.whfast_did_modify = 1
+        s.whfast_corrector, s.whfast_corrector2 = corrector, corrector2
+        s.whfast_kernel = WHFAST_KERNEL[kernel] if isinstance(kernel, str) else kernel
+        s.whfast_keep_unsynchronized = keep_unsynchronized
         s.particles = self.p.ctypes.data
         s.p_jh = self.pj.ctypes.data
         s.cs = self.cs.ctypes.data
@@ -165,6 +173,46 @@ class Sim:
     def whfast(self, steps):
         for _ in range(steps):
             lib().orc_whfast_step(self.ref)
+
+    def whfast_synchronize(self):
+        lib().orc_whfast_synchronize(self.ref)
+
+    def whfast_integrate(self, tmax, exact_finish_time=1):
+        """reb_simulation_integrate (src/simulation.c:372-464) with the exit test of
+        reb_check_exit (:291-354), for WHFast."""
+        s = self.s
+        if tmax != s.t:
+            s.dt = math.copysign(s.dt, 1.0 if tmax > s.t else -1.0)
+        last_full_dt, dt_last_done, last_step = s.dt, 0.0, False
+        while True:
+            sign = math.copysign(1.0, s.dt)
+            if exact_finish_time:
+                if (s.t + s.dt) * sign >= tmax * sign:
+                    if s.t == tmax:
+                        break
+                    if last_step:
+                        tscale = 1e-12 * abs(tmax)
+                        if tscale < 1e-200:
+                            tscale = 1e-12
+                        if abs(s.t - tmax) < tscale:
+                            break
+                        self.whfast_synchronize()
+                        s.dt = tmax - s.t
+                    else:
+                        last_step = True
+                        self.whfast_synchronize()
+                        if dt_last_done != 0.0:
+                            last_full_dt = dt_last_done
+                        s.dt = tmax - s.t
+                else:
+                    last_step = False
+            elif s.t * sign >= tmax * sign:
+                break
+            lib().orc_whfast_step(self.ref)
+            dt_last_done = s.dt
+        self.whfast_synchronize()
+        if exact_finish_time:
+            s.dt = last_full_dt
 
     def energy(self):
         return lib().orc_energy(self.ref)

@@ -45,7 +45,10 @@ class Config(ctypes.Structure):
         ("gravity", ctypes.c_int32), ("collision", ctypes.c_int32), ("collision_resolve", ctypes.c_int32),
         ("boundary", ctypes.c_int32), ("integrator", ctypes.c_int32), ("whfast_safe_mode", ctypes.c_int32),
         ("rand_seed", ctypes.c_uint32), ("status", ctypes.c_int32), ("collisions_log_n", ctypes.c_int64),
-        ("leapfrog_order", ctypes.c_int32), ("whfast_coordinates", ctypes.c_int32)]
+        ("leapfrog_order", ctypes.c_int32), ("whfast_coordinates", ctypes.c_int32),
+        ("whfast_corrector", ctypes.c_int32), ("whfast_corrector2", ctypes.c_int32),
+        ("whfast_kernel", ctypes.c_int32), ("whfast_keep_unsynchronized", ctypes.c_int32),
+        ("exact_finish_time", ctypes.c_int32), ("reserved0", ctypes.c_int32)]
 
 
 class ServerConfig(ctypes.Structure):

@@ -16,6 +16,7 @@ enum : uint32_t {
     DEV_ERR_OVERFLOW = 1u << 4,
     DEV_ERR_KEPLER = 1u << 5,
     DEV_ERR_STACK = 1u << 6,
+    DEV_ERR_PROGRAM = 1u << 7,
 };
 
 // Particle state in HBM, structure of arrays.  All arrays have `cap` entries.
@@ -54,6 +55,7 @@ struct rgpu_sim {
     size_t flush_bytes = 0;
     bool did_modify = true;
     bool whfast_synchronized = true;
+    double dt_last_done = 0.;          // dt of the last completed step (src/rebound.h: dt_last_done)
     SeiCache sei{};
     // last collision search result (device), consumed by the resolve stage
     size_t n_pairs = 0;

@@ -41,6 +41,7 @@ int read_status(rgpu_sim* s) {
     if (st & DEV_ERR_STACK) return set_error(s, RGPU_ERR_TREE_DEPTH, "Tree walk stack overflow.");
     if (st & DEV_ERR_OVERFLOW) return set_error(s, RGPU_ERR_OVERFLOW, "Device output buffer overflow.");
     if (st & DEV_ERR_KEPLER) return set_error(s, RGPU_ERR_ARG, "Kepler solver did not converge.");
+    if (st & DEV_ERR_PROGRAM) return set_error(s, RGPU_ERR_ARG, "Unknown operator in a WHFast program.");
     return set_error(s, RGPU_ERR_CUDA, "unknown device status");
 }
 
@@ -413,6 +414,7 @@ void rgpu_config_default(rgpu_config* c) {
     c->boundary = RGPU_BOUNDARY_NONE;
     c->integrator = RGPU_INTEGRATOR_LEAPFROG;
     c->whfast_safe_mode = 1;
+    c->exact_finish_time = 1;
     c->status = -1;
 }
 
@@ -543,6 +545,7 @@ int rgpu_steps(rgpu_sim* s, int64_t n) {
             default: return set_error(s, RGPU_ERR_ARG, "unknown integrator");
         }
         s->did_modify = false;
+        s->dt_last_done = s->cfg.dt;
         RGPU_TRY(boundary_check(s));
         if (s->cfg.collision != RGPU_COLLISION_NONE) {
             size_t nf = 0;
@@ -555,27 +558,53 @@ int rgpu_steps(rgpu_sim* s, int64_t n) {
     return read_status(s);
 }
 
+// Brings the integrator state to synchronized coordinates (reb_simulation_synchronize).
+static int synchronize_state(rgpu_sim* s) {
+    if (s->cfg.integrator == RGPU_INTEGRATOR_WHFAST) return whfast_synchronize(s);
+    return RGPU_OK;
+}
+
+// reb_simulation_integrate (src/simulation.c:372-464) with the exit test of
+// reb_check_exit (:291-354): with exact_finish_time the state is synchronized
+// before the shortened last step, and dt returns to the last full step at the end.
 int rgpu_integrate(rgpu_sim* s, double tmax) {
     if (!s) return RGPU_ERR_ARG;
-    const double dt = s->cfg.dt;
-    if (dt == 0.0) return set_error(s, RGPU_ERR_ARG, "dt must be nonzero");
-    const double dir = dt > 0 ? 1.0 : -1.0;
-    while ((tmax - s->cfg.t) * dir > 0) {
-        const double remain = tmax - s->cfg.t;
-        if (remain * dir < dt * dir) {
-            // Last, shortened step (exact_finish_time = 1).
-            s->cfg.dt = remain;
-            const int rc = rgpu_steps(s, 1);
-            s->cfg.dt = dt;
-            s->cfg.t = tmax;
-            RGPU_TRY(rc);
+    rgpu_config& c = s->cfg;
+    if (c.dt == 0.0) return set_error(s, RGPU_ERR_ARG, "dt must be nonzero");
+    if (tmax != c.t) c.dt = std::copysign(c.dt, tmax > c.t ? 1.0 : -1.0);
+    double last_full_dt = c.dt;
+    s->dt_last_done = 0.;
+    bool last_step = false;
+    for (;;) {
+        const double dtsign = std::copysign(1., c.dt);
+        if (c.exact_finish_time) {
+            if ((c.t + c.dt) * dtsign >= tmax * dtsign) {         // the next step would overshoot
+                if (c.t == tmax) break;
+                if (last_step) {
+                    double tscale = 1e-12 * std::fabs(tmax);
+                    if (tscale < 1e-200) tscale = 1e-12;
+                    if (std::fabs(c.t - tmax) < tscale) break;
+                    RGPU_TRY(synchronize_state(s));
+                    c.dt = tmax - c.t;
+                } else {
+                    last_step = true;
+                    RGPU_TRY(synchronize_state(s));
+                    if (s->dt_last_done != 0.) last_full_dt = s->dt_last_done;
+                    c.dt = tmax - c.t;
+                }
+            } else {
+                last_step = false;
+            }
+        } else if (c.t * dtsign >= tmax * dtsign) {
             break;
         }
-        const double t_before = s->cfg.t;
+        const double t_before = c.t;
         RGPU_TRY(rgpu_steps(s, 1));
-        if (s->cfg.t == t_before) return set_error(s, RGPU_ERR_ARG, "dt too small to advance t");
+        if (c.status == 7) break;                                   // collision halt
+        if (c.t == t_before) return set_error(s, RGPU_ERR_ARG, "dt too small to advance t");
     }
-    if (s->cfg.integrator == RGPU_INTEGRATOR_WHFAST) RGPU_TRY(whfast_synchronize(s));
+    RGPU_TRY(synchronize_state(s));
+    if (c.exact_finish_time) c.dt = last_full_dt;
     return read_status(s);
 }
 

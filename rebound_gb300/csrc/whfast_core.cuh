@@ -302,7 +302,7 @@ __device__ __forceinline__ void gravity_01(const System<NB>& s, double ax[NB], d
 template <int NB>
 __device__ __forceinline__ void interaction_step(Jacobi<NB>& j, const System<NB>& s, const double ax[NB],
                                                  const double ay[NB], const double az[NB], double G, double dt,
-                                                 int N, int Na) {
+                                                 int N, int Na, bool jacobi_term = true) {
     double jax[NB], jay[NB], jaz[NB];
     double eta = s.m[0];
     double sx = eta * ax[0], sy = eta * ay[0], sz = eta * az[0];
@@ -332,7 +332,7 @@ __device__ __forceinline__ void interaction_step(Jacobi<NB>& j, const System<NB>
         j.vx[i] += dt * jax[i];
         j.vy[i] += dt * jay[i];
         j.vz[i] += dt * jaz[i];
-        if (i > 1) {
+        if (i > 1 && jacobi_term) {   // with gravity = JACOBI the term is in the accelerations
             const double rj2i = 1. / (qx * qx + qy * qy + qz * qz);
             const double rji = sqrt(rj2i);
             const double rj3iM = rji * rj2i * G * eta;

@@ -6,12 +6,38 @@
 
 struct WhfastBuffers {
     double* jac = nullptr;   // 7 * cap: x, y, z, vx, vy, vz, m (Jacobi, p_jh)
-    size_t cap = 0;
+    double* keep = nullptr;  // 7 * cap: p_jh saved across a keep_unsynchronized synchronize
+    size_t cap = 0, keep_cap = 0;
 };
 
 namespace wh_plain {
 
 enum : int { kFromInertial = 1, kFirstHalf = 2, kSyncAtEnd = 4, kSyncOnly = 8 };
+
+// Operators of a WHFast program: one step or synchronize with correctors or a
+// non-default kernel, laid out by the host in the reference's order.
+enum : uint8_t {
+    kOpFromInertial = 0,  // inertial -> Jacobi coordinates (positions and velocities)
+    kOpDrift,             // Kepler drift of every Jacobi body by d
+    kOpCom,               // centre-of-mass drift by d
+    kOpToInertial,        // Jacobi -> inertial
+    kOpGravity,           // BASIC gravity, the 0-1 pair skipped, into the accelerations
+    kOpGravityJacobi,     // gravity = JACOBI (src/gravity.c:108-162)
+    kOpKick,              // interaction step by d with the Jacobi term
+    kOpKickNoJacobiTerm,  // interaction step by d, Jacobi term already in the gravity
+    kOpJerk,              // accelerations += d * jerk (kernel MODIFIEDKICK)
+    kOpLazyShift,         // positions of bodies 1.. += d * accelerations (kernel LAZY)
+};
+
+// Up to 400 operators per launch keeps the kernel's parameters under 4 KB;
+// longer calls run as several launches (the whole state goes through memory
+// between them, so a split anywhere is exact).
+constexpr int kMaxOps = 400;
+struct Program {
+    double d[kMaxOps];
+    uint8_t op[kMaxOps];
+    int32_t n;
+};
 
 template <int NB>
 __device__ void load_sys(wh::System<NB>& s, const ParticlesSoA& p, int N) {
@@ -58,5 +84,8 @@ __device__ void store_jac(const wh::Jacobi<NB>& j, double* jac, size_t cap, int 
 
 // Democratic heliocentric step / synchronize on the handle (whfast_dh.cu).
 int launch_dh(rgpu_sim* s, int flags);
+
+// Runs one program on the handle's system (whfast_prog.cu).
+int launch_program(rgpu_sim* s, const Program& prog);
 
 }  // namespace wh_plain

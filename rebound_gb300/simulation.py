@@ -24,7 +24,8 @@ _CFG_INTS = ("testparticle_type", "N_root_x", "N_root_y", "N_root_z", "N_ghost_x
 
 
 class WHFastSettings:
-    """Subset of rebound's ri_whfast used on the GPU path (safe_mode, coordinates)."""
+    """rebound's ri_whfast on the GPU path: safe_mode, coordinates, correctors, kernel,
+    keep_unsynchronized (src/integrator_whfast.h:28-50)."""
 
     COORDINATES = {"jacobi": 0, "democraticheliocentric": 1}
 
@@ -47,6 +48,42 @@ class WHFastSettings:
     @coordinates.setter
     def coordinates(self, name):
         self._sim._cfg.whfast_coordinates = self.COORDINATES[name]
+
+    # symplectic correctors and kernels (src/integrator_whfast.h:29-37)
+    KERNELS = {"default": 0, "modifiedkick": 1, "composition": 2, "lazy": 3}
+
+    @property
+    def corrector(self):
+        return self._sim._cfg.whfast_corrector
+
+    @corrector.setter
+    def corrector(self, order):
+        self._sim._cfg.whfast_corrector = int(order)
+
+    @property
+    def corrector2(self):
+        return self._sim._cfg.whfast_corrector2
+
+    @corrector2.setter
+    def corrector2(self, v):
+        self._sim._cfg.whfast_corrector2 = int(v)
+
+    @property
+    def kernel(self):
+        k = self._sim._cfg.whfast_kernel
+        return next((n for n, v in self.KERNELS.items() if v == k), k)
+
+    @kernel.setter
+    def kernel(self, name):
+        self._sim._cfg.whfast_kernel = self.KERNELS[name] if isinstance(name, str) else int(name)
+
+    @property
+    def keep_unsynchronized(self):
+        return self._sim._cfg.whfast_keep_unsynchronized
+
+    @keep_unsynchronized.setter
+    def keep_unsynchronized(self, v):
+        self._sim._cfg.whfast_keep_unsynchronized = int(v)
 
 
 class Simulation:
@@ -191,8 +228,10 @@ class Simulation:
         self._push()
         self._after(self._L.rgpu_steps(self._h, int(n)))
 
-    def integrate(self, tmax):
-        """reb_simulation_integrate (src/simulation.c:465) with exact_finish_time = 1."""
+    def integrate(self, tmax, exact_finish_time=1):
+        """reb_simulation_integrate (src/simulation.c:465); exact_finish_time as rebound's
+        Simulation.integrate sets it (1: the last step is shortened to land on tmax)."""
+        self._cfg.exact_finish_time = int(exact_finish_time)
         self._push()
         self._after(self._L.rgpu_integrate(self._h, float(tmax)))
 

@@ -504,9 +504,93 @@ def fixture_whfast_dh():
     np.savez_compressed(os.path.join(HERE, "whfast_dh.npz"), **out)
 
 
+def fixture_whfast_advanced():
+    """WHFast symplectic correctors and kernels (src/integrator_whfast.c:653-785,
+    1113-1259): the scenarios of rebound/tests/test_whfast_advanced.py with the
+    reference's own errors and end states, short trajectories for bit-exact replay,
+    and the reference's IAS15 positions for the comparison of its compias test."""
+    out = {}
+
+    def rel(a, b):
+        return abs((a - b) / b)
+
+    settings = [(0, 0, "default"), (3, 0, "default"), (5, 0, "default"), (7, 0, "default"),
+                (11, 0, "default"), (17, 0, "default"), (0, 0, "modifiedkick"), (3, 0, "modifiedkick"),
+                (5, 0, "modifiedkick"), (7, 0, "modifiedkick"), (11, 0, "modifiedkick"),
+                (17, 0, "modifiedkick"), (17, 0, "composition"), (17, 0, "lazy"), (11, 1, "modifiedkick"),
+                (3, 0, "composition"), (3, 0, "lazy"), (3, 1, "lazy")]
+    sim = rebound.Simulation()
+    sim.add("outer solar system")
+    out["oss"] = state(sim)
+    out["dt"] = 0.0123235235 * sim.particles[1].P
+    out["settings"] = np.array([(c, c2, ["default", "modifiedkick", "composition", "lazy"].index(k))
+                                for c, c2, k in settings], dtype=np.int32)
+
+    def make(c, c2, k, shift=0.0, safe=None):
+        sim = rebound.Simulation()
+        load(sim, out["oss"])
+        for p in sim.particles:
+            p.vx += shift
+        sim.integrator = "whfast"
+        sim.integrator.corrector = c
+        sim.integrator.corrector2 = c2
+        sim.integrator.kernel = k
+        if safe is not None:
+            sim.integrator.safe_mode = safe
+        sim.dt = float(out["dt"])
+        return sim
+
+    for c, c2, k in settings:
+        tag = "c%d_c2%d_%s" % (c, c2, k)
+        sim = make(c, c2, k, safe=False)                         # energy (test_whfast_advanced.py:35-48)
+        e0 = sim.energy()
+        sim.integrate(1000. * 2. * 3.1415)
+        out["energy_err_" + tag] = rel(e0, sim.energy())
+        out["energy_end_" + tag] = state(sim)
+        sim = make(c, c2, k, shift=1.0)                          # energy_notcom (:50-68), safe_mode 1
+        e0 = sim.energy()
+        sim.integrate(1000. * 2. * 3.1415)
+        out["notcom_err_" + tag] = rel(e0, sim.energy())
+        out["notcom_end_" + tag] = state(sim)
+        sim = make(c, c2, k, shift=1050.)                        # compias (:70-92)
+        sim.integrate(13.21415, exact_finish_time=False)
+        out["compias_end_" + tag] = state(sim)
+        out["compias_t_" + tag] = sim.t
+        sim = make(c, c2, k, shift=1.0)                          # backandforth (:94-111)
+        sim.steps(10)
+        sim.dt *= -1
+        sim.steps(10)
+        out["bf_end_" + tag] = state(sim)
+        sim = make(c, c2, k, safe=False)                         # 20 steps, synchronize (bit-exact replay)
+        sim.steps(20)
+        sim.synchronize()
+        out["traj_" + tag] = state(sim)
+    # the IAS15 reference solution of the compias test at the WHFast runs' end time
+    t_end = float(out["compias_t_c3_c20_default"])
+    simi = rebound.Simulation()
+    simi.integrator = "ias15"
+    load(simi, out["oss"])
+    for p in simi.particles:
+        p.vx += 1050.
+    simi.integrate(t_end, exact_finish_time=True)
+    out["compias_ias15"] = state(simi)
+    out["compias_ias15_t"] = simi.t
+    # keep_unsynchronized: steps, synchronize without leaving the drift, more steps
+    for c in (0, 5):
+        sim = make(c, 0, "default", safe=False)
+        sim.integrator.keep_unsynchronized = 1
+        sim.steps(10)
+        sim.synchronize()
+        out["keep_mid_c%d" % c] = state(sim)
+        sim.steps(10)
+        sim.synchronize()
+        out["keep_end_c%d" % c] = state(sim)
+    np.savez_compressed(os.path.join(HERE, "whfast_advanced.npz"), **out)
+
+
 if __name__ == "__main__":
     which = sys.argv[2:] or ["gravity_cases", "ring", "whfast", "sei", "gravity_plummer", "reference_cases",
-                             "leapfrog_orders", "whfast_dh"]
+                             "leapfrog_orders", "whfast_dh", "whfast_advanced"]
     for w in which:
         print("generating", w, flush=True)
         globals()["fixture_" + w]() if w != "sei" else fixture_sei_periodic()

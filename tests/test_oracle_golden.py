@@ -125,3 +125,58 @@ def test_oracle_energy_after_1000_leapfrog_steps_recorded():
     g = golden("gravity_plummer.npz")
     err = abs((g["energy1000"] - g["energy0"]) / g["energy0"])
     assert 0 < err < 1e-2
+
+
+KERNELS = ("default", "modifiedkick", "composition", "lazy")
+
+
+def advanced_cases():
+    g = golden("whfast_advanced.npz")
+    return [(int(c), int(c2), KERNELS[int(k)]) for c, c2, k in g["settings"]]
+
+
+def advanced_sim(g, c, c2, kernel, shift=0.0, safe=1, keep=0):
+    p = g["oss"].copy()
+    p["vx"] += shift
+    return O.Sim(p, dt=float(g["dt"]), safe_mode=safe, corrector=c, corrector2=c2, kernel=kernel,
+                 keep_unsynchronized=keep)
+
+
+@pytest.mark.parametrize("c,c2,kernel", advanced_cases())
+def test_oracle_whfast_correctors_and_kernels(c, c2, kernel):
+    # WHFast correctors / kernels against the reference's own runs of
+    # rebound/tests/test_whfast_advanced.py, bit for bit
+    g = golden("whfast_advanced.npz")
+    tag = "c%d_c2%d_%s" % (c, c2, kernel)
+    s = advanced_sim(g, c, c2, kernel, safe=0)
+    s.whfast(20)
+    s.whfast_synchronize()
+    assert max_diff(s.p, g["traj_" + tag]) == 0.0
+    s = advanced_sim(g, c, c2, kernel, safe=0)
+    e0 = s.energy()
+    s.whfast_integrate(1000. * 2. * 3.1415)
+    assert max_diff(s.p, g["energy_end_" + tag]) == 0.0
+    assert abs((e0 - s.energy()) / s.energy()) == float(g["energy_err_" + tag])
+    s = advanced_sim(g, c, c2, kernel, shift=1.0)
+    s.whfast_integrate(1000. * 2. * 3.1415)
+    assert max_diff(s.p, g["notcom_end_" + tag]) == 0.0
+    s = advanced_sim(g, c, c2, kernel, shift=1050.)
+    s.whfast_integrate(13.21415, exact_finish_time=0)
+    assert max_diff(s.p, g["compias_end_" + tag]) == 0.0 and s.s.t == float(g["compias_t_" + tag])
+    s = advanced_sim(g, c, c2, kernel, shift=1.0)
+    s.whfast(10)
+    s.s.dt *= -1
+    s.whfast(10)
+    assert max_diff(s.p, g["bf_end_" + tag]) == 0.0
+
+
+@pytest.mark.parametrize("c", [0, 5])
+def test_oracle_whfast_keep_unsynchronized(c):
+    g = golden("whfast_advanced.npz")
+    s = advanced_sim(g, c, 0, "default", safe=0, keep=1)
+    s.whfast(10)
+    s.whfast_synchronize()
+    assert max_diff(s.p, g["keep_mid_c%d" % c]) == 0.0
+    s.whfast(10)
+    s.whfast_synchronize()
+    assert max_diff(s.p, g["keep_end_c%d" % c]) == 0.0
