@@ -96,6 +96,7 @@ class Simulation:
         self._L.rgpu_config_default(ctypes.byref(self._cfg))
         self._host = np.zeros(0, dtype=PARTICLE_DTYPE)
         self._host_dirty = False      # host particles changed since the last upload
+        self._host_seen = None        # copy of the array handed out by `particles`
         self._device_newer = False    # device stepped since the last download
         self.ri_whfast = WHFastSettings(self)
 
@@ -187,9 +188,12 @@ class Simulation:
 
     @property
     def particles(self):
-        """Host copy of the particle array (synchronized from the GPU)."""
+        """Host copy of the particle array (synchronized from the GPU).  Changes the
+        caller makes to it are uploaded by the next call that runs on the GPU; a
+        read alone leaves the integrator state as it is (as reading
+        sim.particles does in the reference)."""
         self._pull()
-        self._host_dirty = True    # the caller may modify the returned array
+        self._host_seen = self._host.copy()
         return self._host
 
     def set_particles_array(self, arr):
@@ -199,6 +203,12 @@ class Simulation:
 
     def _push(self):
         check(self._L.rgpu_sim_configure(self._h, ctypes.byref(self._cfg)), self._h)
+        seen = self.__dict__.get("_host_seen")
+        if seen is not None:
+            if not self._host_dirty and (len(seen) != len(self._host) or
+                                         not np.array_equal(seen.view(np.uint8), self._host.view(np.uint8))):
+                self._host_dirty = True
+            self._host_seen = None
         if self._host_dirty:
             check(self._L.rgpu_sim_set_particles(self._h, self._host.ctypes.data, len(self._host),
                                                  PARTICLE_DTYPE.itemsize), self._h)

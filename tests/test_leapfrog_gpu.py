@@ -59,10 +59,23 @@ def test_mixed_energy_drift_reported(gpu):
 
 
 def test_integrate_exact_finish_time(gpu):
+    # reb_simulation_integrate with exact_finish_time = 1 (src/simulation.c:291-354,
+    # 455-458): full steps while t + dt < tmax, one shortened step of tmax - t, exit
+    # once |t - tmax| < 1e-12 tmax, dt back to the last full step.  Each leapfrog
+    # step advances t by two half steps, so t ends where that sum rounds
+    # (0.010499999999999999, which the reference's own run reports as well).
     g = golden("gravity_plummer.npz")
     sim = make(gpu, g["particles"][:256])
     sim.integrate(0.0105)
-    assert sim.t == 0.0105
+    t, dt = 0.0, 1e-3
+    while t + dt < 0.0105:
+        t += dt / 2.
+        t += dt / 2.
+    last = 0.0105 - t
+    t += last / 2.
+    t += last / 2.
+    assert sim.t == t and abs(sim.t - 0.0105) < 1e-12 * 0.0105
+    assert sim.dt == 1e-3
 
 
 @pytest.mark.parametrize("order", [4, 6, 8])
