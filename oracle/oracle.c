@@ -21,6 +21,12 @@ static size_t n_active_of(const orc_sim* r) {
     return r->N_active == SIZE_MAX ? r->N : r->N_active;
 }
 
+/* N_active as WHFast reads it (src/integrator_whfast.c:1119): testparticle_type 1
+ * puts every body into the coordinate transforms. */
+static size_t wh_active_of(const orc_sim* r) {
+    return (r->N_active == SIZE_MAX || r->testparticle_type == 1) ? r->N : r->N_active;
+}
+
 /* ------------------------------------------------------------------------
  * Boundary: src/boundary.c:35-141 (check) and :145-201 (ghost box offsets).
  * ---------------------------------------------------------------------- */
@@ -942,7 +948,7 @@ static void inertial_to_jacobi_acc(const orc_particle* ps, orc_particle* pj, con
 
 static void whfast_kepler_step(orc_sim* r, double dt) {           /* :589-636, serial branch */
     const double m0 = r->particles[0].m;
-    const size_t N = r->N, Na = n_active_of(r);
+    const size_t N = r->N, Na = wh_active_of(r);
     double eta = m0;
     for (size_t i = 1; i < N; i++) {
         if (i < Na) eta += r->p_jh[i].m;
@@ -957,7 +963,7 @@ static void whfast_com_step(orc_sim* r, double dt) {              /* :638-651 */
 }
 
 static void whfast_interaction_step(orc_sim* r, double dt) {      /* :431-492 */
-    const size_t N = r->N, Na = n_active_of(r);
+    const size_t N = r->N, Na = wh_active_of(r);
     orc_particle* pj = r->p_jh;
     /* kernels MODIFIEDKICK and LAZY run with gravity = JACOBI: the Jacobi term is
      * already in the accelerations (:458) */
@@ -1089,7 +1095,7 @@ static const double corr2_b = 0.03486083443891981449909050107438281205803;
 
 /* Jacobi -> inertial, then the accelerations, then a kick of dt. */
 static void whfast_evaluate_kick(orc_sim* r, double dt) {
-    orc_jacobi_to_inertial_posvel(r->particles, r->p_jh, r->particles, r->N, n_active_of(r));
+    orc_jacobi_to_inertial_posvel(r->particles, r->p_jh, r->particles, r->N, wh_active_of(r));
     whfast_update_acceleration(r);
     whfast_interaction_step(r, dt);
 }
@@ -1146,7 +1152,7 @@ void orc_whfast_synchronize(orc_sim* r) {                         /* :1051-1111 
         whfast_com_step(r, d);
         if (r->whfast_corrector2) apply_corrector2(r, -1.);
         if (r->whfast_corrector) apply_corrector(r, -1., r->whfast_corrector);
-        orc_jacobi_to_inertial_posvel(r->particles, r->p_jh, r->particles, r->N, n_active_of(r));
+        orc_jacobi_to_inertial_posvel(r->particles, r->p_jh, r->particles, r->N, wh_active_of(r));
         if (keep) {
             memcpy(r->p_jh, keep, sizeof(orc_particle) * r->N);
             free(keep);
@@ -1158,7 +1164,7 @@ void orc_whfast_synchronize(orc_sim* r) {                         /* :1051-1111 
 
 void orc_whfast_step(orc_sim* r) {                                /* :1113-1259 */
     const double dt = r->dt;
-    const size_t N = r->N, Na = n_active_of(r);
+    const size_t N = r->N, Na = wh_active_of(r);
     r->gravity_ignore_terms = 1;
     if (r->whfast_safe_mode || r->whfast_did_modify) {
         if (r->whfast_is_synchronized == 0) orc_whfast_synchronize(r);

@@ -12,7 +12,7 @@ using namespace wh_plain;
 
 // One step (or a synchronize) of src/integrator_whfast.c for the handle's system.
 template <int NB>
-__global__ void __launch_bounds__(32) whfast_plain(ParticlesSoA p, double* jac, size_t cap, int N, int Na, int tp,
+__global__ void __launch_bounds__(32) whfast_plain(ParticlesSoA p, double* jac, size_t cap, int N, int Na, int Ng, int tp,
                                                    double G, double eps2, double dt, int flags, uint32_t* status) {
     if (threadIdx.x != 0) return;
     wh::System<NB> s;
@@ -33,7 +33,7 @@ __global__ void __launch_bounds__(32) whfast_plain(ParticlesSoA p, double* jac, 
         wh::to_inertial(s, j, N, Na);
         if (pass == 0 && !sync_only) {
             double ax[NB], ay[NB], az[NB];
-            wh::gravity_01(s, ax, ay, az, G, eps2, N, Na, tp);
+            wh::gravity_01(s, ax, ay, az, G, eps2, N, Ng, tp);
             wh::interaction_step(j, s, ax, ay, az, G, dt, N, Na);
 #pragma unroll
             for (int i = 0; i < NB; i++) {
@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(32) whfast_plain(ParticlesSoA p, double* jac, 
     store_jac(j, jac, cap, N);               // synchronize keeps the drifted coordinates, as the reference
 }
 
-typedef void (*PlainKernel)(ParticlesSoA, double*, size_t, int, int, int, double, double, double, int, uint32_t*);
+typedef void (*PlainKernel)(ParticlesSoA, double*, size_t, int, int, int, int, double, double, double, int, uint32_t*);
 
 template <int NB>
 PlainKernel pick() { return whfast_plain<NB>; }
@@ -88,7 +88,7 @@ int launch(rgpu_sim* s, int flags) {
     if (!k) return set_error(s, RGPU_ERR_UNSUPPORTED, "WHFast on the GPU supports 2..16 particles per simulation");
     const rgpu_config& c = s->cfg;
     ktimer_begin(s);
-    k<<<1, 32, 0, s->stream>>>(s->p, s->wh->jac, s->cap, N, (int)n_active(s), c.testparticle_type, c.G,
+    k<<<1, 32, 0, s->stream>>>(s->p, s->wh->jac, s->cap, N, wh_active(s), (int)n_active(s), c.testparticle_type, c.G,
                                c.softening * c.softening, c.dt, flags, s->d_status);
     ktimer_end(s);
     g_launches++;
@@ -203,7 +203,8 @@ struct ProgramBuilder {
 };
 
 bool uses_program(const rgpu_config& c) {
-    return c.whfast_corrector != 0 || c.whfast_corrector2 != 0 || c.whfast_kernel != kKernelDefault;
+    return c.whfast_corrector != 0 || c.whfast_corrector2 != 0 || c.whfast_kernel != kKernelDefault ||
+           c.whfast_coordinates >= 2;
 }
 
 int ensure_keep(rgpu_sim* s) {
@@ -218,13 +219,13 @@ int ensure_keep(rgpu_sim* s) {
 // reb_integrator_whfast_init's checks (src/integrator_whfast.c:909-928).
 int check_config(rgpu_sim* s) {
     const rgpu_config& c = s->cfg;
-    if (c.whfast_coordinates != 0 && c.whfast_coordinates != 1)
-        return set_error(s, RGPU_ERR_UNSUPPORTED, "WHFast coordinates: 0 (Jacobi) or 1 (democratic heliocentric)");
+    if (c.whfast_coordinates < 0 || c.whfast_coordinates > 3)
+        return set_error(s, RGPU_ERR_ARG, "WHFast coordinates: 0 Jacobi, 1 democratic heliocentric, 2 WHDS, 3 barycentric");
     if (c.whfast_kernel < 0 || c.whfast_kernel > 3)
         return set_error(s, RGPU_ERR_ARG, "Kernel method must be 0 (default), 1 (exact modified kick), 2 (composition kernel), or 3 (lazy implementer's modified kick). ");
     if (c.whfast_kernel != kKernelDefault && c.whfast_coordinates != 0)
         return set_error(s, RGPU_ERR_ARG, "Non-standard kernel requires Jacobi coordinates.");
-    if (c.whfast_corrector != 0 && c.whfast_coordinates != 0)
+    if (c.whfast_corrector != 0 && c.whfast_coordinates != 0 && c.whfast_coordinates != 3)
         return set_error(s, RGPU_ERR_ARG, "Symplectic correctors are only compatible with Jacobi and Barycentric coordinates.");
     const int k = c.whfast_corrector;
     if (k != 0 && k != 3 && k != 5 && k != 7 && k != 11 && k != 17)
@@ -236,7 +237,7 @@ int check_config(rgpu_sim* s) {
     return RGPU_OK;
 }
 
-// One step as a program (src/integrator_whfast.c:1113-1259, Jacobi coordinates).
+// One step as a program (src/integrator_whfast.c:1113-1259).
 int program_step(rgpu_sim* s, bool from_inertial) {
     const rgpu_config& c = s->cfg;
     const double dt = c.dt;
@@ -249,10 +250,15 @@ int program_step(rgpu_sim* s, bool from_inertial) {
     } else {
         b.drift_com(dt);
     }
+    const bool jumps = c.whfast_coordinates == 1 || c.whfast_coordinates == 2;
+    if (jumps) b.push(kOpJump, dt / 2.);
     b.push(kOpToInertial);
     b.push(b.grav);
     switch (c.whfast_kernel) {
-        case kKernelDefault: b.push(b.kick, dt); break;
+        case kKernelDefault:
+            b.push(b.kick, dt);
+            if (jumps) b.push(kOpJump, dt / 2.);
+            break;
         case kKernelModifiedKick: b.push(kOpJerk, dt * dt / 12.); b.push(b.kick, dt); break;
         case kKernelComposition:
             b.push(b.kick, -dt / 6.);
@@ -277,7 +283,8 @@ int whfast_step(rgpu_sim* s) {
     if (s->N == 0) return RGPU_OK;
     rgpu_config& c = s->cfg;
     RGPU_TRY(check_config(s));
-    c.gravity_ignore_terms = c.whfast_coordinates == 1 ? 2 : 1;  // :929-938
+    const int k = c.whfast_coordinates;                          // :929-938
+    c.gravity_ignore_terms = k == 0 ? 1 : k == 3 ? 0 : 2;
     int flags = 0;
     if (c.whfast_safe_mode || s->did_modify) {
         if (!s->whfast_synchronized) RGPU_TRY(whfast_synchronize(s));

@@ -13,7 +13,7 @@ namespace {
 using namespace wh_plain;
 
 template <int NB>
-__global__ void __launch_bounds__(32) whfast_plain_dh(ParticlesSoA p, double* buf, size_t cap, int N, int Na, int tp,
+__global__ void __launch_bounds__(32) whfast_plain_dh(ParticlesSoA p, double* buf, size_t cap, int N, int Na, int Ng, int tp,
                                                       double G, double eps2, double dt, int flags, uint32_t* status) {
     if (threadIdx.x != 0) return;
     wh::System<NB> s;
@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(32) whfast_plain_dh(ParticlesSoA p, double* bu
         wh::dh_to_inertial(s, h, N, Na);
         if (pass == 0 && !sync_only) {
             double ax[NB], ay[NB], az[NB];
-            wh::gravity_01<NB, 1>(s, ax, ay, az, G, eps2, N, Na, tp);
+            wh::gravity_01<NB, 1>(s, ax, ay, az, G, eps2, N, Ng, tp);
             wh::interaction_step_dh(h, ax, ay, az, dt, N);
             wh::jump_step_dh(h, s, dt / 2., N, Na);
 #pragma unroll
@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(32) whfast_plain_dh(ParticlesSoA p, double* bu
     store_jac(h, buf, cap, N);               // synchronize keeps the drifted coordinates, as the reference
 }
 
-typedef void (*PlainKernel)(ParticlesSoA, double*, size_t, int, int, int, double, double, double, int, uint32_t*);
+typedef void (*PlainKernel)(ParticlesSoA, double*, size_t, int, int, int, int, double, double, double, int, uint32_t*);
 
 PlainKernel kernel_for(int n) {
     switch (n) {
@@ -78,7 +78,7 @@ int wh_plain::launch_dh(rgpu_sim* s, int flags) {
     if (!k) return set_error(s, RGPU_ERR_UNSUPPORTED, "WHFast on the GPU supports 2..16 particles per simulation");
     const rgpu_config& c = s->cfg;
     ktimer_begin(s);
-    k<<<1, 32, 0, s->stream>>>(s->p, s->wh->jac, s->cap, N, (int)n_active(s), c.testparticle_type, c.G,
+    k<<<1, 32, 0, s->stream>>>(s->p, s->wh->jac, s->cap, N, wh_active(s), (int)n_active(s), c.testparticle_type, c.G,
                                c.softening * c.softening, c.dt, flags, s->d_status);
     ktimer_end(s);
     g_launches++;

@@ -27,6 +27,7 @@ enum : uint8_t {
     kOpKickNoJacobiTerm,  // interaction step by d, Jacobi term already in the gravity
     kOpJerk,              // accelerations += d * jerk (kernel MODIFIEDKICK)
     kOpLazyShift,         // positions of bodies 1.. += d * accelerations (kernel LAZY)
+    kOpJump,              // jump step by d (democratic heliocentric and WHDS coordinates)
 };
 
 // Up to 400 operators per launch keeps the kernel's parameters under 4 KB;
@@ -80,6 +81,13 @@ __device__ void store_jac(const wh::Jacobi<NB>& j, double* jac, size_t cap, int 
         jac[3 * cap + i] = j.vx[i]; jac[4 * cap + i] = j.vy[i]; jac[5 * cap + i] = j.vz[i];
         jac[6 * cap + i] = j.m[i];
     }
+}
+
+// N_active as WHFast reads it (src/integrator_whfast.c:1119): with
+// testparticle_type = 1 every body takes part in the coordinate transforms; the
+// gravity keeps the plain N_active (n_active) for its test-particle loop.
+inline int wh_active(const rgpu_sim* s) {
+    return (s->cfg.testparticle_type == 1 || s->cfg.N_active < 0) ? (int)s->N : (int)s->cfg.N_active;
 }
 
 // Democratic heliocentric step / synchronize on the handle (whfast_dh.cu).

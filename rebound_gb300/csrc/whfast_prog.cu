@@ -1,6 +1,6 @@
-// WHFast programs on an rgpu_sim: the plain one-simulation-per-call path in Jacobi
-// coordinates with a first symplectic corrector of order 3, 5, 7, 11 or 17, the
-// second corrector, or the kernels MODIFIEDKICK, COMPOSITION and LAZY
+// WHFast programs on an rgpu_sim: the plain one-simulation-per-call path with a
+// first symplectic corrector of order 3, 5, 7, 11 or 17, the second corrector, the
+// kernels MODIFIEDKICK, COMPOSITION and LAZY, or WHDS / barycentric coordinates
 // (src/integrator_whfast.c:653-785, 1113-1259; Wisdom, Holman & Touma 1996;
 // Wisdom 2006; Rein, Tamayo & Brown 2019).  The host lays each call out as a list
 // of operators in the reference's order; one thread runs the list.  Every
@@ -106,10 +106,202 @@ __device__ void add_jerk(const wh::System<NB>& s, double ax[NB], double ay[NB], 
     }
 }
 
+// --- coordinate systems other than Jacobi (src/transformations.c:295-644) ---------
+// coords: 0 Jacobi, 1 democratic heliocentric, 2 WHDS (Hernandez & Dehnen 2017),
+// 3 barycentric; the values of REB_INTEGRATOR_WHFAST_COORDINATES.
+
+// reb_transformations_inertial_to_whds_posvel (:295-345): democratic heliocentric
+// positions and centre of mass, velocities of active bodies scaled by (m_0+m_i)/m_0.
 template <int NB>
-__global__ void __launch_bounds__(32) whfast_program(ParticlesSoA p, double* jac, size_t cap, int N, int Na, int tp,
-                                                     double G, double eps2, const __grid_constant__ Program prog,
-                                                     uint32_t* status) {
+__device__ void to_whds(const wh::System<NB>& s, wh::Jacobi<NB>& h, int N, int Na) {
+    wh::to_dh(s, h, N, Na);
+    const double m0 = s.m[0];
+#pragma unroll 1
+    for (int i = 1; i < Na; i++) {
+        const double mf = (m0 + s.m[i]) / m0;
+        h.vx[i] = mf * (s.vx[i] - h.vx[0]); h.vy[i] = mf * (s.vy[i] - h.vy[0]); h.vz[i] = mf * (s.vz[i] - h.vz[0]);
+    }
+}
+
+// reb_transformations_whds_to_inertial_posvel (:347-381).
+template <int NB>
+__device__ void whds_to_inertial(wh::System<NB>& s, const wh::Jacobi<NB>& h, int N, int Na) {
+    wh::dh_to_inertial(s, h, N, Na);          // positions and masses as democratic heliocentric
+    const double m0 = s.m[0];
+#pragma unroll 1
+    for (int i = 1; i < Na; i++) {
+        const double mf = (m0 + s.m[i]) / m0;
+        s.vx[i] = h.vx[i] / mf + h.vx[0]; s.vy[i] = h.vy[i] / mf + h.vy[0]; s.vz[i] = h.vz[i] / mf + h.vz[0];
+    }
+    double vx0 = 0., vy0 = 0., vz0 = 0.;
+#pragma unroll 1
+    for (int i = 1; i < Na; i++) {
+        const double m = s.m[i];
+        vx0 += h.vx[i] * m / (m0 + m); vy0 += h.vy[i] * m / (m0 + m); vz0 += h.vz[i] * m / (m0 + m);
+    }
+    s.vx[0] = h.vx[0] - vx0; s.vy[0] = h.vy[0] - vy0; s.vz[0] = h.vz[0] - vz0;
+}
+
+// reb_transformations_inertial_to_barycentric_posvel (:595-644).
+template <int NB>
+__device__ void to_bary(const wh::System<NB>& s, wh::Jacobi<NB>& b, int N, int Na) {
+    const double m0 = s.m[0];
+    double x = m0 * s.x[0], y = m0 * s.y[0], z = m0 * s.z[0];
+    double vx = m0 * s.vx[0], vy = m0 * s.vy[0], vz = m0 * s.vz[0], M = m0;
+    double sx = 0., sy = 0., sz = 0., svx = 0., svy = 0., svz = 0., sm = 0.;
+#pragma unroll 1
+    for (int i = 1; i < Na; i++) {
+        const double m = s.m[i];
+        sx += s.x[i] * m; sy += s.y[i] * m; sz += s.z[i] * m;
+        svx += s.vx[i] * m; svy += s.vy[i] * m; svz += s.vz[i] * m;
+        sm += m;
+    }
+    x += sx; y += sy; z += sz; vx += svx; vy += svy; vz += svz; M += sm;
+    const double mi = 1.0 / M;
+    b.x[0] = x * mi; b.y[0] = y * mi; b.z[0] = z * mi;
+    b.vx[0] = vx * mi; b.vy[0] = vy * mi; b.vz[0] = vz * mi;
+    b.m[0] = M;
+#pragma unroll 1
+    for (int i = 1; i < N; i++) {
+        b.m[i] = s.m[i];
+        b.x[i] = s.x[i] - b.x[0]; b.y[i] = s.y[i] - b.y[0]; b.z[i] = s.z[i] - b.z[0];
+        b.vx[i] = s.vx[i] - b.vx[0]; b.vy[i] = s.vy[i] - b.vy[0]; b.vz[i] = s.vz[i] - b.vz[0];
+    }
+}
+
+// reb_transformations_barycentric_to_inertial_posvel (:544-593); it also rebuilds
+// the star's mass as the total minus the active bodies'.
+template <int NB>
+__device__ void bary_to_inertial(wh::System<NB>& s, const wh::Jacobi<NB>& b, int N, int Na) {
+    const double M = b.m[0];
+    double x0 = M * b.x[0], y0 = M * b.y[0], z0 = M * b.z[0];
+    double vx0 = M * b.vx[0], vy0 = M * b.vy[0], vz0 = M * b.vz[0], m0 = M;
+    double sx = 0., sy = 0., sz = 0., svx = 0., svy = 0., svz = 0., sm = 0.;
+#pragma unroll 1
+    for (int i = 1; i < N; i++) {
+        s.x[i] = b.x[i] + b.x[0]; s.y[i] = b.y[i] + b.y[0]; s.z[i] = b.z[i] + b.z[0];
+        s.vx[i] = b.vx[i] + b.vx[0]; s.vy[i] = b.vy[i] + b.vy[0]; s.vz[i] = b.vz[i] + b.vz[0];
+        if (i < Na) {
+            const double m = b.m[i];
+            s.m[i] = m;
+            sx += s.x[i] * m; sy += s.y[i] * m; sz += s.z[i] * m;
+            svx += s.vx[i] * m; svy += s.vy[i] * m; svz += s.vz[i] * m;
+            sm += m;
+        }
+    }
+    x0 -= sx; y0 -= sy; z0 -= sz; vx0 -= svx; vy0 -= svy; vz0 -= svz; m0 -= sm;
+    const double m0i = 1. / m0;
+    s.m[0] = m0;
+    s.x[0] = x0 * m0i; s.y[0] = y0 * m0i; s.z[0] = z0 * m0i;
+    s.vx[0] = vx0 * m0i; s.vy[0] = vy0 * m0i; s.vz[0] = vz0 * m0i;
+}
+
+// reb_integrator_whfast_kepler_step (src/integrator_whfast.c:589-636), every
+// coordinate system through one inlined solver: the gravitational parameter of
+// body i is G times the interior Jacobi mass, m_0, m_0 + m_i (WHDS, active) or the
+// total mass (barycentric).
+template <int NB>
+__device__ void drift(wh::Jacobi<NB>& j, double m0, double G, double dt, int N, int Na, int coords,
+                      uint32_t* status) {
+    double eta = m0;
+#pragma unroll 1
+    for (int i = 1; i < N; i++) {
+        double e;
+        if (coords == 0) {
+            if (i < Na) eta += j.m[i];
+            e = eta;
+        } else if (coords == 2) {
+            e = i < Na ? m0 + j.m[i] : m0;
+        } else if (coords == 3) {
+            e = j.m[0];
+        } else {
+            e = m0;
+        }
+        wh::kepler_solver(j.x[i], j.y[i], j.z[i], j.vx[i], j.vy[i], j.vz[i], e * G, dt, status);
+    }
+}
+
+// reb_integrator_whfast_jump_step (:526-584); nothing in Jacobi or barycentric.
+template <int NB>
+__device__ void jump(wh::Jacobi<NB>& h, const wh::System<NB>& s, double dt, int N, int Na, int coords) {
+    if (coords == 1) { wh::jump_step_dh(h, s, dt, N, Na); return; }
+    if (coords != 2) return;
+    const double m0 = s.m[0];
+    double px = 0., py = 0., pz = 0.;
+#pragma unroll 1
+    for (int i = 1; i < Na; i++) {
+        const double m = s.m[i];
+        px += m * h.vx[i] / (m0 + m); py += m * h.vy[i] / (m0 + m); pz += m * h.vz[i] / (m0 + m);
+    }
+#pragma unroll 1
+    for (int i = 1; i < N; i++) {
+        if (i < Na) {
+            const double m = s.m[i];
+            h.x[i] += dt * (px - (m * h.vx[i] / (m0 + m)));
+            h.y[i] += dt * (py - (m * h.vy[i] / (m0 + m)));
+            h.z[i] += dt * (pz - (m * h.vz[i] / (m0 + m)));
+        } else {
+            h.x[i] += dt * px; h.y[i] += dt * py; h.z[i] += dt * pz;
+        }
+    }
+}
+
+// reb_integrator_whfast_interaction_step (:431-524) outside Jacobi coordinates.
+template <int NB>
+__device__ void kick_helio(wh::Jacobi<NB>& h, const wh::System<NB>& s, const double ax[NB], const double ay[NB],
+                           const double az[NB], double G, double dt, int N, int Na, int coords) {
+    const double m0 = s.m[0];
+#pragma unroll 1
+    for (int i = 1; i < N; i++) {
+        if (coords == 2 && i < Na) {
+            const double mi = s.m[i];
+            h.vx[i] += dt * (m0 + mi) * ax[i] / m0;
+            h.vy[i] += dt * (m0 + mi) * ay[i] / m0;
+            h.vz[i] += dt * (m0 + mi) * az[i] / m0;
+        } else if (coords == 3) {
+            const double dr = sqrt(h.x[i] * h.x[i] + h.y[i] * h.y[i] + h.z[i] * h.z[i]);
+            const double pf = G * h.m[0] / (dr * dr * dr);
+            h.vx[i] += dt * (pf * h.x[i] + ax[i]);
+            h.vy[i] += dt * (pf * h.y[i] + ay[i]);
+            h.vz[i] += dt * (pf * h.z[i] + az[i]);
+        } else {
+            h.vx[i] += dt * ax[i]; h.vy[i] += dt * ay[i]; h.vz[i] += dt * az[i];
+        }
+    }
+}
+
+// BASIC gravity for any gravity_ignore_terms (src/gravity.c:180-257): pairs from
+// starti (1, or 2 to skip the 0-1 pair) against startj (0, or 1 to skip body 0).
+template <int NB>
+__device__ void gravity_basic(const wh::System<NB>& s, double ax[NB], double ay[NB], double az[NB], double G,
+                              double eps2, int N, int Ng, int tp, int starti, int startj) {
+#pragma unroll 1
+    for (int i = 0; i < N; i++) { ax[i] = 0.; ay[i] = 0.; az[i] = 0.; }
+    const int st = Ng > starti ? Ng : starti;
+#pragma unroll 1
+    for (int i = starti; i < N; i++) {
+        const int jend = i < Ng ? i : Ng;
+#pragma unroll 1
+        for (int jj = startj; jj < jend; jj++) {
+            const double dx = (0. + s.x[i]) - s.x[jj];
+            const double dy = (0. + s.y[i]) - s.y[jj];
+            const double dz = (0. + s.z[i]) - s.z[jj];
+            const double r = sqrt(dx * dx + dy * dy + dz * dz + eps2);
+            const double pf = G / (r * r * r);
+            const double pfj = -pf * s.m[jj];
+            ax[i] += pfj * dx; ay[i] += pfj * dy; az[i] += pfj * dz;
+            if (i < st ? true : tp != 0) {
+                const double pfi = pf * s.m[i];
+                ax[jj] += pfi * dx; ay[jj] += pfi * dy; az[jj] += pfi * dz;
+            }
+        }
+    }
+}
+
+template <int NB>
+__global__ void __launch_bounds__(32) whfast_program(ParticlesSoA p, double* jac, size_t cap, int N, int Na, int Ng,
+                                                     int tp, int coords, double G, double eps2,
+                                                     const __grid_constant__ Program prog, uint32_t* status) {
     if (threadIdx.x != 0) return;
     wh::System<NB> s;
     wh::Jacobi<NB> j;
@@ -121,21 +313,36 @@ __global__ void __launch_bounds__(32) whfast_program(ParticlesSoA p, double* jac
         const bool on = i < N;
         ax[i] = on ? p.ax[i] : 0.; ay[i] = on ? p.ay[i] : 0.; az[i] = on ? p.az[i] : 0.;
     }
+    // gravity_ignore_terms of each coordinate system (:929-938)
+    const int starti = coords == 3 ? 1 : 2;
+    const int startj = (coords == 1 || coords == 2) ? 1 : 0;
 #pragma unroll 1
     for (int k = 0; k < prog.n; k++) {
         const double d = prog.d[k];
         const int op = prog.op[k];
         switch (op) {
-            case kOpFromInertial: wh::to_jacobi(s, j, N, Na); break;
-            case kOpDrift: wh::kepler_step(j, s.m[0], G, d, N, Na, status); break;
+            case kOpFromInertial:
+                if (coords == 0) wh::to_jacobi(s, j, N, Na);
+                else if (coords == 1) wh::to_dh(s, j, N, Na);
+                else if (coords == 2) to_whds(s, j, N, Na);
+                else to_bary(s, j, N, Na);
+                break;
+            case kOpDrift: drift(j, s.m[0], G, d, N, Na, coords, status); break;
             case kOpCom: wh::com_step(j, d); break;
-            case kOpToInertial: wh::to_inertial(s, j, N, Na); break;
-            case kOpGravity: wh::gravity_01(s, ax, ay, az, G, eps2, N, Na, tp); break;
+            case kOpToInertial:
+                if (coords == 0) wh::to_inertial(s, j, N, Na);
+                else if (coords == 1) wh::dh_to_inertial(s, j, N, Na);
+                else if (coords == 2) whds_to_inertial(s, j, N, Na);
+                else bary_to_inertial(s, j, N, Na);
+                break;
+            case kOpGravity: gravity_basic(s, ax, ay, az, G, eps2, N, Ng, tp, starti, startj); break;
             case kOpGravityJacobi: gravity_jacobi(s, ax, ay, az, G, N); break;
             case kOpKick:
             case kOpKickNoJacobiTerm:
-                wh::interaction_step(j, s, ax, ay, az, G, d, N, Na, op == kOpKick);
+                if (coords == 0) wh::interaction_step(j, s, ax, ay, az, G, d, N, Na, op == kOpKick);
+                else kick_helio(j, s, ax, ay, az, G, d, N, Na, coords);
                 break;
+            case kOpJump: jump(j, s, d, N, Na, coords); break;
             case kOpJerk: add_jerk(s, ax, ay, az, G, d, N); break;
             case kOpLazyShift:
 #pragma unroll 1
@@ -152,11 +359,12 @@ __global__ void __launch_bounds__(32) whfast_program(ParticlesSoA p, double* jac
     for (int i = 0; i < NB; i++) {
         if (i >= N) break;
         p.ax[i] = ax[i]; p.ay[i] = ay[i]; p.az[i] = az[i];
+        p.m[i] = s.m[i];                      // the barycentric transform rebuilds the star's mass
     }
 }
 
-typedef void (*ProgKernel)(ParticlesSoA, double*, size_t, int, int, int, double, double, const Program,
-                           uint32_t*);
+typedef void (*ProgKernel)(ParticlesSoA, double*, size_t, int, int, int, int, int, double, double,
+                           const Program, uint32_t*);
 
 ProgKernel kernel_for(int n) {
     switch (n) {
@@ -186,8 +394,8 @@ int wh_plain::launch_program(rgpu_sim* s, const Program& prog) {
     if (!k) return set_error(s, RGPU_ERR_UNSUPPORTED, "WHFast on the GPU supports 2..16 particles per simulation");
     const rgpu_config& c = s->cfg;
     ktimer_begin(s);
-    k<<<1, 32, 0, s->stream>>>(s->p, s->wh->jac, s->cap, N, (int)n_active(s), c.testparticle_type, c.G,
-                               c.softening * c.softening, prog, s->d_status);
+    k<<<1, 32, 0, s->stream>>>(s->p, s->wh->jac, s->cap, N, wh_active(s), (int)n_active(s), c.testparticle_type,
+                               c.whfast_coordinates, c.G, c.softening * c.softening, prog, s->d_status);
     ktimer_end(s);
     g_launches++;
     RGPU_CUDA(s, cudaGetLastError());

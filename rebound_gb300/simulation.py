@@ -27,7 +27,7 @@ class WHFastSettings:
     """rebound's ri_whfast on the GPU path: safe_mode, coordinates, correctors, kernel,
     keep_unsynchronized (src/integrator_whfast.h:28-50)."""
 
-    COORDINATES = {"jacobi": 0, "democraticheliocentric": 1}
+    COORDINATES = {"jacobi": 0, "democraticheliocentric": 1, "whds": 2, "barycentric": 3}
 
     def __init__(self, sim):
         self._sim = sim

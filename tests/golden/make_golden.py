@@ -588,9 +588,117 @@ def fixture_whfast_advanced():
     np.savez_compressed(os.path.join(HERE, "whfast_advanced.npz"), **out)
 
 
+def fixture_whfast_coords():
+    """WHFast in WHDS and barycentric coordinates and the test-particle scenarios of
+    rebound/tests/test_whfast_testparticles.py in all four coordinate systems: the
+    inputs the reference builds from orbital elements and the reference's own end
+    states."""
+    import math
+    out = {}
+    coords = ("jacobi", "democraticheliocentric", "whds", "barycentric")
+
+    def run(arr, coordinates, dt, safe=1, N_active=-1, tp_type=0, corrector=0):
+        sim = rebound.Simulation()
+        sim.testparticle_type = tp_type
+        load(sim, arr)
+        if N_active > 0:
+            sim.N_active = N_active
+        sim.integrator = "whfast"
+        sim.integrator.coordinates = coordinates
+        sim.integrator.safe_mode = safe
+        sim.integrator.corrector = corrector
+        sim.dt = dt
+        return sim
+
+    # WHDS outer solar system (rebound/tests/test_whfast.py:9-19)
+    sim = rebound.Simulation()
+    sim.add("outer solar system")
+    out["oss"] = state(sim)
+    sim = run(out["oss"], "whds", 0.005 * 12. * 2. * 3.1415)
+    e0 = sim.energy()
+    sim.integrate(1000. * 2. * 3.1415)
+    out["whds_oss_err"] = abs((e0 - sim.energy()) / sim.energy())
+    out["whds_oss_end"] = state(sim)
+    # two planets, 100 steps in each safe mode
+    sim = rebound.Simulation()
+    sim.add(m=1.)
+    sim.add(m=1e-3, a=1., e=.1)
+    sim.add(m=1e-3, a=3., e=0.1)
+    out["two"] = state(sim)
+    jupyr = 2. * math.pi
+    for c in ("whds", "barycentric"):
+        for safe in (1, 0):
+            sim = run(out["two"], c, 0.005123 * jupyr, safe)
+            sim.steps(100)
+            sim.synchronize()
+            out["two_%s_safe%d" % (c, safe)] = state(sim)
+    for order, safe, n in ((5, 0, 50), (17, 1, 10)):
+        sim = run(out["two"], "barycentric", 0.005123 * jupyr, safe, corrector=order)
+        sim.steps(n)
+        sim.synchronize()
+        out["two_barycentric_c%d" % order] = state(sim)
+    # test particles (rebound/tests/test_whfast_testparticles.py)
+    for N in (1, 2):
+        sim = rebound.Simulation()
+        sim.add(m=1)
+        for i in range(N):
+            sim.add(m=0, P=1, e=0.1, f=i)
+        out["tp_N%d" % N] = state(sim)
+        sim = rebound.Simulation()
+        sim.add(m=1)
+        sim.add(m=1e-3, P=0.4)
+        sim.add(m=1e-3, P=0.7)
+        for i in range(N):
+            sim.add(m=0, P=1, e=0.1, f=i)
+        out["tpp_N%d" % N] = state(sim)
+        sim = rebound.Simulation()
+        sim.add(m=1)
+        sim.add(m=1e-3, P=0.4)
+        for i in range(N):
+            sim.add(m=0, P=1, e=0.1, f=i)
+        out["mtp_N%d" % N] = state(sim)
+        for c in coords:
+            for na in [-1] + list(range(1, N + 2)):
+                sim = run(out["tp_N%d" % N], c, 1e-1, N_active=na)
+                sim.integrate(1)
+                out["tp_N%d_%s_na%d" % (N, c, na)] = state(sim)
+            for na in [-1] + list(range(3, N + 4)):
+                sim = run(out["tpp_N%d" % N], c, 1e-3, N_active=na)
+                sim.integrate(1)
+                out["tpp_N%d_%s_na%d" % (N, c, na)] = state(sim)
+            sim = run(out["mtp_N%d" % N], c, 1e-3)
+            sim.integrate(1)
+            out["mtp_N%d_%s_massless" % (N, c)] = state(sim)
+            heavy = out["mtp_N%d" % N].copy()
+            heavy["m"][2:] = 1.
+            sim = run(heavy, c, 1e-3, N_active=2)
+            sim.integrate(1)
+            out["mtp_N%d_%s_massive" % (N, c)] = state(sim)
+    sim = rebound.Simulation()
+    sim.add(m=1)
+    sim.add(m=1e-3, P=1, e=0.1)
+    out["tp1"] = state(sim)
+    sim = rebound.Simulation()
+    sim.add(m=1)
+    sim.add(m=1e-3, P=0.4)
+    sim.add(m=1e-3, P=0.7, e=0.1)
+    sim.add(m=1e-3, P=1.0)
+    out["tp1p"] = state(sim)
+    for c in coords:
+        for na in (-1, 1):
+            sim = run(out["tp1"], c, 1e-3, N_active=na, tp_type=1)
+            sim.integrate(1)
+            out["tp1_%s_na%d" % (c, na)] = state(sim)
+        for na in (-1, 3):
+            sim = run(out["tp1p"], c, 1e-3, N_active=na, tp_type=1)
+            sim.integrate(1)
+            out["tp1p_%s_na%d" % (c, na)] = state(sim)
+    np.savez_compressed(os.path.join(HERE, "whfast_coords.npz"), **out)
+
+
 if __name__ == "__main__":
     which = sys.argv[2:] or ["gravity_cases", "ring", "whfast", "sei", "gravity_plummer", "reference_cases",
-                             "leapfrog_orders", "whfast_dh", "whfast_advanced"]
+                             "leapfrog_orders", "whfast_dh", "whfast_advanced", "whfast_coords"]
     for w in which:
         print("generating", w, flush=True)
         globals()["fixture_" + w]() if w != "sei" else fixture_sei_periodic()

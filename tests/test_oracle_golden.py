@@ -180,3 +180,24 @@ def test_oracle_whfast_keep_unsynchronized(c):
     s.whfast(10)
     s.whfast_synchronize()
     assert max_diff(s.p, g["keep_end_c%d" % c]) == 0.0
+
+
+def coords_cases():
+    g = golden("whfast_coords.npz")
+    cases = []
+    for N in (1, 2):
+        cases += [("tp_N%d" % N, "tp_N%d_jacobi_na%d" % (N, na), 1e-1, na, 0) for na in [-1] + list(range(1, N + 2))]
+        cases += [("tpp_N%d" % N, "tpp_N%d_jacobi_na%d" % (N, na), 1e-3, na, 0) for na in [-1] + list(range(3, N + 4))]
+    cases += [("tp1", "tp1_jacobi_na%d" % na, 1e-3, na, 1) for na in (-1, 1)]
+    cases += [("tp1p", "tp1p_jacobi_na%d" % na, 1e-3, na, 1) for na in (-1, 3)]
+    return cases
+
+
+@pytest.mark.parametrize("start,end,dt,na,tp", coords_cases())
+def test_oracle_whfast_test_particles(start, end, dt, na, tp):
+    # rebound/tests/test_whfast_testparticles.py, Jacobi coordinates: the reference's
+    # own end states, bit for bit (N_active as WHFast reads it for testparticle_type 1)
+    g = golden("whfast_coords.npz")
+    s = O.Sim(g[start], dt=dt, N_active=None if na < 0 else na, testparticle_type=tp)
+    s.whfast_integrate(1.0)
+    assert max_diff(s.p, g[end]) == 0.0
