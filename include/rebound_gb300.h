@@ -83,7 +83,7 @@ typedef struct rgpu_config {
     int32_t status;            /* REB_STATUS_* value after a step (7 = collision halt) */
     int64_t collisions_log_n;  /* number of resolved hardsphere collisions */
     int32_t leapfrog_order;    /* 2 (default; 0 means 2), 4, 6 or 8: src/integrator_leapfrog.c:97-203 */
-    int32_t whfast_coordinates; /* 0 Jacobi (default), 1 democratic heliocentric (src/integrator_whfast.h) */
+    int32_t whfast_coordinates; /* 0 Jacobi (default), 1 democratic heliocentric, 2 WHDS, 3 barycentric (src/integrator_whfast.h:39-43) */
     /* src/integrator_whfast.h:29-47 (Jacobi coordinates only where not 0): */
     int32_t whfast_corrector;   /* first symplectic corrector order: 0 (off), 3, 5, 7, 11 or 17 */
     int32_t whfast_corrector2;  /* 1: second symplectic corrector */
