@@ -166,6 +166,30 @@ int rgpu_energy(rgpu_sim* sim, double* energy);
 /* Wait for the simulation's stream; returns the first device error, if any. */
 int rgpu_sim_sync(rgpu_sim* sim);
 
+/* ---- snapshots and archives (Simulationarchive counterpart) ------------ */
+/* A snapshot is the device-resident state as it is -- configuration, particles
+ * (not synchronized), WHFast coordinates and flags, dt_last_done, SEI cache,
+ * step count -- so that a handle restored from it continues bit for bit.
+ * Replaces reb_simulation_save_to_file / reb_simulation_create_from_simulationarchive
+ * (src/simulationarchive.c:410-470) for this path; the byte layout is this
+ * library's own (one record per snapshot, appended). */
+int rgpu_sim_snapshot_size(rgpu_sim* sim, size_t* bytes);
+int rgpu_sim_snapshot_write(rgpu_sim* sim, void* buf, size_t cap, size_t* written);
+int rgpu_sim_snapshot_read(rgpu_sim* sim, const void* buf, size_t n);
+/* interval = step = 0: append one snapshot now (reb_simulation_save_to_file);
+ * interval != 0: a snapshot whenever t passes the next multiple
+ * (reb_simulation_save_to_file_interval, src/simulationarchive.c:639-648);
+ * step != 0: every `step` steps (reb_simulation_save_to_file_step, :657-666).
+ * Automatic snapshots are taken before each step and at the end of
+ * rgpu_integrate, as reb_simulationarchive_heartbeat (:377-408).
+ * delete_file: remove the file first. */
+int rgpu_sim_save_to_file(rgpu_sim* sim, const char* path, double interval, int64_t step, int delete_file);
+/* Times and byte offsets of the whole snapshots in an archive (host only; a record
+ * cut short by an interrupted write ends the list).  n = number found. */
+int rgpu_archive_scan(const char* path, double* times, int64_t* offsets, size_t cap, size_t* n);
+/* Restore snapshot `index` (negative counts from the end). */
+int rgpu_sim_load_from_file(rgpu_sim* sim, const char* path, int64_t index);
+
 /* ---- measurement helpers ---------------------------------------------- */
 /* Average duration (ms) of the last launch of the dominant force kernel of
  * this handle, measured with CUDA events on the handle's stream. */

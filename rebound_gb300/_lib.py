@@ -91,6 +91,13 @@ SIGNATURES = {
     "rgpu_synchronize": (ctypes.c_int, [_P]),
     "rgpu_energy": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double)]),
     "rgpu_sim_sync": (ctypes.c_int, [_P]),
+    "rgpu_sim_snapshot_size": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_size_t)]),
+    "rgpu_sim_snapshot_write": (ctypes.c_int, [_P, _P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+    "rgpu_sim_snapshot_read": (ctypes.c_int, [_P, _P, ctypes.c_size_t]),
+    "rgpu_sim_save_to_file": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_double, ctypes.c_int64, ctypes.c_int]),
+    "rgpu_archive_scan": (ctypes.c_int, [ctypes.c_char_p, _P, _P, ctypes.c_size_t,
+                                         ctypes.POINTER(ctypes.c_size_t)]),
+    "rgpu_sim_load_from_file": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_int64]),
     "rgpu_sim_last_kernel_ms": (ctypes.c_double, [_P]),
     "rgpu_launch_count": (ctypes.c_int64, []),
     "rgpu_sim_kernel_timer": (ctypes.c_int, [_P, ctypes.c_int]),

@@ -56,6 +56,10 @@ struct rgpu_sim {
     bool did_modify = true;
     bool whfast_synchronized = true;
     double dt_last_done = 0.;          // dt of the last completed step (src/rebound.h: dt_last_done)
+    int64_t steps_done = 0;            // src/rebound.h: steps_done
+    std::string archive_path;          // automatic snapshots (src/rebound.h: simulationarchive_*)
+    double archive_interval = 0., archive_next = 0.;
+    int64_t archive_step = 0, archive_next_step = 0;
     SeiCache sei{};
     // last collision search result (device), consumed by the resolve stage
     size_t n_pairs = 0;
@@ -95,6 +99,9 @@ void collide_free(rgpu_sim* s);
 int whfast_step(rgpu_sim* s);
 int whfast_synchronize(rgpu_sim* s);
 void whfast_free(rgpu_sim* s);
+int whfast_load_coordinates(rgpu_sim* s, const double* host7N);   // 7 N doubles, field-major
+// snapshot.cu
+int archive_heartbeat(rgpu_sim* s);
 // step.cu
 int boundary_check(rgpu_sim* s);
 void ghostbox(const rgpu_config& c, int i, int j, int k, double gb[6]);

@@ -538,6 +538,7 @@ int rgpu_collision_search(rgpu_sim* s, rgpu_collision* out, size_t cap, size_t* 
 int rgpu_steps(rgpu_sim* s, int64_t n) {
     if (!s || n < 0) return RGPU_ERR_ARG;
     for (int64_t k = 0; k < n; k++) {
+        RGPU_TRY(archive_heartbeat(s));                  // src/simulation.c:507-508
         switch (s->cfg.integrator) {
             case RGPU_INTEGRATOR_LEAPFROG: RGPU_TRY(leapfrog_step(s)); break;
             case RGPU_INTEGRATOR_SEI: RGPU_TRY(sei_step(s, s->sei)); break;
@@ -546,6 +547,7 @@ int rgpu_steps(rgpu_sim* s, int64_t n) {
         }
         s->did_modify = false;
         s->dt_last_done = s->cfg.dt;
+        s->steps_done++;
         RGPU_TRY(boundary_check(s));
         if (s->cfg.collision != RGPU_COLLISION_NONE) {
             size_t nf = 0;
@@ -605,6 +607,7 @@ int rgpu_integrate(rgpu_sim* s, double tmax) {
     }
     RGPU_TRY(synchronize_state(s));
     if (c.exact_finish_time) c.dt = last_full_dt;
+    RGPU_TRY(archive_heartbeat(s));                      // :459
     return read_status(s);
 }
 

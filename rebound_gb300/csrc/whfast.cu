@@ -329,6 +329,14 @@ int whfast_synchronize(rgpu_sim* s) {
     return RGPU_OK;
 }
 
+int whfast_load_coordinates(rgpu_sim* s, const double* host7N) {
+    RGPU_TRY(ensure_jac(s));
+    for (int f = 0; f < 7; f++)
+        RGPU_CUDA(s, cudaMemcpyAsync(s->wh->jac + f * s->wh->cap, host7N + f * s->N, sizeof(double) * s->N,
+                                     cudaMemcpyHostToDevice, s->stream));
+    return RGPU_OK;
+}
+
 void whfast_free(rgpu_sim* s) {
     if (!s->wh) return;
     cudaFree(s->wh->jac);

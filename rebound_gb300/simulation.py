@@ -287,6 +287,27 @@ class Simulation:
     def last_kernel_ms(self):
         return self._L.rgpu_sim_last_kernel_ms(self._h)
 
+    # ---- snapshots (Simulationarchive counterpart) --------------------------
+    def save_to_file(self, filename, interval=None, step=None, delete_file=False):
+        """rebound's Simulation.save_to_file (rebound/simulation.py:1166): one snapshot
+        now, or automatic snapshots every `interval` of time / every `step` steps
+        during later steps and integrations.  Snapshots keep the unsynchronized
+        integrator state, so a run restarted from one continues bit for bit."""
+        self._push()
+        check(self._L.rgpu_sim_save_to_file(self._h, str(filename).encode(), float(interval or 0.),
+                                            int(step or 0), int(bool(delete_file))), self._h)
+
+    @classmethod
+    def from_file(cls, filename, index=-1):
+        """A new simulation restored from snapshot `index` of an archive file."""
+        sim = cls()
+        check(sim._L.rgpu_sim_load_from_file(sim._h, str(filename).encode(), int(index)), sim._h)
+        check(sim._L.rgpu_sim_get_config(sim._h, ctypes.byref(sim._cfg)))
+        sim._host = np.zeros(sim._L.rgpu_sim_N(sim._h), dtype=PARTICLE_DTYPE)
+        sim._host_dirty = False
+        sim._device_newer = True
+        return sim
+
     @property
     def handle(self):
         self._push()
@@ -296,3 +317,74 @@ class Simulation:
 def accelerations(sim):
     p = sim.particles
     return np.stack([p["ax"], p["ay"], p["az"]], axis=1)
+
+
+class Simulationarchive:
+    """rebound's Simulationarchive (rebound/simulationarchive.py) over an archive
+    written by Simulation.save_to_file: len(), indexing (a new Simulation per
+    snapshot), tmin / tmax and getSimulation(t, mode)."""
+
+    def __init__(self, filename):
+        self.filename = str(filename)
+        L = _lib.load()
+        n = ctypes.c_size_t(0)
+        rc = L.rgpu_archive_scan(self.filename.encode(), None, None, 0, ctypes.byref(n))
+        if rc not in (0, 9):
+            raise _lib.RGPUError(rc, "cannot read archive " + self.filename)
+        self.t = np.zeros(n.value)
+        self.offsets = np.zeros(n.value, dtype=np.int64)
+        if n.value:
+            check(L.rgpu_archive_scan(self.filename.encode(), self.t.ctypes.data, self.offsets.ctypes.data,
+                                      n.value, ctypes.byref(n)))
+
+    def __len__(self):
+        return len(self.t)
+
+    def __getitem__(self, key):
+        if not isinstance(key, (int, np.integer)):
+            raise AttributeError("Must access individual simulations with integer index.")
+        if key < 0:
+            key += len(self)
+        if key >= len(self) or key < 0:
+            raise IndexError("Index out of range, number of snapshots stored in binary: %d." % len(self))
+        return Simulation.from_file(self.filename, int(key))
+
+    @property
+    def tmin(self):
+        return float(self.t[0])
+
+    @property
+    def tmax(self):
+        return float(self.t[-1])
+
+    def _snapshot_index(self, t):
+        """Index of the last snapshot at or before t (rebound/simulationarchive.py:159-177)."""
+        if t > self.tmax or t < self.tmin:
+            raise ValueError("Requested time outside of baseline stored in binary file.")
+        lo, hi = 0, len(self)
+        while True:
+            bi = lo + (hi - lo) // 2
+            if self.t[bi] > t:
+                hi = bi
+            else:
+                lo = bi
+            if hi - 1 <= lo:
+                return lo
+
+    def getSimulation(self, t, mode="snapshot", keep_unsynchronized=1):
+        """rebound/simulationarchive.py:179-241: the snapshot before t, integrated to
+        t ('exact'), past it by at most one step ('close'), or as stored ('snapshot')."""
+        if mode not in ("snapshot", "close", "exact"):
+            raise AttributeError("Unknown mode.")
+        sim = self[self._snapshot_index(t)]
+        if sim.integrator == "whfast":
+            if sim.ri_whfast.safe_mode == 1 or mode == "exact":
+                keep_unsynchronized = 0
+            sim.ri_whfast.keep_unsynchronized = keep_unsynchronized
+        if mode == "snapshot":
+            sim.synchronize()
+        elif mode == "close":
+            sim.integrate(t, exact_finish_time=0)
+        else:
+            sim.integrate(t, exact_finish_time=1)
+        return sim

@@ -696,9 +696,36 @@ def fixture_whfast_coords():
     np.savez_compressed(os.path.join(HERE, "whfast_coords.npz"), **out)
 
 
+def fixture_archive_cases():
+    """Restart scenarios of rebound/tests/test_simulationarchive.py:86-365: the
+    three-body input the reference builds from orbital elements and the reference's
+    own state at t = 80 (exact_finish_time = 0) for each integrator setting."""
+    out = {}
+    sim = rebound.Simulation()
+    sim.add(m=1)
+    sim.add(m=1e-3, a=1, e=0.1, omega=0.1, M=0.1, inc=0.1, Omega=0.1)
+    sim.add(m=1e-3, a=-2, e=1.1, omega=0.1, M=0.1, inc=0.1, Omega=0.1)
+    out["start"] = state(sim)
+    for coords in ("jacobi", "democraticheliocentric", "whds"):
+        for safe in (0, 1):
+            for corrector in ((0, 5) if coords == "jacobi" else (0,)):
+                sim = rebound.Simulation()
+                load(sim, out["start"])
+                sim.integrator = "whfast"
+                sim.integrator.coordinates = coords
+                sim.integrator.corrector = corrector
+                sim.dt = 0.1313
+                sim.integrator.safe_mode = safe
+                sim.integrate(80., exact_finish_time=0)
+                out["end_%s_safe%d_c%d" % (coords, safe, corrector)] = state(sim)
+                out["t_%s_safe%d_c%d" % (coords, safe, corrector)] = sim.t
+    np.savez_compressed(os.path.join(HERE, "archive_cases.npz"), **out)
+
+
 if __name__ == "__main__":
     which = sys.argv[2:] or ["gravity_cases", "ring", "whfast", "sei", "gravity_plummer", "reference_cases",
-                             "leapfrog_orders", "whfast_dh", "whfast_advanced", "whfast_coords"]
+                             "leapfrog_orders", "whfast_dh", "whfast_advanced", "whfast_coords",
+                             "archive_cases"]
     for w in which:
         print("generating", w, flush=True)
         globals()["fixture_" + w]() if w != "sei" else fixture_sei_periodic()
