@@ -49,8 +49,10 @@ def test_plummer_generator_matches_reference_draws():
     g = golden("gravity_plummer.npz")
     p = R.ics.plummer(4096, seed=int(g["plummer_seed"]))
     ref = g["particles"]
+    # host libm (pow, sin, cos) may differ by an ulp between machines; the draw
+    # sequence itself must match, so the bar is a few ulps of the largest value
     for f in ("x", "y", "z", "vx", "vy", "vz", "m"):
-        np.testing.assert_allclose(p[f], ref[f], rtol=1e-14, atol=1e-15)
+        np.testing.assert_allclose(p[f], ref[f], rtol=1e-14, atol=1e-14)
     raw = R.ics.plummer(64, seed=int(g["plummer_seed"]), rmax=1e300)
     for f in ("x", "y", "z", "vx", "vy", "vz"):
         np.testing.assert_allclose(raw[f], g["plummer_raw"][f], rtol=1e-14, atol=1e-15)
