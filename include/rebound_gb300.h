@@ -52,7 +52,8 @@ enum { RGPU_GRAVITY_NONE = 0, RGPU_GRAVITY_BASIC = 1, RGPU_GRAVITY_COMPENSATED =
         * provably never opened and its monopole is summed by a tiled sweep in
         * mixed precision (FP64 displacement via two-float splits, FP32 force). */
        RGPU_GRAVITY_TREE_SPLIT = 66 };
-enum { RGPU_COLLISION_NONE = 0, RGPU_COLLISION_DIRECT = 1, RGPU_COLLISION_TREE = 2 };
+enum { RGPU_COLLISION_NONE = 0, RGPU_COLLISION_DIRECT = 1, RGPU_COLLISION_TREE = 2,
+       RGPU_COLLISION_LINE = 4, RGPU_COLLISION_LINETREE = 5 };   /* paths over the last step */
 enum { RGPU_BOUNDARY_NONE = 0, RGPU_BOUNDARY_OPEN = 1, RGPU_BOUNDARY_PERIODIC = 2, RGPU_BOUNDARY_SHEAR = 3 };
 enum { RGPU_INTEGRATOR_LEAPFROG = 0, RGPU_INTEGRATOR_SEI = 1, RGPU_INTEGRATOR_WHFAST = 2 };
 enum { RGPU_RESOLVE_HALT = 0, RGPU_RESOLVE_HARDSPHERE = 1, RGPU_RESOLVE_NONE = 2 };

@@ -28,7 +28,7 @@ ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: 
           8: "tree too deep", 9: "output overflow", 10: "capacity exceeded", 11: "timeout"}
 
 GRAVITY = {"none": 0, "basic": 1, "compensated": 2, "tree": 3, "mixed": 64, "mixed_split": 65, "tree_split": 66}
-COLLISION = {"none": 0, "direct": 1, "tree": 2}
+COLLISION = {"none": 0, "direct": 1, "tree": 2, "line": 4, "linetree": 5}
 BOUNDARY = {"none": 0, "open": 1, "periodic": 2, "shear": 3}
 INTEGRATOR = {"leapfrog": 0, "sei": 1, "whfast": 2}
 RESOLVE = {"halt": 0, "hardsphere": 1, "none": 2}

@@ -1,4 +1,4 @@
-// Direct collision search (src/collision.c:64-124) and the post-search stage of
+// Direct collision search (src/collision.c:64-124), the LINE search (:125-196), and the post-search stage of
 // reb_collision_search (src/collision.c:336-404): the rand_r shuffle of the pair
 // list and the sequential resolve, hardsphere (src/collision.c:573-665) or halt.
 //
@@ -24,21 +24,38 @@ struct Ring {
     double off[27][6];
 };
 
-__device__ __forceinline__ int direct_pairs_one(int g, int i, const Ring& ring, ParticlesSoA p, int N,
+// LINE = true: the LINE search (src/collision.c:125-196): pairs j > i whose straight
+// paths over the last step (dt_last_done) come within the sum of the radii.
+template <bool LINE>
+__device__ __forceinline__ int direct_pairs_one(int g, int i, const Ring& ring, ParticlesSoA p, int N, double dtl,
                                                 rgpu_collision* out, long long base) {
     const double* gb = ring.off[g];
     const double sx = gb[0] + p.x[i], sy = gb[1] + p.y[i], sz = gb[2] + p.z[i];
     const double svx = gb[3] + p.vx[i], svy = gb[4] + p.vy[i], svz = gb[5] + p.vz[i];
     const double r1 = p.r[i];
     int found = 0;
-    for (int j = 0; j < N; j++) {
-        if (i == j) continue;
+    for (int j = LINE ? i + 1 : 0; j < N; j++) {
+        if (!LINE && i == j) continue;
         const double dx = sx - p.x[j], dy = sy - p.y[j], dz = sz - p.z[j];
-        const double sr = r1 + p.r[j];
         const double r2 = dx * dx + dy * dy + dz * dz;
-        if (r2 > sr * sr) continue;
         const double dvx = svx - p.vx[j], dvy = svy - p.vy[j], dvz = svz - p.vz[j];
-        if (dvx * dx + dvy * dy + dvz * dz > 0) continue;
+        if (LINE) {
+            const double dx2 = dx - dtl * dvx, dy2 = dy - dtl * dvy, dz2 = dz - dtl * dvz;   // at the start
+            const double r2b = dx2 * dx2 + dy2 * dy2 + dz2 * dz2;
+            const double tc = (dx * dvx + dy * dvy + dz * dvz) / (dvx * dvx + dvy * dvy + dvz * dvz);
+            double rmin2 = r2 < r2b ? r2 : r2b;
+            if (tc / dtl >= 0. && tc / dtl <= 1.) {
+                const double dx3 = dx - tc * dvx, dy3 = dy - tc * dvy, dz3 = dz - tc * dvz;  // closest approach
+                const double r3 = dx3 * dx3 + dy3 * dy3 + dz3 * dz3;
+                rmin2 = rmin2 < r3 ? rmin2 : r3;
+            }
+            const double rsum = r1 + p.r[j];
+            if (rmin2 > rsum * rsum) continue;
+        } else {
+            const double sr = r1 + p.r[j];
+            if (r2 > sr * sr) continue;
+            if (dvx * dx + dvy * dy + dvz * dz > 0) continue;
+        }
         if (out) {
             rgpu_collision& o = out[base + found];
             o.p1 = (size_t)i; o.p2 = (size_t)j; o.ri = 0;
@@ -49,18 +66,20 @@ __device__ __forceinline__ int direct_pairs_one(int g, int i, const Ring& ring, 
     return found;
 }
 
-__global__ void direct_count(Ring ring, ParticlesSoA p, int N, int* count) {
+template <bool LINE>
+__global__ void direct_count(Ring ring, ParticlesSoA p, int N, double dtl, int* count) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= (long long)ring.n * N) return;
     const int g = (int)(t / N), i = (int)(t % N);
-    count[t] = direct_pairs_one(g, i, ring, p, N, nullptr, 0);
+    count[t] = direct_pairs_one<LINE>(g, i, ring, p, N, dtl, nullptr, 0);
 }
 
-__global__ void direct_write(Ring ring, ParticlesSoA p, int N, const long long* off, rgpu_collision* out) {
+template <bool LINE>
+__global__ void direct_write(Ring ring, ParticlesSoA p, int N, double dtl, const long long* off, rgpu_collision* out) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= (long long)ring.n * N) return;
     const int g = (int)(t / N), i = (int)(t % N);
-    direct_pairs_one(g, i, ring, p, N, out, off[t]);
+    direct_pairs_one<LINE>(g, i, ring, p, N, dtl, out, off[t]);
 }
 
 __global__ void scan_counts(const int* __restrict__ cnt, long long n, long long* __restrict__ off) {
@@ -135,7 +154,7 @@ void hardsphere(Body& p1, Body& p2, const double gb[6], double eps, double minve
 
 }  // namespace
 
-int direct_collisions(rgpu_sim* s, rgpu_collision* out, size_t cap, size_t* n_found, bool device_only) {
+int direct_collisions(rgpu_sim* s, rgpu_collision* out, size_t cap, size_t* n_found, bool device_only, bool line) {
     const int N = (int)s->N;
     *n_found = 0;
     s->n_pairs = 0;
@@ -157,7 +176,9 @@ int direct_collisions(rgpu_sim* s, rgpu_collision* out, size_t cap, size_t* n_fo
         s->pc_cap = (size_t)nt;
     }
     const unsigned grid = (unsigned)((nt + kB - 1) / kB);
-    direct_count<<<grid, kB, 0, s->stream>>>(ring, s->p, N, s->pc_count);
+    const double dtl = s->dt_last_done;
+    if (line) direct_count<true><<<grid, kB, 0, s->stream>>>(ring, s->p, N, dtl, s->pc_count);
+    else direct_count<false><<<grid, kB, 0, s->stream>>>(ring, s->p, N, dtl, s->pc_count);
     scan_counts<<<1, 256, 0, s->stream>>>(s->pc_count, nt, s->pc_off);
     g_launches += 2;
     long long total = 0;
@@ -172,7 +193,8 @@ int direct_collisions(rgpu_sim* s, rgpu_collision* out, size_t cap, size_t* n_fo
         s->dp_cap = want;
     }
     if (total) {
-        direct_write<<<grid, kB, 0, s->stream>>>(ring, s->p, N, s->pc_off, s->dp_pairs);
+        if (line) direct_write<true><<<grid, kB, 0, s->stream>>>(ring, s->p, N, dtl, s->pc_off, s->dp_pairs);
+        else direct_write<false><<<grid, kB, 0, s->stream>>>(ring, s->p, N, dtl, s->pc_off, s->dp_pairs);
         g_launches++;
     }
     *n_found = (size_t)total;

@@ -89,10 +89,12 @@ int direct_accel(rgpu_sim* s, int mode);
 int direct_energy(rgpu_sim* s, double* e);
 // tree.cu
 int tree_accel(rgpu_sim* s);
-int tree_collisions(rgpu_sim* s, rgpu_collision* out, size_t cap, size_t* n_found, bool device_only);
+int tree_collisions(rgpu_sim* s, rgpu_collision* out, size_t cap, size_t* n_found, bool device_only,
+                    bool line = false);
 void tree_free(rgpu_sim* s);
 // collide.cu
-int direct_collisions(rgpu_sim* s, rgpu_collision* out, size_t cap, size_t* n_found, bool device_only);
+int direct_collisions(rgpu_sim* s, rgpu_collision* out, size_t cap, size_t* n_found, bool device_only,
+                      bool line = false);
 int resolve_collisions_device(rgpu_sim* s);
 void collide_free(rgpu_sim* s);
 // whfast.cu

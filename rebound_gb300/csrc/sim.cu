@@ -466,7 +466,8 @@ const char* rgpu_sim_last_error(const rgpu_sim* s) { return s ? s->msg.c_str() :
 
 int rgpu_sim_configure(rgpu_sim* s, const rgpu_config* c) {
     if (!s || !c) return RGPU_ERR_ARG;
-    if (c->gravity == RGPU_GRAVITY_TREE || c->gravity == RGPU_GRAVITY_TREE_SPLIT || c->collision == RGPU_COLLISION_TREE) {
+    if (c->gravity == RGPU_GRAVITY_TREE || c->gravity == RGPU_GRAVITY_TREE_SPLIT || c->collision == RGPU_COLLISION_TREE ||
+        c->collision == RGPU_COLLISION_LINETREE) {
         if (c->root_size <= 0.0)
             return set_error(s, RGPU_ERR_ARG, "Set root_size to a finite value to use a tree based gravity or collision solver.");
     }
@@ -531,6 +532,8 @@ int rgpu_collision_search(rgpu_sim* s, rgpu_collision* out, size_t cap, size_t* 
         case RGPU_COLLISION_NONE: return RGPU_OK;
         case RGPU_COLLISION_DIRECT: return direct_collisions(s, out, cap, n_found, false);
         case RGPU_COLLISION_TREE: return tree_collisions(s, out, cap, n_found, false);
+        case RGPU_COLLISION_LINE: return direct_collisions(s, out, cap, n_found, false, true);
+        case RGPU_COLLISION_LINETREE: return tree_collisions(s, out, cap, n_found, false, true);
         default: return set_error(s, RGPU_ERR_UNSUPPORTED, "Collision routine not implemented.");
     }
 }
@@ -551,8 +554,13 @@ int rgpu_steps(rgpu_sim* s, int64_t n) {
         RGPU_TRY(boundary_check(s));
         if (s->cfg.collision != RGPU_COLLISION_NONE) {
             size_t nf = 0;
-            if (s->cfg.collision == RGPU_COLLISION_DIRECT) RGPU_TRY(direct_collisions(s, nullptr, 0, &nf, true));
-            else RGPU_TRY(tree_collisions(s, nullptr, 0, &nf, true));
+            switch (s->cfg.collision) {
+                case RGPU_COLLISION_DIRECT: RGPU_TRY(direct_collisions(s, nullptr, 0, &nf, true)); break;
+                case RGPU_COLLISION_TREE: RGPU_TRY(tree_collisions(s, nullptr, 0, &nf, true)); break;
+                case RGPU_COLLISION_LINE: RGPU_TRY(direct_collisions(s, nullptr, 0, &nf, true, true)); break;
+                case RGPU_COLLISION_LINETREE: RGPU_TRY(tree_collisions(s, nullptr, 0, &nf, true, true)); break;
+                default: return set_error(s, RGPU_ERR_UNSUPPORTED, "Collision routine not implemented.");
+            }
             RGPU_TRY(resolve_collisions_device(s));
             if (s->cfg.status == 7) break;   // REB_STATUS_COLLISION from the halt resolver
         }

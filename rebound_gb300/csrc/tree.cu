@@ -51,7 +51,7 @@ struct TreeBuffers {
     long long* pair_off = nullptr;
     rgpu_collision* pairs = nullptr;
     size_t pairs_cap = 0;
-    double* r_top = nullptr;        // per-block top-2 radii
+    double* r_top = nullptr;        // per-block top-2 radii, then the largest squared speed
     void* sweep = nullptr;          // split mode: per-root monopole records
     size_t sweep_cap = 0;
 };
@@ -500,21 +500,40 @@ __global__ void __launch_bounds__(kSweepTile) sweep_far(ParticlesSoA p, int N, c
 // Roots farther than the search radius from the shifted particle cannot pass the
 // descent test r < r1 + r2nd + (sqrt(3)/2) w, so each particle scans only the
 // window of root boxes around it (index order preserved, same pair set and order).
+// LINE = true: the LINETREE search (src/collision.c:270-330, 506-572), which tests
+// the straight paths of the last step (dt_last_done) instead of the overlap now and
+// descends while r < r1 + dt |v1| + maxdrift + (sqrt(3)/2) w.
+template <bool LINE>
 __device__ __forceinline__ int tree_pairs_one(int i, ParticlesSoA p, CellArrays c, BoxGeom g,
                                               const GhostArr* __restrict__ gh, int nring, double r2nd, double rmax,
-                                              rgpu_collision* out, long long base, int* stack,
-                                              uint32_t* status) {
+                                              double dtl, double vmax2, rgpu_collision* out, long long base,
+                                              int* stack, uint32_t* status) {
     const double p1x = p.x[i], p1y = p.y[i], p1z = p.z[i];
     const double p1vx = p.vx[i], p1vy = p.vy[i], p1vz = p.vz[i], p1r = p.r[i];
-    // A root can only contribute if its cell is within max(r1 + r_max, r1 + r2nd +
-    // (sqrt(3)/2) w) of the shifted particle (leaf roots are tested directly).
-    const double reach = p1r + fmax(rmax, r2nd + 0.8660254037844387 * g.root_size);
-    const int K = (int)ceil(reach / g.root_size) + 2;
+    double maxdrift = 0., p1r_dtv = 0.;
+    if (LINE) {
+        maxdrift = dtl * sqrt(vmax2);
+        p1r_dtv = p1r + dtl * sqrt(p1vx * p1vx + p1vy * p1vy + p1vz * p1vz);
+    }
     int found = 0;
     for (int g0 = 0; g0 < nring; g0++) {
         const double* gb = gh->off[g0];
         const double sx = gb[0] + p1x, sy = gb[1] + p1y, sz = gb[2] + p1z;
         const double svx = gb[3] + p1vx, svy = gb[4] + p1vy, svz = gb[5] + p1vz;
+        // A root can only contribute if its cell centre is within the descent radius
+        // of the shifted particle or, for a one-particle root, if that particle can
+        // pass the pair test (for LINE: the end-of-step distance is at most the
+        // radii plus the relative path length |dt| (|v1 + v_gb| + v_max)).
+        double reach;
+        if (LINE) {
+            const double adt = fabs(dtl);
+            const double desc = fabs(p1r_dtv) + fabs(maxdrift) + 0.8660254037844387 * g.root_size;
+            const double leaf = p1r + rmax + adt * (sqrt(svx * svx + svy * svy + svz * svz) + sqrt(vmax2));
+            reach = fmax(desc, leaf) * (1. + 1e-12);
+        } else {
+            reach = p1r + fmax(rmax, r2nd + 0.8660254037844387 * g.root_size);
+        }
+        const int K = (int)ceil(reach / g.root_size) + 2;
         const int ixv = (int)floor((sx + g.bx / 2.) / g.root_size);
         const int iyv = (int)floor((sy + g.by / 2.) / g.root_size);
         const int izv = (int)floor((sz + g.bz / 2.) / g.root_size);
@@ -535,10 +554,24 @@ __device__ __forceinline__ int tree_pairs_one(int i, ParticlesSoA p, CellArrays 
                     if (pt == i) continue;
                     const double dx = sx - p.x[pt], dy = sy - p.y[pt], dz = sz - p.z[pt];
                     const double r2 = dx * dx + dy * dy + dz * dz;
-                    const double rp = p1r + p.r[pt];
-                    if (r2 > rp * rp) continue;
                     const double dvx = svx - p.vx[pt], dvy = svy - p.vy[pt], dvz = svz - p.vz[pt];
-                    if (dvx * dx + dvy * dy + dvz * dz > 0) continue;
+                    if (LINE) {
+                        const double dx2 = dx - dtl * dvx, dy2 = dy - dtl * dvy, dz2 = dz - dtl * dvz;
+                        const double r2b = dx2 * dx2 + dy2 * dy2 + dz2 * dz2;
+                        const double tc = (dx * dvx + dy * dvy + dz * dvz) / (dvx * dvx + dvy * dvy + dvz * dvz);
+                        double rmin2 = r2 < r2b ? r2 : r2b;
+                        if (tc / dtl >= 0. && tc / dtl <= 1.) {
+                            const double dx3 = dx - tc * dvx, dy3 = dy - tc * dvy, dz3 = dz - tc * dvz;
+                            const double r3 = dx3 * dx3 + dy3 * dy3 + dz3 * dz3;
+                            rmin2 = rmin2 < r3 ? rmin2 : r3;
+                        }
+                        const double rsum = p1r + p.r[pt];
+                        if (rmin2 > rsum * rsum) continue;
+                    } else {
+                        const double rp = p1r + p.r[pt];
+                        if (r2 > rp * rp) continue;
+                        if (dvx * dx + dvy * dy + dvz * dz > 0) continue;
+                    }
                     if (out) {
                         rgpu_collision& o = out[base + found];
                         o.p1 = (size_t)i; o.p2 = (size_t)pt; o.ri = (size_t)r;
@@ -548,7 +581,8 @@ __device__ __forceinline__ int tree_pairs_one(int i, ParticlesSoA p, CellArrays 
                 } else {
                     const double dx = sx - c.x[q], dy = sy - c.y[q], dz = sz - c.z[q];
                     const double r2 = dx * dx + dy * dy + dz * dz;
-                    const double rp = p1r + r2nd + 0.86602540378443 * c.w[q];
+                    const double rp = LINE ? p1r_dtv + maxdrift + 0.86602540378443 * c.w[q]
+                                           : p1r + r2nd + 0.86602540378443 * c.w[q];
                     if (r2 < rp * rp) {
                         const int f = c.first[q], n = c.nchild[q];
                         if (sp + n > kStack) { atomicOr(status, DEV_ERR_STACK); return found; }
@@ -561,22 +595,46 @@ __device__ __forceinline__ int tree_pairs_one(int i, ParticlesSoA p, CellArrays 
     return found;
 }
 
+// Largest squared speed of the particles (src/collision.c:273-277), as the bits of
+// a non-negative double so that an integer atomicMax orders them.
+__global__ void max_speed2(ParticlesSoA p, int N, unsigned long long* out) {
+    __shared__ double part[kB];
+    double l = 0.;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        const double v2 = p.vx[i] * p.vx[i] + p.vy[i] * p.vy[i] + p.vz[i] * p.vz[i];
+        l = l > v2 ? l : v2;
+    }
+    part[threadIdx.x] = l;
+    __syncthreads();
+    for (int w = kB / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) part[threadIdx.x] = fmax(part[threadIdx.x], part[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicMax(out, (unsigned long long)__double_as_longlong(part[0]));
+}
+
+template <bool LINE>
 __global__ void __launch_bounds__(128) tree_pairs_count(ParticlesSoA p, int N, CellArrays c, BoxGeom g,
                                                         const GhostArr* __restrict__ gh, int nring, const double* r2nd,
-                                                        int* count, uint32_t* status) {
+                                                        double dtl, const unsigned long long* vmax2, int* count,
+                                                        uint32_t* status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     int stack[kStack];
-    count[i] = tree_pairs_one(i, p, c, g, gh, nring, r2nd[0], r2nd[1], nullptr, 0, stack, status);
+    count[i] = tree_pairs_one<LINE>(i, p, c, g, gh, nring, r2nd[0], r2nd[1], dtl,
+                                    LINE ? __longlong_as_double((long long)*vmax2) : 0., nullptr, 0, stack, status);
 }
 
+template <bool LINE>
 __global__ void __launch_bounds__(128) tree_pairs_write(ParticlesSoA p, int N, CellArrays c, BoxGeom g,
                                                         const GhostArr* __restrict__ gh, int nring, const double* r2nd,
+                                                        double dtl, const unsigned long long* vmax2,
                                                         const long long* off, rgpu_collision* out, uint32_t* status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     int stack[kStack];
-    tree_pairs_one(i, p, c, g, gh, nring, r2nd[0], r2nd[1], out, off[i], stack, status);
+    tree_pairs_one<LINE>(i, p, c, g, gh, nring, r2nd[0], r2nd[1], dtl,
+                         LINE ? __longlong_as_double((long long)*vmax2) : 0., out, off[i], stack, status);
 }
 
 // Second-largest radius (src/simulation.c:718-800): the second element of the
@@ -680,7 +738,7 @@ int ensure_tree(rgpu_sim* s) {
         t->cap = s->cap;
     }
     if (!t->counter) RGPU_CUDA(s, cudaMalloc(&t->counter, sizeof(int)));
-    if (!t->r_top) RGPU_CUDA(s, cudaMalloc(&t->r_top, sizeof(double) * 2 * 1024));
+    if (!t->r_top) RGPU_CUDA(s, cudaMalloc(&t->r_top, sizeof(double) * (2 * 1024 + 1)));   // + max speed^2
     return RGPU_OK;
 }
 
@@ -841,7 +899,7 @@ int tree_accel(rgpu_sim* s) {
     return RGPU_OK;
 }
 
-int tree_collisions(rgpu_sim* s, rgpu_collision* out, size_t cap, size_t* n_found, bool device_only) {
+int tree_collisions(rgpu_sim* s, rgpu_collision* out, size_t cap, size_t* n_found, bool device_only, bool line) {
     const int N = (int)s->N;
     *n_found = 0;
     if (!N) return RGPU_OK;
@@ -860,8 +918,19 @@ int tree_collisions(rgpu_sim* s, rgpu_collision* out, size_t cap, size_t* n_foun
     top2_radii<<<nb, kB, 0, s->stream>>>(s->p.r, N, t->r_top);
     top2_final<<<1, 1, 0, s->stream>>>(t->r_top, nb, N);
     CellArrays c = arrays(t);
-    tree_pairs_count<<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, c, g, g_ghosts, nring, t->r_top,
-                                                              t->pair_count, s->d_status);
+    unsigned long long* vmax2 = reinterpret_cast<unsigned long long*>(t->r_top + 2 * 1024);
+    if (line) {
+        RGPU_CUDA(s, cudaMemsetAsync(vmax2, 0, sizeof(double), s->stream));
+        max_speed2<<<nb, kB, 0, s->stream>>>(s->p, N, vmax2);
+        g_launches++;
+    }
+    const double dtl = s->dt_last_done;
+    if (line)
+        tree_pairs_count<true><<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, c, g, g_ghosts, nring, t->r_top,
+                                                                        dtl, vmax2, t->pair_count, s->d_status);
+    else
+        tree_pairs_count<false><<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, c, g, g_ghosts, nring, t->r_top,
+                                                                         dtl, vmax2, t->pair_count, s->d_status);
     exclusive_scan_counts<<<1, kB, 0, s->stream>>>(t->pair_count, N, t->pair_off);
     g_launches += 4;
     long long total = 0;
@@ -877,8 +946,14 @@ int tree_collisions(rgpu_sim* s, rgpu_collision* out, size_t cap, size_t* n_foun
         t->pairs_cap = want;
     }
     if (total) {
-        tree_pairs_write<<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, c, g, g_ghosts, nring, t->r_top,
-                                                                  t->pair_off, t->pairs, s->d_status);
+        if (line)
+            tree_pairs_write<true><<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, c, g, g_ghosts, nring, t->r_top,
+                                                                            dtl, vmax2, t->pair_off, t->pairs,
+                                                                            s->d_status);
+        else
+            tree_pairs_write<false><<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, c, g, g_ghosts, nring,
+                                                                             t->r_top, dtl, vmax2, t->pair_off,
+                                                                             t->pairs, s->d_status);
         g_launches++;
     }
     *n_found = (size_t)total;

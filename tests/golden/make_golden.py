@@ -722,10 +722,45 @@ def fixture_archive_cases():
     np.savez_compressed(os.path.join(HERE, "archive_cases.npz"), **out)
 
 
+def fixture_collision_line():
+    """LINE and LINETREE collision searches (src/collision.c:125-196, 270-330,
+    506-572) after one step, so that dt_last_done is set: the shearing-sheet patch
+    after one SEI + tree-gravity step, and a periodic box of fast particles after one
+    leapfrog drift; the reference's pair lists in its discovery order."""
+    out = {}
+    sim = ring_patch(200.0, seed=7)
+    out["ring_start"] = state(sim)
+    sim.collision = "none"
+    sim.steps(1)
+    out["ring_after1"] = state(sim)
+    out["ring_pairs_line"] = collision_pairs(sim, "line")
+    out["ring_pairs_linetree"] = collision_pairs(sim, "linetree")
+    sim = rebound.Simulation()
+    sim.rand_seed = 11
+    sim.integrator = "leapfrog"
+    sim.gravity = "none"
+    sim.boundary = "periodic"
+    sim.root_size = 10.
+    sim.N_ghost_x = sim.N_ghost_y = sim.N_ghost_z = 1
+    sim.dt = 0.3
+    sp = ctypes.byref(sim)
+    for _ in range(500):
+        u = lambda a, b: clibrebound.reb_random_uniform(sp, ctypes.c_double(a), ctypes.c_double(b))
+        nrm = lambda: clibrebound.reb_random_normal(sp, ctypes.c_double(1.0))
+        sim.add(m=0.0, r=u(0.2, 0.4), x=u(-5., 5.), y=u(-5., 5.), z=u(-5., 5.), vx=nrm(), vy=nrm(), vz=nrm())
+    out["box_start"] = state(sim)
+    sim.steps(1)
+    out["box_after1"] = state(sim)
+    out["box_pairs_line"] = collision_pairs(sim, "line")
+    out["box_pairs_linetree"] = collision_pairs(sim, "linetree")
+    out["box_pairs_direct"] = collision_pairs(sim, "direct")
+    np.savez_compressed(os.path.join(HERE, "collision_line.npz"), **out)
+
+
 if __name__ == "__main__":
     which = sys.argv[2:] or ["gravity_cases", "ring", "whfast", "sei", "gravity_plummer", "reference_cases",
                              "leapfrog_orders", "whfast_dh", "whfast_advanced", "whfast_coords",
-                             "archive_cases"]
+                             "archive_cases", "collision_line"]
     for w in which:
         print("generating", w, flush=True)
         globals()["fixture_" + w]() if w != "sei" else fixture_sei_periodic()
