@@ -726,15 +726,17 @@ def fixture_collision_line():
     """LINE and LINETREE collision searches (src/collision.c:125-196, 270-330,
     506-572) after one step, so that dt_last_done is set: the shearing-sheet patch
     after one SEI + tree-gravity step, and a periodic box of fast particles after one
-    leapfrog drift; the reference's pair lists in its discovery order."""
+    leapfrog drift; the reference's pair lists after its rand_r shuffle (src/collision.c:
+    336-342), with the shuffle seed each search started from."""
     out = {}
     sim = ring_patch(200.0, seed=7)
     out["ring_start"] = state(sim)
     sim.collision = "none"
     sim.steps(1)
     out["ring_after1"] = state(sim)
-    out["ring_pairs_line"] = collision_pairs(sim, "line")
-    out["ring_pairs_linetree"] = collision_pairs(sim, "linetree")
+    for mode in ("line", "linetree"):
+        out["ring_seed_" + mode] = np.int64(sim.rand_seed)        # the search ends with the rand_r shuffle
+        out["ring_pairs_" + mode] = collision_pairs(sim, mode)
     sim = rebound.Simulation()
     sim.rand_seed = 11
     sim.integrator = "leapfrog"
@@ -751,9 +753,9 @@ def fixture_collision_line():
     out["box_start"] = state(sim)
     sim.steps(1)
     out["box_after1"] = state(sim)
-    out["box_pairs_line"] = collision_pairs(sim, "line")
-    out["box_pairs_linetree"] = collision_pairs(sim, "linetree")
-    out["box_pairs_direct"] = collision_pairs(sim, "direct")
+    for mode in ("line", "linetree", "direct"):
+        out["box_seed_" + mode] = np.int64(sim.rand_seed)
+        out["box_pairs_" + mode] = collision_pairs(sim, mode)
     np.savez_compressed(os.path.join(HERE, "collision_line.npz"), **out)
 
 

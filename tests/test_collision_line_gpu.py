@@ -5,8 +5,12 @@ sum of the radii, in the reference's discovery order.
 Inputs, the state after the step and the reference's pair lists come from
 tests/golden/collision_line.npz (made from the reference by
 tests/golden/make_golden.py): a shearing-sheet patch after one SEI + tree-gravity
-step, and a periodic box of fast particles after one leapfrog drift.
+step, and a periodic box of fast particles after one leapfrog drift.  The search
+returns pairs in discovery order; the test applies the reference's rand_r shuffle
+from the recorded seed and then requires the reference's list entry for entry.
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -42,6 +46,22 @@ def box(gpu, start):
     return sim
 
 
+def shuffled(pairs, seed):
+    """The reference's post-search shuffle (src/collision.c:336-342): swap entry i with
+    entry rand_r(&seed) % n, i = 0..n-1, using the C library's rand_r."""
+    libc = ctypes.CDLL(None)
+    libc.rand_r.argtypes = [ctypes.POINTER(ctypes.c_uint)]
+    out = pairs.copy()
+    s = ctypes.c_uint(int(seed))
+    n = len(out)
+    for i in range(n):
+        j = libc.rand_r(ctypes.byref(s)) % n
+        tmp = out[i].copy()
+        out[i] = out[j]
+        out[j] = tmp
+    return out
+
+
 def same_pairs(got, ref, with_root):
     assert len(got) == len(ref) > 0
     assert np.array_equal(got["p1"], ref["p1"]) and np.array_equal(got["p2"], ref["p2"])
@@ -63,7 +83,8 @@ def test_line_searches_match_reference(gpu, scene, mode):
     for f in XV:
         assert np.array_equal(p[f], g[scene + "_after1"][f]), f
     sim.collision = mode
-    same_pairs(sim.collision_search(), g[key], with_root=(mode == "linetree"))
+    got = shuffled(sim.collision_search(), g["%s_seed_%s" % (scene, mode)])   # discovery order, then shuffled
+    same_pairs(got, g[key], with_root=(mode == "linetree"))
 
 
 def test_line_finds_crossings_the_overlap_test_misses(gpu):
