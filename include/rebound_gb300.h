@@ -263,9 +263,11 @@ int rgpu_direct_accel_noalloc(const double* x, const double* y, const double* z,
  * no softening; src/integrator_whfast.c:1113-1259) advanced together.
  * particles: all systems' records back to back (stride bytes each, layout of
  * struct reb_particle); system s owns records [offsets[s], offsets[s+1]).
- * dts: per-system timestep.  exact != 0 selects kernels compiled without FMA
+ * dts: per-system timestep.  exact = 1 selects kernels compiled without FMA
  * contraction (bit-identical to the reference's serial build); 0 selects the
- * faster FMA-contracted kernels. */
+ * faster FMA-contracted kernels; 2 runs democratic heliocentric coordinates
+ * (the splitting of WHFast512, src/integrator_whfast512.c), bit-identical to
+ * WHFast with coordinates = DEMOCRATICHELIOCENTRIC and safe_mode 1. */
 typedef struct rgpu_ensemble rgpu_ensemble;
 int  rgpu_ensemble_create(rgpu_ensemble** out, const void* particles, size_t stride, const int64_t* offsets,
                           size_t n_systems, const double* dts, double G, int exact);

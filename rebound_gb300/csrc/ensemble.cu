@@ -1,6 +1,6 @@
 // Batched WHFast ensemble: thousands of independent small planetary systems
-// (one REBOUND simulation each, WHFast Jacobi / DEFAULT kernel / safe_mode 1)
-// advanced together on one GPU.
+// (one REBOUND simulation each, WHFast DEFAULT kernel / safe_mode 1, Jacobi or
+// democratic heliocentric coordinates) advanced together on one GPU.
 //
 // Systems are grouped into buckets by body count; each bucket is a
 // structure-of-arrays block [field][body][system] in HBM.  One thread advances
@@ -20,6 +20,7 @@
 
 void* ensemble_exact_persistent_fn();
 void* ensemble_exact_energy_fn(int nb);
+void* ensemble_dh_persistent_fn();
 
 struct EnsBucket {
     int nb = 0;
@@ -36,7 +37,8 @@ struct rgpu_ensemble {
     std::vector<int64_t> offsets;      // n_systems + 1 particle offsets
     size_t n_systems = 0;
     double G = 1.0;
-    int exact = 0;
+    int exact = 0;               // 1: no FMA contraction (bit-identical to the reference)
+    int dh = 0;                  // 1: democratic heliocentric coordinates (implies exact)
     int block = 128;
     int64_t steps_per_launch = 256;
     cudaStream_t stream = nullptr;
@@ -72,6 +74,7 @@ EnergyFn energy_fn(const rgpu_ensemble* e, int nb) {
 typedef void (*PersistentFn)(const ens_fast::Unit*, int, int, double, unsigned int*, uint32_t*);
 
 PersistentFn persistent_fn(const rgpu_ensemble* e) {
+    if (e->dh) return (PersistentFn)ensemble_dh_persistent_fn();
     return e->exact ? (PersistentFn)ensemble_exact_persistent_fn() : ens_fast::persistent_kernel;
 }
 
@@ -151,7 +154,9 @@ int rgpu_ensemble_create(rgpu_ensemble** out, const void* particles, size_t stri
     if (!e) return RGPU_ERR_NOMEM;
     e->n_systems = n_systems;
     e->G = G;
+    if (exact < 0 || exact > 2) { delete e; return RGPU_ERR_ARG; }
     e->exact = exact != 0;
+    e->dh = exact == 2;
     e->offsets.assign(offsets, offsets + n_systems + 1);
     std::map<int, std::vector<int>> groups;
     for (size_t s = 0; s < n_systems; s++) {

@@ -3,13 +3,17 @@
 // structure-of-arrays [field][body][system] so a warp's loads and stores are
 // coalesced across systems; each thread keeps its system in registers (spilling
 // to L1-cached local memory for the largest systems) for a whole chunk of
-// steps.  Included twice: ensemble.cu (FMA contraction, fast) and
-// ensemble_exact.cu (--fmad=false, bit-identical to the reference).
+// steps.  Included three times: ensemble.cu (FMA contraction, fast),
+// ensemble_exact.cu (--fmad=false, bit-identical to the reference) and
+// ensemble_dh.cu (democratic heliocentric coordinates, --fmad=false).
 #pragma once
 #include "whfast_core.cuh"
 
 #ifndef ENSEMBLE_NS
 #error "define ENSEMBLE_NS before including ensemble_kernels.cuh"
+#endif
+#ifndef ENSEMBLE_STEP
+#define ENSEMBLE_STEP wh::step_safe     // Jacobi coordinates; ensemble_dh.cu: democratic heliocentric
 #endif
 
 namespace ENSEMBLE_NS {
@@ -29,7 +33,7 @@ __device__ __noinline__ void advance_system(double* __restrict__ st, const doubl
         s.m[i] = st[6 * f + o];
     }
     const double h = dt[sid];
-    for (int k = 0; k < n_steps; k++) wh::step_safe<NB>(s, G, 0.0, h, NB, NB, 0, status);
+    for (int k = 0; k < n_steps; k++) ENSEMBLE_STEP<NB>(s, G, 0.0, h, NB, NB, 0, status);
     t[sid] += h * n_steps;
 #pragma unroll
     for (int i = 0; i < NB; i++) {

@@ -464,6 +464,28 @@ __device__ __forceinline__ void step_safe(System<NB>& s, double G, double eps2, 
     to_inertial(s, j, N, Na);
 }
 
+// One WHFast step in democratic heliocentric coordinates with safe_mode = 1 (the
+// splitting WHFast512 vectorises, src/integrator_whfast512.c; the step of
+// src/integrator_whfast.c:1113-1259 with coordinates = DEMOCRATICHELIOCENTRIC):
+// drift, half jump, kick by the planets' mutual forces, half jump, drift.
+template <int NB>
+__device__ __forceinline__ void step_safe_dh(System<NB>& s, double G, double eps2, double dt, int N, int Na, int tp,
+                                             uint32_t* status) {
+    Jacobi<NB> h;
+    to_dh(s, h, N, Na);
+    kepler_step_dh(h, s.m[0], G, dt / 2., N, status);
+    com_step(h, dt / 2.);
+    jump_step_dh(h, s, dt / 2., N, Na);
+    dh_to_inertial(s, h, N, Na);
+    double ax[NB], ay[NB], az[NB];
+    gravity_01<NB, 1>(s, ax, ay, az, G, eps2, N, Na, tp);
+    interaction_step_dh(h, ax, ay, az, dt, N);
+    jump_step_dh(h, s, dt / 2., N, Na);
+    kepler_step_dh(h, s.m[0], G, dt / 2., N, status);
+    com_step(h, dt / 2.);
+    dh_to_inertial(s, h, N, Na);
+}
+
 // Total energy (src/tools.c:108-162) of one system.
 template <int NB>
 __device__ __forceinline__ double energy(const System<NB>& s, double G, int N, int Na, int tp) {

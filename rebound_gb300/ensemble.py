@@ -16,7 +16,13 @@ from ._lib import PARTICLE_DTYPE, RGPUError
 
 
 class Ensemble:
-    def __init__(self, systems, dts, G=1.0, exact=False):
+    """coordinates="democraticheliocentric" runs the WHFast512 splitting (always
+    bit-exact: no FMA contraction)."""
+
+    def __init__(self, systems, dts, G=1.0, exact=False, coordinates="jacobi"):
+        if coordinates not in ("jacobi", "democraticheliocentric"):
+            raise ValueError("coordinates: jacobi or democraticheliocentric")
+        mode = 2 if coordinates == "democraticheliocentric" else int(bool(exact))
         self._L = _lib.load()
         self.sizes = np.array([len(s) for s in systems], dtype=np.int64)
         self.offsets = np.concatenate([[0], np.cumsum(self.sizes)]).astype(np.int64)
@@ -25,7 +31,7 @@ class Ensemble:
         h = ctypes.c_void_p()
         rc = self._L.rgpu_ensemble_create(ctypes.byref(h), self.records.ctypes.data, PARTICLE_DTYPE.itemsize,
                                           self.offsets.ctypes.data, len(systems), self.dts.ctypes.data,
-                                          float(G), int(bool(exact)))
+                                          float(G), mode)
         if rc:
             raise RGPUError(rc, "ensemble create")
         self._h = h

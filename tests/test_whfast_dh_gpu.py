@@ -114,3 +114,29 @@ def test_safe_mode_off_synchronize_mid_run(gpu, coords):
     out, ref = sim.particles, g["two_sync_mid_" + coords]
     for f in XV:
         assert np.array_equal(out[f], ref[f]), f
+
+
+def test_dh_ensemble_bit_exact(gpu):
+    # the batched democratic heliocentric kernels (the WHFast512 splitting) follow the
+    # reference's own 100-step run and, for 200 generated systems, the plain path
+    from rebound_gb300.ensemble import Ensemble
+    g = golden("whfast_dh.npz")
+    ens = Ensemble([g["two"]], [0.005123 * 2. * math.pi], coordinates="democraticheliocentric")
+    ens.steps(100)
+    p = ens.particles()[0]
+    for f in XV:
+        assert np.array_equal(p[f], g["two_after100_safe1"][f]), f
+    systems, periods = gpu.ics.planetary_systems(200, seed=5)
+    dts = periods / 20.0
+    ens = Ensemble(systems, dts, coordinates="democraticheliocentric")
+    ens.autotune(probe_steps=2, max_steps_per_launch=16)
+    ens = Ensemble(systems, dts, coordinates="democraticheliocentric")
+    ens.set_launch(64, 7)                      # ragged chunks must not change results
+    ens.steps(50)
+    out = ens.particles()
+    for s in (0, 17, 99, 199):
+        sim = dh_sim(gpu, systems[s], dts[s])
+        sim.steps(50)
+        q = sim.particles
+        for f in XV:
+            assert np.array_equal(q[f], out[s][f]), (s, f)
