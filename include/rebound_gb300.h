@@ -91,7 +91,8 @@ typedef struct rgpu_config {
     int32_t whfast_kernel;      /* 0 DEFAULT, 1 MODIFIEDKICK, 2 COMPOSITION, 3 LAZY */
     int32_t whfast_keep_unsynchronized;  /* 1: synchronize leaves the integrator state unsynchronized */
     int32_t exact_finish_time;  /* src/rebound.h: 1 (default) lands integrate exactly on tmax */
-    int32_t reserved0;
+    int32_t tree_quadrupole;    /* 1: tree cells carry mass quadrupoles, as the reference built with
+                                   -DQUADRUPOLE (src/tree.c:147-320, src/Makefile.defs:90-91) */
 } rgpu_config;
 
 /* One overlapping, approaching pair: same layout as struct reb_collision

@@ -292,6 +292,7 @@ void orc_gravity_compensated_omp(orc_sim* r) {
  * ---------------------------------------------------------------------- */
 typedef struct ocell {
     double x, y, z, w, m, mx, my, mz;
+    double mxx, mxy, mxz, myy, myz, mzz;     /* mass quadrupole (QUADRUPOLE builds) */
     struct ocell* oct[8];
     long pt;                /* >=0 leaf particle, <0 minus particle count */
 } ocell;
@@ -387,7 +388,8 @@ static int tree_build(orc_sim* r, otree* t) {                  /* tree.c:254-271
     return 0;
 }
 
-static void cell_gravity_data(const orc_sim* r, ocell* c) {     /* tree.c:147-207 (monopole) */
+static void cell_gravity_data(const orc_sim* r, ocell* c) {     /* tree.c:147-207 */
+    c->mxx = c->mxy = c->mxz = c->myy = c->myz = c->mzz = 0.;
     if (c->pt < 0) {
         c->m = 0; c->mx = 0; c->my = 0; c->mz = 0;
         for (int o = 0; o < 8; o++) {
@@ -403,6 +405,21 @@ static void cell_gravity_data(const orc_sim* r, ocell* c) {     /* tree.c:147-20
         }
         const double mt = c->m;
         if (mt > 0) { c->mx /= mt; c->my /= mt; c->mz /= mt; }
+        if (r->tree_quadrupole) {                                   /* tree.c:180-198, Hernquist 1987 */
+            for (int o = 0; o < 8; o++) {
+                const ocell* d = c->oct[o];
+                if (!d) continue;
+                const double dm = d->m;
+                const double qx = d->mx - c->mx, qy = d->my - c->my, qz = d->mz - c->mz;
+                const double qr2 = qx * qx + qy * qy + qz * qz;
+                c->mxx += d->mxx + dm * (3. * qx * qx - qr2);
+                c->mxy += d->mxy + dm * 3. * qx * qy;
+                c->mxz += d->mxz + dm * 3. * qx * qz;
+                c->myy += d->myy + dm * (3. * qy * qy - qr2);
+                c->myz += d->myz + dm * 3. * qy * qz;
+            }
+            c->mzz = -c->mxx - c->myy;
+        }
     } else {
         const orc_particle* p = &r->particles[c->pt];
         c->m = p->m; c->mx = p->x; c->my = p->y; c->mz = p->z;
@@ -418,6 +435,17 @@ static void cell_accel(const orc_sim* r, long pt, const ocell* c, const double g
         if (c->w * c->w > r->opening_angle2 * r2) {
             for (int o = 0; o < 8; o++)
                 if (c->oct[o]) cell_accel(r, pt, c->oct[o], gx, gy, gz, ax, ay, az);
+        } else if (r->tree_quadrupole) {                            /* tree.c:293-306 */
+            const double rr = sqrt(r2 + eps2);
+            const double pf = -G / (rr * rr * rr) * c->m;
+            double qpf = G / (rr * rr * rr * rr * rr);
+            *ax += qpf * (dx * c->mxx + dy * c->mxy + dz * c->mxz);
+            *ay += qpf * (dx * c->mxy + dy * c->myy + dz * c->myz);
+            *az += qpf * (dx * c->mxz + dy * c->myz + dz * c->mzz);
+            const double mrr = dx * dx * c->mxx + dy * dy * c->myy + dz * dz * c->mzz
+                             + 2. * dx * dy * c->mxy + 2. * dx * dz * c->mxz + 2. * dy * dz * c->myz;
+            qpf *= -5.0 / (2.0 * rr * rr) * mrr;
+            *ax += (qpf + pf) * dx; *ay += (qpf + pf) * dy; *az += (qpf + pf) * dz;
         } else {
             const double rr = sqrt(r2 + eps2);
             const double pf = -G / (rr * rr * rr) * c->m;

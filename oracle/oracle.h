@@ -72,6 +72,8 @@ typedef struct orc_sim {
     int whfast_corrector2;
     int whfast_kernel;          /* 0 DEFAULT, 1 MODIFIEDKICK, 2 COMPOSITION, 3 LAZY */
     int whfast_keep_unsynchronized;
+    int tree_quadrupole;        /* 1: the reference built with -DQUADRUPOLE (src/tree.c:147-320) */
+    int reserved0;
 } orc_sim;
 
 /* Gravity (src/gravity.c). *_serial = the reference built without OpenMP;

@@ -43,7 +43,8 @@ class OrcSim(ctypes.Structure):
         ("sei_lastdt", ctypes.c_double), ("sei_sindt", ctypes.c_double), ("sei_tandt", ctypes.c_double),
         ("sei_sindtz", ctypes.c_double), ("sei_tandtz", ctypes.c_double),
         ("whfast_corrector", ctypes.c_int), ("whfast_corrector2", ctypes.c_int),
-        ("whfast_kernel", ctypes.c_int), ("whfast_keep_unsynchronized", ctypes.c_int)]
+        ("whfast_kernel", ctypes.c_int), ("whfast_keep_unsynchronized", ctypes.c_int),
+        ("tree_quadrupole", ctypes.c_int), ("reserved0", ctypes.c_int)]
 
 
 def _elf_matches_host(path):
@@ -121,7 +122,7 @@ class Sim:
     def __init__(self, particles, G=1.0, softening=0.0, dt=0.0, t=0.0, N_active=None,
                  testparticle_type=0, boundary="none", root_size=-1.0, N_root=(1, 1, 1),
                  N_ghost=(0, 0, 0), OMEGA=0.0, OMEGAZ=-1.0, opening_angle2=0.25, safe_mode=1,
-                 corrector=0, corrector2=0, kernel=0, keep_unsynchronized=0):
+                 corrector=0, corrector2=0, kernel=0, keep_unsynchronized=0, quadrupole=0):
         self.p = np.ascontiguousarray(particles, dtype=PARTICLE_DTYPE).copy()
         n = len(self.p)
         self.pj = np.zeros(n, dtype=PARTICLE_DTYPE)
@@ -141,6 +142,7 @@ class Sim:
         s.whfast_corrector, s.whfast_corrector2 = corrector, corrector2
         s.whfast_kernel = WHFAST_KERNEL[kernel] if isinstance(kernel, str) else kernel
         s.whfast_keep_unsynchronized = keep_unsynchronized
+        s.tree_quadrupole = quadrupole
         s.particles = self.p.ctypes.data
         s.p_jh = self.pj.ctypes.data
         s.cs = self.cs.ctypes.data

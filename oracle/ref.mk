@@ -9,6 +9,9 @@
 #                                         importable as the `librebound` module the
 #                                         reference's Python package looks for)
 #   oracle/_ref/librebound_omp.so         OpenMP build (-DOPENMP), for timing
+#   oracle/_ref/librebound_quad.so        serial parity build with -DQUADRUPOLE (the
+#                                         reference's compile-time quadrupole tree,
+#                                         src/Makefile.defs:90-91), for fixtures
 #
 # The recipe compiles every src/*.c like the reference's setup.py does, without
 # the HTTP server (-DSERVER is omitted) and without OpenGL.
@@ -19,7 +22,7 @@ SRCS := $(filter-out $(REF)/src/server.c,$(sort $(wildcard $(REF)/src/*.c)))
 CFLAGS := -std=c99 -O3 -fPIC -D_GNU_SOURCE -fstrict-aliasing -Wno-unknown-pragmas \
           -Wno-unreachable-code -DGITHASH=reference -I$(REF)/src
 
-all: $(OUT)/librebound$(EXT_SUFFIX) $(OUT)/librebound_omp.so
+all: $(OUT)/librebound$(EXT_SUFFIX) $(OUT)/librebound_omp.so $(OUT)/librebound_quad.so
 
 $(OUT)/librebound$(EXT_SUFFIX): $(SRCS)
 	@mkdir -p $(OUT)
@@ -28,5 +31,9 @@ $(OUT)/librebound$(EXT_SUFFIX): $(SRCS)
 $(OUT)/librebound_omp.so: $(SRCS)
 	@mkdir -p $(OUT)
 	$(CC) $(CFLAGS) -DOPENMP -fopenmp -shared $(SRCS) -lm -fopenmp -o $@
+
+$(OUT)/librebound_quad.so: $(SRCS)
+	@mkdir -p $(OUT)
+	$(CC) $(CFLAGS) -ffp-contract=off -DQUADRUPOLE -shared $(SRCS) -lm -o $@
 
 .PHONY: all

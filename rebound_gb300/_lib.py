@@ -48,7 +48,7 @@ class Config(ctypes.Structure):
         ("leapfrog_order", ctypes.c_int32), ("whfast_coordinates", ctypes.c_int32),
         ("whfast_corrector", ctypes.c_int32), ("whfast_corrector2", ctypes.c_int32),
         ("whfast_kernel", ctypes.c_int32), ("whfast_keep_unsynchronized", ctypes.c_int32),
-        ("exact_finish_time", ctypes.c_int32), ("reserved0", ctypes.c_int32)]
+        ("exact_finish_time", ctypes.c_int32), ("tree_quadrupole", ctypes.c_int32)]
 
 
 class ServerConfig(ctypes.Structure):

@@ -34,6 +34,7 @@ struct TreeBuffers {
     size_t ccap = 0;
     double *cx = nullptr, *cy = nullptr, *cz = nullptr, *cw = nullptr;
     double *cm = nullptr, *cmx = nullptr, *cmy = nullptr, *cmz = nullptr;
+    double *cqxx = nullptr, *cqxy = nullptr, *cqxz = nullptr, *cqyy = nullptr, *cqyz = nullptr;  // quadrupole
     int* cstart = nullptr;          // range in sorted order
     int* cend = nullptr;
     int* cfirst = nullptr;          // first child (children contiguous, octant order)
@@ -198,6 +199,7 @@ __global__ void radix_scatter(const unsigned long long* __restrict__ keys, const
 // --- 3. cells ------------------------------------------------------------------
 struct CellArrays {
     double *x, *y, *z, *w, *m, *mx, *my, *mz;
+    double *qxx, *qxy, *qxz, *qyy, *qyz;     // mass quadrupole (q_zz = -q_xx - q_yy)
     int *start, *end, *first, *nchild, *pt, *depth;
     unsigned long long* path;
 };
@@ -294,11 +296,12 @@ __global__ void split_level(const unsigned long long* __restrict__ keys, const i
     }
 }
 
-// --- 4. mass and centre of mass, src/tree.c:147-207 (monopole) ----------------------
-__global__ void reduce_level(ParticlesSoA p, CellArrays c, int lvl_begin, int lvl_end) {
+// --- 4. mass, centre of mass and (quad) the mass quadrupole, src/tree.c:147-207 ------
+__global__ void reduce_level(ParticlesSoA p, CellArrays c, int lvl_begin, int lvl_end, int quad) {
     const int cell = lvl_begin + blockIdx.x * blockDim.x + threadIdx.x;
     if (cell >= lvl_end) return;
     const int pt = c.pt[cell];
+    if (quad) { c.qxx[cell] = 0.; c.qxy[cell] = 0.; c.qxz[cell] = 0.; c.qyy[cell] = 0.; c.qyz[cell] = 0.; }
     if (pt == INT_MIN) { c.m[cell] = 0.; c.mx[cell] = c.my[cell] = c.mz[cell] = 0.; return; }
     if (pt >= 0) {
         c.m[cell] = p.m[pt]; c.mx[cell] = p.x[pt]; c.my[cell] = p.y[pt]; c.mz[cell] = p.z[pt];
@@ -315,6 +318,21 @@ __global__ void reduce_level(ParticlesSoA p, CellArrays c, int lvl_begin, int lv
     }
     if (m > 0) { mx /= m; my /= m; mz /= m; }
     c.m[cell] = m; c.mx[cell] = mx; c.my[cell] = my; c.mz[cell] = mz;
+    if (!quad) return;
+    // Hernquist (1987): the children's quadrupoles shifted to this cell's centre of
+    // mass, accumulated in octant order (src/tree.c:180-198)
+    double qxx = 0., qxy = 0., qxz = 0., qyy = 0., qyz = 0.;
+    for (int k = 0; k < n; k++) {
+        const double dm = c.m[f + k];
+        const double qx = c.mx[f + k] - mx, qy = c.my[f + k] - my, qz = c.mz[f + k] - mz;
+        const double qr2 = qx * qx + qy * qy + qz * qz;
+        qxx += c.qxx[f + k] + dm * (3. * qx * qx - qr2);
+        qxy += c.qxy[f + k] + dm * 3. * qx * qy;
+        qxz += c.qxz[f + k] + dm * 3. * qx * qz;
+        qyy += c.qyy[f + k] + dm * (3. * qy * qy - qr2);
+        qyz += c.qyz[f + k] + dm * 3. * qy * qz;
+    }
+    c.qxx[cell] = qxx; c.qxy[cell] = qxy; c.qxz[cell] = qxz; c.qyy[cell] = qyy; c.qyz[cell] = qyz;
 }
 
 // --- 5. the walk -----------------------------------------------------------------
@@ -325,6 +343,8 @@ struct GhostArr {
 
 constexpr int kStack = 192;
 
+// QUAD: the far-cell term of a QUADRUPOLE build (src/tree.c:293-306).
+template <bool QUAD>
 __global__ void __launch_bounds__(128) walk_exact(ParticlesSoA p, int N, CellArrays c, int n_root,
                                                   const GhostArr* __restrict__ gh, double G, double eps2,
                                                   double oa2, uint32_t* status) {
@@ -350,6 +370,21 @@ __global__ void __launch_bounds__(128) walk_exact(ParticlesSoA p, int N, CellArr
                         const int f = c.first[q], n = c.nchild[q];
                         if (sp + n > kStack) { atomicOr(status, DEV_ERR_STACK); sp = 0; break; }
                         for (int k = n - 1; k >= 0; k--) stack[sp++] = f + k;
+                        continue;
+                    }
+                    if (QUAD) {
+                        const double rr = exactfp::sqrt_rn(r2 + eps2);
+                        const double pf = exactfp::div_rn(-G, rr * rr * rr) * c.m[q];
+                        const double qxx = c.qxx[q], qxy = c.qxy[q], qxz = c.qxz[q], qyy = c.qyy[q], qyz = c.qyz[q];
+                        const double qzz = -qxx - qyy;
+                        double qpf = exactfp::div_rn(G, rr * rr * rr * rr * rr);
+                        ax += qpf * (dx * qxx + dy * qxy + dz * qxz);
+                        ay += qpf * (dx * qxy + dy * qyy + dz * qyz);
+                        az += qpf * (dx * qxz + dy * qyz + dz * qzz);
+                        const double mrr = dx * dx * qxx + dy * dy * qyy + dz * dz * qzz + 2. * dx * dy * qxy +
+                                           2. * dx * dz * qxz + 2. * dy * dz * qyz;
+                        qpf *= exactfp::div_rn(-5.0, 2.0 * rr * rr) * mrr;
+                        ax += (qpf + pf) * dx; ay += (qpf + pf) * dy; az += (qpf + pf) * dz;
                         continue;
                     }
                 } else if (pt == i) {
@@ -696,12 +731,14 @@ __global__ void exclusive_scan_counts(const int* __restrict__ cnt, int N, long l
 // --- host side -------------------------------------------------------------------------
 CellArrays arrays(TreeBuffers* t) {
     return CellArrays{t->cx, t->cy, t->cz, t->cw, t->cm, t->cmx, t->cmy, t->cmz,
-                      t->cstart, t->cend, t->cfirst, t->cnchild, t->cpt, t->cdepth, t->cpath};
+                      t->cqxx, t->cqxy, t->cqxz, t->cqyy, t->cqyz, t->cstart, t->cend, t->cfirst, t->cnchild, t->cpt, t->cdepth, t->cpath};
 }
 
 void free_cells(TreeBuffers* t) {
-    double* d[] = {t->cx, t->cy, t->cz, t->cw, t->cm, t->cmx, t->cmy, t->cmz};
+    double* d[] = {t->cx, t->cy, t->cz, t->cw, t->cm, t->cmx, t->cmy, t->cmz,
+                   t->cqxx, t->cqxy, t->cqxz, t->cqyy, t->cqyz};
     for (double* q : d) cudaFree(q);
+    t->cqxx = t->cqxy = t->cqxz = t->cqyy = t->cqyz = nullptr;
     int* n[] = {t->cstart, t->cend, t->cfirst, t->cnchild, t->cpt, t->cdepth};
     for (int* q : n) cudaFree(q);
     cudaFree(t->cpath);
@@ -713,7 +750,8 @@ void free_cells(TreeBuffers* t) {
 
 int alloc_cells(rgpu_sim* s, TreeBuffers* t, size_t ccap) {
     free_cells(t);
-    double** d[] = {&t->cx, &t->cy, &t->cz, &t->cw, &t->cm, &t->cmx, &t->cmy, &t->cmz};
+    double** d[] = {&t->cx, &t->cy, &t->cz, &t->cw, &t->cm, &t->cmx, &t->cmy, &t->cmz,
+                    &t->cqxx, &t->cqxy, &t->cqxz, &t->cqyy, &t->cqyz};
     for (double** q : d) RGPU_CUDA(s, cudaMalloc(q, sizeof(double) * ccap));
     int** n[] = {&t->cstart, &t->cend, &t->cfirst, &t->cnchild, &t->cpt, &t->cdepth};
     for (int** q : n) RGPU_CUDA(s, cudaMalloc(q, sizeof(int) * ccap));
@@ -837,7 +875,10 @@ int build_tree_once(rgpu_sim* s, bool* overflow) {
     const int nl = (int)t->level_begin.size() - 1;
     for (int d = nl - 1; d >= 0; d--) {
         const int b = t->level_begin[d], e = t->level_begin[d + 1];
-        if (e > b) { reduce_level<<<grid_for(e - b, kB), kB, 0, st>>>(s->p, c, b, e); g_launches++; }
+        if (e > b) {
+            reduce_level<<<grid_for(e - b, kB), kB, 0, st>>>(s->p, c, b, e, s->cfg.tree_quadrupole != 0);
+            g_launches++;
+        }
     }
     RGPU_CUDA(s, cudaGetLastError());
     return RGPU_OK;
@@ -867,14 +908,20 @@ int tree_accel(rgpu_sim* s) {
     const double eps2 = cf.softening * cf.softening;
     if (cf.gravity != RGPU_GRAVITY_TREE_SPLIT) {
         ktimer_begin(s);
-        walk_exact<<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, arrays(t), t->n_root, g_ghosts, cf.G, eps2,
-                                                             cf.opening_angle2, s->d_status);
+        if (cf.tree_quadrupole)
+            walk_exact<true><<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, arrays(t), t->n_root, g_ghosts, cf.G,
+                                                                      eps2, cf.opening_angle2, s->d_status);
+        else
+            walk_exact<false><<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, arrays(t), t->n_root, g_ghosts, cf.G,
+                                                                       eps2, cf.opening_angle2, s->d_status);
         ktimer_end(s);
         g_launches++;
         RGPU_CUDA(s, cudaGetLastError());
         return RGPU_OK;
     }
     // Split mode: near-window walk (reference semantics) + far-root monopole sweep.
+    if (cf.tree_quadrupole)
+        return set_error(s, RGPU_ERR_UNSUPPORTED, "the split tree mode sums far roots as monopoles (no quadrupole)");
     if (!(cf.opening_angle2 > 0.))
         return set_error(s, RGPU_ERR_ARG, "split tree mode needs opening_angle2 > 0");
     const int K = (int)ceil(1.0 / sqrt(cf.opening_angle2)) + 1;

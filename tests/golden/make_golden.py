@@ -3,7 +3,7 @@
 Run in a container that has the reference sources (it reads them where they
 lie and never copies them):
 
-    make -f oracle/ref.mk REF=<reference checkout>      # builds oracle/_ref/
+    make -f oracle/ref.mk REF=<reference checkout>      # builds oracle/_ref/ (incl. the -DQUADRUPOLE build)
     python tests/golden/make_golden.py <reference checkout>
 
 The reference's own Python package is imported from the checkout and loads the
@@ -759,10 +759,40 @@ def fixture_collision_line():
     np.savez_compressed(os.path.join(HERE, "collision_line.npz"), **out)
 
 
+def fixture_tree_quadrupole():
+    """Tree gravity with quadrupole moments (src/tree.c:147-207, 273-320 with
+    QUADRUPOLE defined; src/Makefile.defs:90-91): the reference built with
+    -DQUADRUPOLE (oracle/_ref/librebound_quad.so, from oracle/ref.mk) evaluates the
+    shearing-sheet patch; its accelerations next to the monopole build's."""
+    qlib = ctypes.CDLL(os.path.join(REPO, "oracle", "_ref", "librebound_quad.so"))
+    qlib.reb_simulation_create.restype = ctypes.c_void_p
+    qlib.reb_simulation_add.argtypes = [ctypes.c_void_p, rebound.Particle]
+    qlib.reb_simulation_update_acceleration.argtypes = [ctypes.c_void_p]
+    out = {}
+    for L, theta2 in ((200.0, 0.25), (200.0, 0.5)):
+        src = ring_patch(L, seed=7)
+        src.opening_angle2 = theta2
+        qptr = qlib.reb_simulation_create()
+        Q = ctypes.cast(qptr, ctypes.POINTER(rebound.Simulation)).contents
+        for f in ("G", "softening", "dt", "OMEGA", "root_size", "N_root_x", "N_root_y", "N_root_z",
+                  "N_ghost_x", "N_ghost_y", "N_ghost_z", "opening_angle2"):
+            setattr(Q, f, getattr(src, f))
+        Q.gravity = "tree"
+        Q.boundary = "shear"
+        for i in range(src.N):
+            qlib.reb_simulation_add(qptr, src.particles[i])
+        qlib.reb_simulation_update_acceleration(qptr)
+        tag = "t%g" % theta2
+        out["particles"] = state(src)
+        out["acc_quad_" + tag] = np.stack([state(Q)[k] for k in ("ax", "ay", "az")], axis=1)
+        out["acc_mono_" + tag] = accel(src)
+    np.savez_compressed(os.path.join(HERE, "tree_quadrupole.npz"), **out)
+
+
 if __name__ == "__main__":
     which = sys.argv[2:] or ["gravity_cases", "ring", "whfast", "sei", "gravity_plummer", "reference_cases",
                              "leapfrog_orders", "whfast_dh", "whfast_advanced", "whfast_coords",
-                             "archive_cases", "collision_line"]
+                             "archive_cases", "collision_line", "tree_quadrupole"]
     for w in which:
         print("generating", w, flush=True)
         globals()["fixture_" + w]() if w != "sei" else fixture_sei_periodic()

@@ -201,3 +201,18 @@ def test_oracle_whfast_test_particles(start, end, dt, na, tp):
     s = O.Sim(g[start], dt=dt, N_active=None if na < 0 else na, testparticle_type=tp)
     s.whfast_integrate(1.0)
     assert max_diff(s.p, g[end]) == 0.0
+
+
+@pytest.mark.parametrize("theta2", [0.25, 0.5])
+def test_oracle_tree_quadrupole(theta2):
+    # the tree with quadrupole moments against the reference built with -DQUADRUPOLE
+    gq = golden("tree_quadrupole.npz")
+    g = golden("ring_patch.npz")
+    G, OM, soft, dt, rs, nx, ny, nz, gx, gy, gz, oa2, t = g["meta"]
+    s = O.Sim(gq["particles"], G=G, softening=soft, dt=dt, boundary="shear", root_size=rs,
+              N_root=(int(nx), int(ny), int(nz)), N_ghost=(int(gx), int(gy), int(gz)), OMEGA=OM,
+              opening_angle2=theta2, t=t, quadrupole=1)
+    acc = s.gravity("tree")
+    assert np.array_equal(acc, gq["acc_quad_t%g" % theta2])
+    s.s.tree_quadrupole = 0
+    assert np.array_equal(s.gravity("tree"), gq["acc_mono_t%g" % theta2])

@@ -225,3 +225,23 @@ def test_tree_split_mode_matches_exact_walk(gpu):
     for q in (0.5, 0.9, 0.99):
         qe, qs = np.quantile(e_exact, q), np.quantile(e_split, q)
         assert abs(qs - qe) <= 1e-2 * qe, (q, qe, qs)
+
+
+@pytest.mark.parametrize("theta2", [0.25, 0.5])
+def test_tree_quadrupole_bit_exact(gpu, theta2):
+    # mass quadrupoles in the cells and the quadrupole far-cell term, against the
+    # reference built with -DQUADRUPOLE (tests/golden/tree_quadrupole.npz)
+    gq = golden("tree_quadrupole.npz")
+    g = golden("ring_patch.npz")
+    sim = ring_gpu(gpu, g, gq["particles"])
+    sim.opening_angle2 = theta2
+    sim.tree_quadrupole = 1
+    sim.update_acceleration()
+    assert np.array_equal(gpu.accelerations(sim), gq["acc_quad_t%g" % theta2])
+    sim.tree_quadrupole = 0
+    sim.update_acceleration()
+    assert np.array_equal(gpu.accelerations(sim), gq["acc_mono_t%g" % theta2])
+    sim.tree_quadrupole = 1
+    sim.gravity = "tree_split"
+    with pytest.raises(gpu.RGPUError, match="monopoles"):
+        sim.update_acceleration()
