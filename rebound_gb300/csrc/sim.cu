@@ -581,6 +581,7 @@ int rgpu_integrate(rgpu_sim* s, double tmax) {
     if (!s) return RGPU_ERR_ARG;
     rgpu_config& c = s->cfg;
     if (c.dt == 0.0) return set_error(s, RGPU_ERR_ARG, "dt must be nonzero");
+    c.status = -1;                                                  // REB_STATUS_RUNNING (:389-391)
     if (tmax != c.t) c.dt = std::copysign(c.dt, tmax > c.t ? 1.0 : -1.0);
     double last_full_dt = c.dt;
     s->dt_last_done = 0.;

@@ -142,7 +142,11 @@ struct ProgramBuilder {
     explicit ProgramBuilder(rgpu_sim* sim) : s(sim) {
         prog.n = 0;
         const bool jac = s->cfg.whfast_kernel == kKernelModifiedKick || s->cfg.whfast_kernel == kKernelLazy;
-        grav = jac ? kOpGravityJacobi : kOpGravity;     // :929-931 switch gravity to JACOBI
+        // :929-931 switch gravity to JACOBI; otherwise the simulation's own gravity
+        const int g = s->cfg.gravity;
+        grav = jac ? kOpGravityJacobi
+                   : g == RGPU_GRAVITY_COMPENSATED ? kOpGravityCompensated
+                   : g == RGPU_GRAVITY_NONE ? kOpGravityNone : kOpGravity;
         kick = jac ? kOpKickNoJacobiTerm : kOpKick;
     }
     void push(uint8_t op, double d = 0.) {
@@ -204,7 +208,7 @@ struct ProgramBuilder {
 
 bool uses_program(const rgpu_config& c) {
     return c.whfast_corrector != 0 || c.whfast_corrector2 != 0 || c.whfast_kernel != kKernelDefault ||
-           c.whfast_coordinates >= 2;
+           c.whfast_coordinates >= 2 || c.gravity != RGPU_GRAVITY_BASIC;
 }
 
 int ensure_keep(rgpu_sim* s) {
@@ -232,6 +236,8 @@ int check_config(rgpu_sim* s) {
         return set_error(s, RGPU_ERR_ARG, "First symplectic correctors are only available in the following orders: 0, 3, 5, 7, 11, 17.");
     if (c.whfast_corrector2 != 0 && c.whfast_coordinates != 0)
         return set_error(s, RGPU_ERR_UNSUPPORTED, "The second symplectic corrector runs in Jacobi coordinates on the GPU.");
+    if (c.gravity != RGPU_GRAVITY_BASIC && c.gravity != RGPU_GRAVITY_COMPENSATED && c.gravity != RGPU_GRAVITY_NONE)
+        return set_error(s, RGPU_ERR_UNSUPPORTED, "WHFast on the GPU evaluates BASIC, COMPENSATED or NONE gravity");
     if (c.whfast_keep_unsynchronized && c.whfast_safe_mode)
         return set_error(s, RGPU_ERR_ARG, "whfast->keep_unsynchronized == 1 is not compatible with safe_mode. Must set whfast->safe_mode = 0.");
     return RGPU_OK;

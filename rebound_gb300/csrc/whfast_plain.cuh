@@ -28,6 +28,8 @@ enum : uint8_t {
     kOpJerk,              // accelerations += d * jerk (kernel MODIFIEDKICK)
     kOpLazyShift,         // positions of bodies 1.. += d * accelerations (kernel LAZY)
     kOpJump,              // jump step by d (democratic heliocentric and WHDS coordinates)
+    kOpGravityCompensated,  // gravity = COMPENSATED (src/gravity.c:284-531), same terms skipped
+    kOpGravityNone,       // gravity = NONE: zero accelerations
 };
 
 // Up to 400 operators per launch keeps the kernel's parameters under 4 KB;

@@ -298,6 +298,44 @@ __device__ void gravity_basic(const wh::System<NB>& s, double ax[NB], double ay[
     }
 }
 
+// Compensated (Kahan) accumulation of one force term (src/gravity.c:431-446).
+__device__ __forceinline__ void kahan_add(double& a, double& c, double inc) {
+    const double y = inc - c;
+    const double t = a + y;
+    c = (t - a) - y;
+    a = t;
+}
+
+// reb_gravity_compensated_calculate_acceleration, serial branch (src/gravity.c:
+// 284-297, 415-531): pairs i < j among the active bodies, then test particles,
+// each term added with a Kahan correction; ign = gravity_ignore_terms.
+template <int NB>
+__device__ void gravity_compensated(const wh::System<NB>& s, double ax[NB], double ay[NB], double az[NB], double G,
+                                    double eps2, int N, int Ng, int tp, int ign) {
+    double cx[NB], cy[NB], cz[NB];
+#pragma unroll 1
+    for (int i = 0; i < N; i++) { ax[i] = 0.; ay[i] = 0.; az[i] = 0.; cx[i] = 0.; cy[i] = 0.; cz[i] = 0.; }
+#pragma unroll 1
+    for (int i = 0; i < N; i++) {
+        const bool active = i < Ng;
+#pragma unroll 1
+        for (int j = active ? i + 1 : 0; j < Ng; j++) {
+            if (ign == 1 && ((j == 1 && i == 0) || (i == 1 && j == 0))) continue;
+            if (ign == 2 && (j == 0 || i == 0)) continue;
+            const double dx = s.x[i] - s.x[j], dy = s.y[i] - s.y[j], dz = s.z[i] - s.z[j];
+            const double r2 = dx * dx + dy * dy + dz * dz + eps2;
+            const double r = sqrt(r2);
+            const double pf = G / (r2 * r);
+            const double pfj = -pf * s.m[j];
+            kahan_add(ax[i], cx[i], pfj * dx); kahan_add(ay[i], cy[i], pfj * dy); kahan_add(az[i], cz[i], pfj * dz);
+            if (active || tp) {
+                const double pfi = pf * s.m[i];
+                kahan_add(ax[j], cx[j], pfi * dx); kahan_add(ay[j], cy[j], pfi * dy); kahan_add(az[j], cz[j], pfi * dz);
+            }
+        }
+    }
+}
+
 template <int NB>
 __global__ void __launch_bounds__(32) whfast_program(ParticlesSoA p, double* jac, size_t cap, int N, int Na, int Ng,
                                                      int tp, int coords, double G, double eps2,
@@ -337,6 +375,13 @@ __global__ void __launch_bounds__(32) whfast_program(ParticlesSoA p, double* jac
                 break;
             case kOpGravity: gravity_basic(s, ax, ay, az, G, eps2, N, Ng, tp, starti, startj); break;
             case kOpGravityJacobi: gravity_jacobi(s, ax, ay, az, G, N); break;
+            case kOpGravityCompensated:
+                gravity_compensated(s, ax, ay, az, G, eps2, N, Ng, tp, coords == 0 ? 1 : coords == 3 ? 0 : 2);
+                break;
+            case kOpGravityNone:
+#pragma unroll 1
+                for (int i = 0; i < N; i++) { ax[i] = 0.; ay[i] = 0.; az[i] = 0.; }
+                break;
             case kOpKick:
             case kOpKickNoJacobiTerm:
                 if (coords == 0) wh::interaction_step(j, s, ax, ay, az, G, d, N, Na, op == kOpKick);

@@ -23,6 +23,11 @@ _CFG_INTS = ("testparticle_type", "N_root_x", "N_root_y", "N_root_z", "N_ghost_x
              "N_ghost_z", "rand_seed", "gravity_ignore_terms", "leapfrog_order", "tree_quadrupole")
 
 
+class Collision(Exception):
+    """An integration stopped because two particles collided and collision_resolve
+    is "halt" (rebound's Collision exception)."""
+
+
 class WHFastSettings:
     """rebound's ri_whfast on the GPU path: safe_mode, coordinates, correctors, kernel,
     keep_unsynchronized (src/integrator_whfast.h:28-50)."""
@@ -244,6 +249,8 @@ class Simulation:
         self._cfg.exact_finish_time = int(exact_finish_time)
         self._push()
         self._after(self._L.rgpu_integrate(self._h, float(tmax)))
+        if self._cfg.status == 7:                # REB_STATUS_COLLISION (rebound/simulation.py:1324)
+            raise Collision("Two particles collided (d < r1+r2)")
 
     def collision_search(self):
         """Pair list of the search half of reb_collision_search (src/collision.c:49)."""

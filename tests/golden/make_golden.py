@@ -789,10 +789,60 @@ def fixture_tree_quadrupole():
     np.savez_compressed(os.path.join(HERE, "tree_quadrupole.npz"), **out)
 
 
+def fixture_whfast_gravity():
+    """WHFast with the simulation's gravity set to COMPENSATED or NONE (the
+    reference's WHFast evaluates r->gravity): the scenarios of
+    rebound/tests/test_gravity.py:55-94 with the reference's own end states and its
+    IAS15 value, and 100-step outer-solar-system runs per coordinate system."""
+    out = {}
+    sim = rebound.Simulation()
+    sim.gravity = "compensated"
+    sim.integrator = "whfast"
+    sim.testparticle_type = 0
+    sim.add(m=1.)
+    sim.add(m=1e-3, a=1.)
+    out["comp0_start"] = state(sim)
+    out["comp0_dt"] = sim.dt
+    sim.N_active = 1
+    sim.integrate(10.)
+    out["comp0_end"] = state(sim)
+    for integ in ("whfast", "ias15"):
+        sim = rebound.Simulation()
+        sim.gravity = "compensated"
+        sim.integrator = integ
+        if integ == "whfast":
+            sim.dt = 1e-4
+        sim.testparticle_type = 1
+        sim.add(m=1.)
+        sim.add(m=1e-3, a=1.)
+        sim.add(m=1e-3, a=1.4)
+        out["comp1_start"] = state(sim)
+        sim.N_active = 2
+        sim.integrate(10.)
+        out["comp1_end_" + integ] = state(sim)
+    sim = rebound.Simulation()
+    sim.add("outer solar system")
+    out["oss"] = state(sim)
+    for gravity in ("compensated", "none"):
+        for coords in ("jacobi", "democraticheliocentric", "whds", "barycentric"):
+            sim = rebound.Simulation()
+            load(sim, out["oss"])
+            sim.gravity = gravity
+            sim.integrator = "whfast"
+            sim.integrator.coordinates = coords
+            sim.integrator.safe_mode = 0
+            sim.dt = 0.5
+            sim.steps(100)
+            sim.synchronize()
+            out["oss_%s_%s" % (gravity, coords)] = state(sim)
+    np.savez_compressed(os.path.join(HERE, "whfast_gravity.npz"), **out)
+
+
 if __name__ == "__main__":
     which = sys.argv[2:] or ["gravity_cases", "ring", "whfast", "sei", "gravity_plummer", "reference_cases",
                              "leapfrog_orders", "whfast_dh", "whfast_advanced", "whfast_coords",
-                             "archive_cases", "collision_line", "tree_quadrupole"]
+                             "archive_cases", "collision_line", "tree_quadrupole",
+                             "whfast_gravity"]
     for w in which:
         print("generating", w, flush=True)
         globals()["fixture_" + w]() if w != "sei" else fixture_sei_periodic()
