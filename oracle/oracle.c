@@ -974,13 +974,168 @@ static void inertial_to_jacobi_acc(const orc_particle* ps, orc_particle* pj, con
     pj[0].ax = sx * mti; pj[0].ay = sy * mti; pj[0].az = sz * mti;
 }
 
+/* Democratic heliocentric, WHDS and barycentric coordinates
+ * (src/transformations.c:295-644); coordinates = 0 Jacobi, 1 democratic
+ * heliocentric, 2 WHDS, 3 barycentric. */
+static void inertial_to_helio(const orc_particle* P, orc_particle* h, size_t N, size_t Na, int whds) {
+    double x0 = 0., y0 = 0., z0 = 0., vx0 = 0., vy0 = 0., vz0 = 0., m0 = 0.;   /* :388-425, :295-345 */
+    for (size_t i = 0; i < Na; i++) {
+        const double m = P[i].m;
+        x0 += P[i].x * m; y0 += P[i].y * m; z0 += P[i].z * m;
+        vx0 += P[i].vx * m; vy0 += P[i].vy * m; vz0 += P[i].vz * m;
+        m0 += m;
+    }
+    h[0].x = x0 / m0; h[0].y = y0 / m0; h[0].z = z0 / m0;
+    h[0].vx = vx0 / m0; h[0].vy = vy0 / m0; h[0].vz = vz0 / m0;
+    h[0].m = m0;
+    const double ms = P[0].m;
+    for (size_t i = 1; i < N; i++) {
+        h[i].x = P[i].x - P[0].x; h[i].y = P[i].y - P[0].y; h[i].z = P[i].z - P[0].z;
+        if (whds && i < Na) {
+            const double mf = (ms + P[i].m) / ms;
+            h[i].vx = mf * (P[i].vx - h[0].vx); h[i].vy = mf * (P[i].vy - h[0].vy); h[i].vz = mf * (P[i].vz - h[0].vz);
+        } else {
+            h[i].vx = P[i].vx - h[0].vx; h[i].vy = P[i].vy - h[0].vy; h[i].vz = P[i].vz - h[0].vz;
+        }
+        h[i].m = P[i].m;
+    }
+}
+
+static void helio_to_inertial(orc_particle* P, const orc_particle* h, size_t N, size_t Na, int whds) {
+    const double mtot = h[0].m;                                      /* :427-473, :347-381 */
+    double x0 = 0., y0 = 0., z0 = 0.;
+    for (size_t i = 1; i < Na; i++) {
+        const double m = h[i].m;
+        x0 += h[i].x * m / mtot; y0 += h[i].y * m / mtot; z0 += h[i].z * m / mtot;
+        P[i].m = m;
+    }
+    P[0].x = h[0].x - x0; P[0].y = h[0].y - y0; P[0].z = h[0].z - z0;
+    for (size_t i = 1; i < N; i++) {
+        P[i].x = h[i].x + P[0].x; P[i].y = h[i].y + P[0].y; P[i].z = h[i].z + P[0].z;
+    }
+    const double m0 = P[0].m;
+    for (size_t i = 1; i < N; i++) {
+        if (whds && i < Na) {
+            const double mf = (m0 + P[i].m) / m0;
+            P[i].vx = h[i].vx / mf + h[0].vx; P[i].vy = h[i].vy / mf + h[0].vy; P[i].vz = h[i].vz / mf + h[0].vz;
+        } else {
+            P[i].vx = h[i].vx + h[0].vx; P[i].vy = h[i].vy + h[0].vy; P[i].vz = h[i].vz + h[0].vz;
+        }
+    }
+    double vx0 = 0., vy0 = 0., vz0 = 0.;
+    for (size_t i = 1; i < Na; i++) {
+        const double m = P[i].m;
+        if (whds) { vx0 += h[i].vx * m / (m0 + m); vy0 += h[i].vy * m / (m0 + m); vz0 += h[i].vz * m / (m0 + m); }
+        else { vx0 += h[i].vx * m / m0; vy0 += h[i].vy * m / m0; vz0 += h[i].vz * m / m0; }
+    }
+    P[0].vx = h[0].vx - vx0; P[0].vy = h[0].vy - vy0; P[0].vz = h[0].vz - vz0;
+}
+
+static void inertial_to_bary(const orc_particle* P, orc_particle* b, size_t N, size_t Na) {   /* :595-644 */
+    b[0].x = P[0].m * P[0].x; b[0].y = P[0].m * P[0].y; b[0].z = P[0].m * P[0].z;
+    b[0].vx = P[0].m * P[0].vx; b[0].vy = P[0].m * P[0].vy; b[0].vz = P[0].m * P[0].vz;
+    b[0].m = P[0].m;
+    double sx = 0., sy = 0., sz = 0., svx = 0., svy = 0., svz = 0., sm = 0.;
+    for (size_t i = 1; i < Na; i++) {
+        const double m = P[i].m;
+        b[i].m = m;
+        sx += P[i].x * m; sy += P[i].y * m; sz += P[i].z * m;
+        svx += P[i].vx * m; svy += P[i].vy * m; svz += P[i].vz * m;
+        sm += m;
+    }
+    b[0].x += sx; b[0].y += sy; b[0].z += sz; b[0].vx += svx; b[0].vy += svy; b[0].vz += svz; b[0].m += sm;
+    const double mi = 1.0 / b[0].m;
+    b[0].x *= mi; b[0].y *= mi; b[0].z *= mi; b[0].vx *= mi; b[0].vy *= mi; b[0].vz *= mi;
+    for (size_t i = 1; i < N; i++) {
+        if (i >= Na) b[i].m = P[i].m;
+        b[i].x = P[i].x - b[0].x; b[i].y = P[i].y - b[0].y; b[i].z = P[i].z - b[0].z;
+        b[i].vx = P[i].vx - b[0].vx; b[i].vy = P[i].vy - b[0].vy; b[i].vz = P[i].vz - b[0].vz;
+    }
+}
+
+static void bary_to_inertial(orc_particle* P, const orc_particle* b, size_t N, size_t Na) {   /* :544-593 */
+    P[0].x = b[0].m * b[0].x; P[0].y = b[0].m * b[0].y; P[0].z = b[0].m * b[0].z;
+    P[0].vx = b[0].m * b[0].vx; P[0].vy = b[0].m * b[0].vy; P[0].vz = b[0].m * b[0].vz;
+    P[0].m = b[0].m;
+    double sx = 0., sy = 0., sz = 0., svx = 0., svy = 0., svz = 0., sm = 0.;
+    for (size_t i = 1; i < N; i++) {
+        P[i].x = b[i].x + b[0].x; P[i].y = b[i].y + b[0].y; P[i].z = b[i].z + b[0].z;
+        P[i].vx = b[i].vx + b[0].vx; P[i].vy = b[i].vy + b[0].vy; P[i].vz = b[i].vz + b[0].vz;
+        if (i < Na) {
+            const double m = b[i].m;
+            P[i].m = m;
+            sx += P[i].x * m; sy += P[i].y * m; sz += P[i].z * m;
+            svx += P[i].vx * m; svy += P[i].vy * m; svz += P[i].vz * m;
+            sm += m;
+        }
+    }
+    P[0].x -= sx; P[0].y -= sy; P[0].z -= sz; P[0].vx -= svx; P[0].vy -= svy; P[0].vz -= svz; P[0].m -= sm;
+    const double m0i = 1. / P[0].m;
+    P[0].x *= m0i; P[0].y *= m0i; P[0].z *= m0i; P[0].vx *= m0i; P[0].vy *= m0i; P[0].vz *= m0i;
+}
+
+/* reb_integrator_whfast_from_inertial / _to_inertial (src/integrator_whfast.c:950-1024) */
+static void whfast_from_inertial(orc_sim* r) {
+    const size_t N = r->N, Na = wh_active_of(r);
+    switch (r->whfast_coordinates) {
+        case 1: inertial_to_helio(r->particles, r->p_jh, N, Na, 0); break;
+        case 2: inertial_to_helio(r->particles, r->p_jh, N, Na, 1); break;
+        case 3: inertial_to_bary(r->particles, r->p_jh, N, Na); break;
+        default: orc_inertial_to_jacobi_posvel(r->particles, r->p_jh, r->particles, N, Na);
+    }
+}
+
+static void whfast_to_inertial(orc_sim* r) {
+    const size_t N = r->N, Na = wh_active_of(r);
+    switch (r->whfast_coordinates) {
+        case 1: helio_to_inertial(r->particles, r->p_jh, N, Na, 0); break;
+        case 2: helio_to_inertial(r->particles, r->p_jh, N, Na, 1); break;
+        case 3: bary_to_inertial(r->particles, r->p_jh, N, Na); break;
+        default: orc_jacobi_to_inertial_posvel(r->particles, r->p_jh, r->particles, N, Na);
+    }
+}
+
 static void whfast_kepler_step(orc_sim* r, double dt) {           /* :589-636, serial branch */
     const double m0 = r->particles[0].m;
     const size_t N = r->N, Na = wh_active_of(r);
     double eta = m0;
     for (size_t i = 1; i < N; i++) {
-        if (i < Na) eta += r->p_jh[i].m;
-        orc_whfast_kepler_solver(&r->p_jh[i], eta * r->G, dt);
+        double e;
+        switch (r->whfast_coordinates) {
+            case 1: e = m0; break;
+            case 2: e = i < Na ? m0 + r->p_jh[i].m : m0; break;
+            case 3: e = r->p_jh[0].m; break;
+            default: if (i < Na) eta += r->p_jh[i].m; e = eta;
+        }
+        orc_whfast_kepler_solver(&r->p_jh[i], e * r->G, dt);
+    }
+}
+
+/* reb_integrator_whfast_jump_step (:526-584): democratic heliocentric and WHDS only. */
+static void whfast_jump_step(orc_sim* r, double dt) {
+    const int c = r->whfast_coordinates;
+    if (c != 1 && c != 2) return;
+    orc_particle* h = r->p_jh;
+    const orc_particle* P = r->particles;
+    const size_t N = r->N, Na = wh_active_of(r);
+    const double m0 = P[0].m;
+    double px = 0., py = 0., pz = 0.;
+    for (size_t i = 1; i < Na; i++) {
+        const double m = P[i].m;
+        if (c == 1) { px += m * h[i].vx; py += m * h[i].vy; pz += m * h[i].vz; }
+        else { px += m * h[i].vx / (m0 + m); py += m * h[i].vy / (m0 + m); pz += m * h[i].vz / (m0 + m); }
+    }
+    for (size_t i = 1; i < N; i++) {
+        if (c == 1) {
+            h[i].x += dt * (px / m0); h[i].y += dt * (py / m0); h[i].z += dt * (pz / m0);
+        } else if (i < Na) {
+            const double m = P[i].m;
+            h[i].x += dt * (px - (m * h[i].vx / (m0 + m)));
+            h[i].y += dt * (py - (m * h[i].vy / (m0 + m)));
+            h[i].z += dt * (pz - (m * h[i].vz / (m0 + m)));
+        } else {
+            h[i].x += dt * px; h[i].y += dt * py; h[i].z += dt * pz;
+        }
     }
 }
 
@@ -990,7 +1145,34 @@ static void whfast_com_step(orc_sim* r, double dt) {              /* :638-651 */
     r->p_jh[0].z += dt * r->p_jh[0].vz;
 }
 
-static void whfast_interaction_step(orc_sim* r, double dt) {      /* :431-492 */
+static void whfast_interaction_step_jacobi(orc_sim* r, double dt);
+
+static void whfast_interaction_step(orc_sim* r, double dt) {      /* :431-524 */
+    const int c = r->whfast_coordinates;
+    if (c == 0) { whfast_interaction_step_jacobi(r, dt); return; }
+    orc_particle* h = r->p_jh;
+    const orc_particle* P = r->particles;
+    const size_t N = r->N, Na = wh_active_of(r);
+    const double m0 = P[0].m;
+    for (size_t i = 1; i < N; i++) {
+        if (c == 2 && i < Na) {                                    /* :502-508 */
+            const double mi = P[i].m;
+            h[i].vx += dt * (m0 + mi) * P[i].ax / m0;
+            h[i].vy += dt * (m0 + mi) * P[i].ay / m0;
+            h[i].vz += dt * (m0 + mi) * P[i].az / m0;
+        } else if (c == 3) {                                       /* :517-524 */
+            const double dr = sqrt(h[i].x * h[i].x + h[i].y * h[i].y + h[i].z * h[i].z);
+            const double pf = r->G * h[0].m / (dr * dr * dr);
+            h[i].vx += dt * (pf * h[i].x + P[i].ax);
+            h[i].vy += dt * (pf * h[i].y + P[i].ay);
+            h[i].vz += dt * (pf * h[i].z + P[i].az);
+        } else {                                                   /* :494-500 */
+            h[i].vx += dt * P[i].ax; h[i].vy += dt * P[i].ay; h[i].vz += dt * P[i].az;
+        }
+    }
+}
+
+static void whfast_interaction_step_jacobi(orc_sim* r, double dt) {  /* :431-492 */
     const size_t N = r->N, Na = wh_active_of(r);
     orc_particle* pj = r->p_jh;
     /* kernels MODIFIEDKICK and LAZY run with gravity = JACOBI: the Jacobi term is
@@ -1045,8 +1227,13 @@ static void gravity_jacobi(orc_sim* r) {
 /* reb_simulation_update_acceleration for WHFast: BASIC with the 0-1 pair
  * skipped, or JACOBI for kernels MODIFIEDKICK and LAZY (:929-931). */
 static void whfast_update_acceleration(orc_sim* r) {
-    if (r->whfast_kernel == 1 || r->whfast_kernel == 3) gravity_jacobi(r);
-    else orc_gravity_basic_serial(r);
+    if (r->whfast_kernel == 1 || r->whfast_kernel == 3) { gravity_jacobi(r); return; }
+    switch (r->whfast_gravity) {                                   /* the simulation's gravity */
+        case 1: orc_gravity_compensated_serial(r); break;
+        case 2: for (size_t i = 0; i < r->N; i++) r->particles[i].ax = r->particles[i].ay = r->particles[i].az = 0.;
+                break;
+        default: orc_gravity_basic_serial(r);
+    }
 }
 
 /* reb_integrator_whfast_calculate_jerk (:786-870) into jx, jy, jz. */
@@ -1123,7 +1310,7 @@ static const double corr2_b = 0.03486083443891981449909050107438281205803;
 
 /* Jacobi -> inertial, then the accelerations, then a kick of dt. */
 static void whfast_evaluate_kick(orc_sim* r, double dt) {
-    orc_jacobi_to_inertial_posvel(r->particles, r->p_jh, r->particles, r->N, wh_active_of(r));
+    whfast_to_inertial(r);
     whfast_update_acceleration(r);
     whfast_interaction_step(r, dt);
 }
@@ -1180,7 +1367,7 @@ void orc_whfast_synchronize(orc_sim* r) {                         /* :1051-1111 
         whfast_com_step(r, d);
         if (r->whfast_corrector2) apply_corrector2(r, -1.);
         if (r->whfast_corrector) apply_corrector(r, -1., r->whfast_corrector);
-        orc_jacobi_to_inertial_posvel(r->particles, r->p_jh, r->particles, r->N, wh_active_of(r));
+        whfast_to_inertial(r);
         if (keep) {
             memcpy(r->p_jh, keep, sizeof(orc_particle) * r->N);
             free(keep);
@@ -1193,10 +1380,11 @@ void orc_whfast_synchronize(orc_sim* r) {                         /* :1051-1111 
 void orc_whfast_step(orc_sim* r) {                                /* :1113-1259 */
     const double dt = r->dt;
     const size_t N = r->N, Na = wh_active_of(r);
-    r->gravity_ignore_terms = 1;
+    const int coords = r->whfast_coordinates;
+    r->gravity_ignore_terms = coords == 0 ? 1 : coords == 3 ? 0 : 2;   /* :929-938 */
     if (r->whfast_safe_mode || r->whfast_did_modify) {
         if (r->whfast_is_synchronized == 0) orc_whfast_synchronize(r);
-        orc_inertial_to_jacobi_posvel(r->particles, r->p_jh, r->particles, N, Na);
+        whfast_from_inertial(r);
         r->whfast_did_modify = 0;
     }
     if (r->whfast_is_synchronized) {
@@ -1209,7 +1397,8 @@ void orc_whfast_step(orc_sim* r) {                                /* :1113-1259 
         whfast_kepler_step(r, dt);
         whfast_com_step(r, dt);
     }
-    orc_jacobi_to_inertial_posvel(r->particles, r->p_jh, r->particles, N, Na);
+    whfast_jump_step(r, dt / 2.);
+    whfast_to_inertial(r);
     r->t += dt / 2.;
     whfast_update_acceleration(r);
     switch (r->whfast_kernel) {
@@ -1250,6 +1439,7 @@ void orc_whfast_step(orc_sim* r) {                                /* :1113-1259 
         }
         default:                                                   /* DEFAULT */
             whfast_interaction_step(r, dt);
+            whfast_jump_step(r, dt / 2.);
     }
     r->whfast_is_synchronized = 0;
     if (r->whfast_safe_mode) orc_whfast_synchronize(r);

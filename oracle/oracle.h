@@ -73,6 +73,8 @@ typedef struct orc_sim {
     int whfast_kernel;          /* 0 DEFAULT, 1 MODIFIEDKICK, 2 COMPOSITION, 3 LAZY */
     int whfast_keep_unsynchronized;
     int tree_quadrupole;        /* 1: the reference built with -DQUADRUPOLE (src/tree.c:147-320) */
+    int whfast_coordinates;     /* 0 Jacobi, 1 democratic heliocentric, 2 WHDS, 3 barycentric */
+    int whfast_gravity;         /* the gravity WHFast evaluates: 0 BASIC, 1 COMPENSATED, 2 NONE */
     int reserved0;
 } orc_sim;
 

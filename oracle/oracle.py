@@ -44,7 +44,8 @@ class OrcSim(ctypes.Structure):
         ("sei_sindtz", ctypes.c_double), ("sei_tandtz", ctypes.c_double),
         ("whfast_corrector", ctypes.c_int), ("whfast_corrector2", ctypes.c_int),
         ("whfast_kernel", ctypes.c_int), ("whfast_keep_unsynchronized", ctypes.c_int),
-        ("tree_quadrupole", ctypes.c_int), ("reserved0", ctypes.c_int)]
+        ("tree_quadrupole", ctypes.c_int), ("whfast_coordinates", ctypes.c_int),
+        ("whfast_gravity", ctypes.c_int), ("reserved0", ctypes.c_int)]
 
 
 def _elf_matches_host(path):
@@ -114,6 +115,7 @@ def lib():
 GRAVITY = {"none": 0, "basic": 1, "compensated": 2, "tree": 3, "basic_omp": 101, "compensated_omp": 102}
 BOUNDARY = {"none": 0, "open": 1, "periodic": 2, "shear": 3}
 WHFAST_KERNEL = {"default": 0, "modifiedkick": 1, "composition": 2, "lazy": 3}
+WHFAST_COORDINATES = {"jacobi": 0, "democraticheliocentric": 1, "whds": 2, "barycentric": 3}
 
 
 class Sim:
@@ -122,7 +124,8 @@ class Sim:
     def __init__(self, particles, G=1.0, softening=0.0, dt=0.0, t=0.0, N_active=None,
                  testparticle_type=0, boundary="none", root_size=-1.0, N_root=(1, 1, 1),
                  N_ghost=(0, 0, 0), OMEGA=0.0, OMEGAZ=-1.0, opening_angle2=0.25, safe_mode=1,
-                 corrector=0, corrector2=0, kernel=0, keep_unsynchronized=0, quadrupole=0):
+                 corrector=0, corrector2=0, kernel=0, keep_unsynchronized=0, quadrupole=0,
+                 coordinates="jacobi", whfast_gravity="basic"):
         self.p = np.ascontiguousarray(particles, dtype=PARTICLE_DTYPE).copy()
         n = len(self.p)
         self.pj = np.zeros(n, dtype=PARTICLE_DTYPE)
@@ -143,6 +146,8 @@ class Sim:
         s.whfast_kernel = WHFAST_KERNEL[kernel] if isinstance(kernel, str) else kernel
         s.whfast_keep_unsynchronized = keep_unsynchronized
         s.tree_quadrupole = quadrupole
+        s.whfast_coordinates = WHFAST_COORDINATES[coordinates] if isinstance(coordinates, str) else coordinates
+        s.whfast_gravity = {"basic": 0, "compensated": 1, "none": 2}[whfast_gravity]
         s.particles = self.p.ctypes.data
         s.p_jh = self.pj.ctypes.data
         s.cs = self.cs.ctypes.data

@@ -216,3 +216,71 @@ def test_oracle_tree_quadrupole(theta2):
     assert np.array_equal(acc, gq["acc_quad_t%g" % theta2])
     s.s.tree_quadrupole = 0
     assert np.array_equal(s.gravity("tree"), gq["acc_mono_t%g" % theta2])
+
+
+COORDS = ("jacobi", "democraticheliocentric", "whds", "barycentric")
+
+
+@pytest.mark.parametrize("coords,safe", [(c, s) for c in ("democraticheliocentric", "whds", "barycentric")
+                                         for s in (1, 0)])
+def test_oracle_whfast_other_coordinates(coords, safe):
+    # 100-step two-planet runs of the reference in each coordinate system, bit for bit
+    import math
+    name, key = ("whfast_dh.npz", "two_after100_safe%d" % safe) if coords == "democraticheliocentric" \
+        else ("whfast_coords.npz", "two_%s_safe%d" % (coords, safe))
+    g = golden(name)
+    s = O.Sim(g["two"], dt=0.005123 * 2. * math.pi, safe_mode=safe, coordinates=coords)
+    s.whfast(100)
+    s.whfast_synchronize()
+    assert max_diff(s.p, g[key]) == 0.0
+
+
+@pytest.mark.parametrize("order,safe,n", [(5, 0, 50), (17, 1, 10)])
+def test_oracle_whfast_barycentric_correctors(order, safe, n):
+    import math
+    g = golden("whfast_coords.npz")
+    s = O.Sim(g["two"], dt=0.005123 * 2. * math.pi, safe_mode=safe, coordinates="barycentric", corrector=order)
+    s.whfast(n)
+    s.whfast_synchronize()
+    assert max_diff(s.p, g["two_barycentric_c%d" % order]) == 0.0
+
+
+def test_oracle_whds_outer_solar_system():
+    g = golden("whfast_coords.npz")
+    s = O.Sim(g["oss"], dt=0.005 * 12. * 2. * 3.1415, coordinates="whds")
+    s.whfast_integrate(1000. * 2. * 3.1415)
+    assert max_diff(s.p, g["whds_oss_end"]) == 0.0
+
+
+@pytest.mark.parametrize("coords", COORDS)
+def test_oracle_test_particles_every_coordinate_system(coords):
+    # rebound/tests/test_whfast_testparticles.py scenarios, the reference's end states
+    g = golden("whfast_coords.npz")
+    for N in (1, 2):
+        for start, dt, nas in (("tp_N%d" % N, 0.1, [-1] + list(range(1, N + 2))),
+                               ("tpp_N%d" % N, 1e-3, [-1] + list(range(3, N + 4)))):
+            for na in nas:
+                s = O.Sim(g[start], dt=dt, N_active=None if na < 0 else na, coordinates=coords)
+                s.whfast_integrate(1.0)
+                assert max_diff(s.p, g["%s_%s_na%d" % (start, coords, na)]) == 0.0, (start, na)
+
+
+@pytest.mark.parametrize("gravity", ["compensated", "none"])
+@pytest.mark.parametrize("coords", COORDS)
+def test_oracle_whfast_gravity_modes(gravity, coords):
+    g = golden("whfast_gravity.npz")
+    s = O.Sim(g["oss"], dt=0.5, safe_mode=0, coordinates=coords, whfast_gravity=gravity)
+    s.whfast(100)
+    s.whfast_synchronize()
+    assert max_diff(s.p, g["oss_%s_%s" % (gravity, coords)]) == 0.0
+
+
+def test_oracle_whfast_compensated_test_particles():
+    # rebound/tests/test_gravity.py:55-94 runs, the reference's own end states
+    g = golden("whfast_gravity.npz")
+    s = O.Sim(g["comp0_start"], dt=float(g["comp0_dt"]), N_active=1, whfast_gravity="compensated")
+    s.whfast_integrate(10.)
+    assert max_diff(s.p, g["comp0_end"]) == 0.0 and s.p["x"][0] == 0.0
+    s = O.Sim(g["comp1_start"], dt=1e-4, N_active=2, testparticle_type=1, whfast_gravity="compensated")
+    s.whfast_integrate(10.)
+    assert max_diff(s.p, g["comp1_end_whfast"]) == 0.0
