@@ -196,29 +196,33 @@ __device__ void bary_to_inertial(wh::System<NB>& s, const wh::Jacobi<NB>& b, int
     s.vx[0] = vx0 * m0i; s.vy[0] = vy0 * m0i; s.vz[0] = vz0 * m0i;
 }
 
-// reb_integrator_whfast_kepler_step (src/integrator_whfast.c:589-636), every
-// coordinate system through one inlined solver: the gravitational parameter of
-// body i is G times the interior Jacobi mass, m_0, m_0 + m_i (WHDS, active) or the
-// total mass (barycentric).
+// reb_integrator_whfast_kepler_step (src/integrator_whfast.c:589-636), one body
+// per lane: lane i (1 <= i < N) drifts body i.  The bodies' Kepler solves are
+// independent; the gravitational parameter of body i is G times the interior
+// Jacobi mass (rebuilt by lane i with the serial loop's additions in the same
+// order, so it rounds identically), m_0, m_0 + m_i (WHDS, active) or the total
+// mass (barycentric).  The caller brackets the call with __syncwarp().
 template <int NB>
-__device__ void drift(wh::Jacobi<NB>& j, double m0, double G, double dt, int N, int Na, int coords,
-                      uint32_t* status) {
-    double eta = m0;
+__device__ void drift_lane(wh::Jacobi<NB>& j, double m0, double G, double dt, int N, int Na, int coords,
+                           uint32_t* status) {
+    const int i = threadIdx.x;
+    if (i < 1 || i >= N) return;
+    double e;
+    if (coords == 0) {
+        e = m0;
 #pragma unroll 1
-    for (int i = 1; i < N; i++) {
-        double e;
-        if (coords == 0) {
-            if (i < Na) eta += j.m[i];
-            e = eta;
-        } else if (coords == 2) {
-            e = i < Na ? m0 + j.m[i] : m0;
-        } else if (coords == 3) {
-            e = j.m[0];
-        } else {
-            e = m0;
-        }
-        wh::kepler_solver(j.x[i], j.y[i], j.z[i], j.vx[i], j.vy[i], j.vz[i], e * G, dt, status);
+        for (int k = 1; k <= i; k++)
+            if (k < Na) e += j.m[k];
+    } else if (coords == 2) {
+        e = i < Na ? m0 + j.m[i] : m0;
+    } else if (coords == 3) {
+        e = j.m[0];
+    } else {
+        e = m0;
     }
+    double x = j.x[i], y = j.y[i], z = j.z[i], vx = j.vx[i], vy = j.vy[i], vz = j.vz[i];
+    wh::kepler_solver(x, y, z, vx, vy, vz, e * G, dt, status);
+    j.x[i] = x; j.y[i] = y; j.z[i] = z; j.vx[i] = vx; j.vy[i] = vy; j.vz[i] = vz;
 }
 
 // reb_integrator_whfast_jump_step (:526-584); nothing in Jacobi or barycentric.
@@ -340,17 +344,25 @@ template <int NB>
 __global__ void __launch_bounds__(32) whfast_program(ParticlesSoA p, double* jac, size_t cap, int N, int Na, int Ng,
                                                      int tp, int coords, double G, double eps2,
                                                      const __grid_constant__ Program prog, uint32_t* status) {
-    if (threadIdx.x != 0) return;
+    // Lane 0 interprets the program; every lane takes part in the drifts (one body
+    // each).  The coordinates live in shared memory so that all lanes see them.
+    __shared__ wh::Jacobi<NB> j;
+    __shared__ int stop;
+    const int lane = threadIdx.x;
     wh::System<NB> s;
-    wh::Jacobi<NB> j;
     double ax[NB], ay[NB], az[NB];
-    load_sys(s, p, N);
-    load_jac(j, jac, cap, N);
+    if (lane == 0) {
+        stop = 0;
+        load_sys(s, p, N);
+        load_jac(j, jac, cap, N);
 #pragma unroll
-    for (int i = 0; i < NB; i++) {
-        const bool on = i < N;
-        ax[i] = on ? p.ax[i] : 0.; ay[i] = on ? p.ay[i] : 0.; az[i] = on ? p.az[i] : 0.;
+        for (int i = 0; i < NB; i++) {
+            const bool on = i < N;
+            ax[i] = on ? p.ax[i] : 0.; ay[i] = on ? p.ay[i] : 0.; az[i] = on ? p.az[i] : 0.;
+        }
     }
+    __syncwarp();
+    const double m0 = p.m[0];                       // the star's mass as the drift reads it
     // gravity_ignore_terms of each coordinate system (:929-938)
     const int starti = coords == 3 ? 1 : 2;
     const int startj = (coords == 1 || coords == 2) ? 1 : 0;
@@ -358,46 +370,55 @@ __global__ void __launch_bounds__(32) whfast_program(ParticlesSoA p, double* jac
     for (int k = 0; k < prog.n; k++) {
         const double d = prog.d[k];
         const int op = prog.op[k];
-        switch (op) {
-            case kOpFromInertial:
-                if (coords == 0) wh::to_jacobi(s, j, N, Na);
-                else if (coords == 1) wh::to_dh(s, j, N, Na);
-                else if (coords == 2) to_whds(s, j, N, Na);
-                else to_bary(s, j, N, Na);
-                break;
-            case kOpDrift: drift(j, s.m[0], G, d, N, Na, coords, status); break;
-            case kOpCom: wh::com_step(j, d); break;
-            case kOpToInertial:
-                if (coords == 0) wh::to_inertial(s, j, N, Na);
-                else if (coords == 1) wh::dh_to_inertial(s, j, N, Na);
-                else if (coords == 2) whds_to_inertial(s, j, N, Na);
-                else bary_to_inertial(s, j, N, Na);
-                break;
-            case kOpGravity: gravity_basic(s, ax, ay, az, G, eps2, N, Ng, tp, starti, startj); break;
-            case kOpGravityJacobi: gravity_jacobi(s, ax, ay, az, G, N); break;
-            case kOpGravityCompensated:
-                gravity_compensated(s, ax, ay, az, G, eps2, N, Ng, tp, coords == 0 ? 1 : coords == 3 ? 0 : 2);
-                break;
-            case kOpGravityNone:
-#pragma unroll 1
-                for (int i = 0; i < N; i++) { ax[i] = 0.; ay[i] = 0.; az[i] = 0.; }
-                break;
-            case kOpKick:
-            case kOpKickNoJacobiTerm:
-                if (coords == 0) wh::interaction_step(j, s, ax, ay, az, G, d, N, Na, op == kOpKick);
-                else kick_helio(j, s, ax, ay, az, G, d, N, Na, coords);
-                break;
-            case kOpJump: jump(j, s, d, N, Na, coords); break;
-            case kOpJerk: add_jerk(s, ax, ay, az, G, d, N); break;
-            case kOpLazyShift:
-#pragma unroll 1
-                for (int i = 1; i < N; i++) {
-                    s.x[i] += d * ax[i]; s.y[i] += d * ay[i]; s.z[i] += d * az[i];
-                }
-                break;
-            default: atomicOr(status, DEV_ERR_PROGRAM); return;
+        if (op == kOpDrift) {
+            drift_lane(j, m0, G, d, N, Na, coords, status);
+            __syncwarp();
+            continue;
         }
+        if (lane == 0) {
+            switch (op) {
+                case kOpFromInertial:
+                    if (coords == 0) wh::to_jacobi(s, j, N, Na);
+                    else if (coords == 1) wh::to_dh(s, j, N, Na);
+                    else if (coords == 2) to_whds(s, j, N, Na);
+                    else to_bary(s, j, N, Na);
+                    break;
+                case kOpCom: wh::com_step(j, d); break;
+                case kOpToInertial:
+                    if (coords == 0) wh::to_inertial(s, j, N, Na);
+                    else if (coords == 1) wh::dh_to_inertial(s, j, N, Na);
+                    else if (coords == 2) whds_to_inertial(s, j, N, Na);
+                    else bary_to_inertial(s, j, N, Na);
+                    break;
+                case kOpGravity: gravity_basic(s, ax, ay, az, G, eps2, N, Ng, tp, starti, startj); break;
+                case kOpGravityJacobi: gravity_jacobi(s, ax, ay, az, G, N); break;
+                case kOpGravityCompensated:
+                    gravity_compensated(s, ax, ay, az, G, eps2, N, Ng, tp, coords == 0 ? 1 : coords == 3 ? 0 : 2);
+                    break;
+                case kOpGravityNone:
+#pragma unroll 1
+                    for (int i = 0; i < N; i++) { ax[i] = 0.; ay[i] = 0.; az[i] = 0.; }
+                    break;
+                case kOpKick:
+                case kOpKickNoJacobiTerm:
+                    if (coords == 0) wh::interaction_step(j, s, ax, ay, az, G, d, N, Na, op == kOpKick);
+                    else kick_helio(j, s, ax, ay, az, G, d, N, Na, coords);
+                    break;
+                case kOpJump: jump(j, s, d, N, Na, coords); break;
+                case kOpJerk: add_jerk(s, ax, ay, az, G, d, N); break;
+                case kOpLazyShift:
+#pragma unroll 1
+                    for (int i = 1; i < N; i++) {
+                        s.x[i] += d * ax[i]; s.y[i] += d * ay[i]; s.z[i] += d * az[i];
+                    }
+                    break;
+                default: atomicOr(status, DEV_ERR_PROGRAM); stop = 1; break;
+            }
+        }
+        __syncwarp();
+        if (stop) return;
     }
+    if (lane != 0) return;
     store_pos_vel(s, p, N);
     store_jac(j, jac, cap, N);
 #pragma unroll
