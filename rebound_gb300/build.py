@@ -18,7 +18,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
           "-diag-suppress", "1444", "-I" + os.path.join(os.path.dirname(HERE), "include")]
 # Units whose arithmetic must not be contracted into FMAs.
-NO_FMAD = {"sim.cu", "tree.cu", "collide.cu", "whfast.cu", "whfast_dh.cu", "whfast_prog.cu", "ensemble_exact.cu", "ensemble_dh.cu"}
+NO_FMAD = {"sim.cu", "tree.cu", "collide.cu", "whfast.cu", "whfast_prog.cu", "ensemble_exact.cu", "ensemble_dh.cu"}
 
 
 def elf_matches_host(path):

@@ -1,74 +1,16 @@
 // WHFast on an rgpu_sim: the plain, one-simulation-per-call GPU path that a
 // REBOUND integrator plugin drives one step at a time
-// (src/integrator_whfast.c:1113-1259).  One kernel launch per step; the
-// system's state lives in the handle's SoA arrays (inertial) plus a Jacobi
-// buffer for safe_mode = 0.  Compiled with --fmad=false: bit-identical to the
-// reference's serial build.
+// (src/integrator_whfast.c:1113-1259).  Each step or synchronize is laid out as
+// a program of operators in the reference's order (ProgramBuilder) and run by
+// whfast_program (whfast_prog.cu) in one launch: one lane interprets it, the
+// Kepler drifts use one lane per body.  The system's state lives in the
+// handle's SoA arrays (inertial) plus a coordinate buffer for safe_mode = 0.
+// Compiled with --fmad=false: bit-identical to the reference's serial build.
 #include "whfast_plain.cuh"
 
 namespace {
 
 using namespace wh_plain;
-
-// One step (or a synchronize) of src/integrator_whfast.c for the handle's system.
-template <int NB>
-__global__ void __launch_bounds__(32) whfast_plain(ParticlesSoA p, double* jac, size_t cap, int N, int Na, int Ng, int tp,
-                                                   double G, double eps2, double dt, int flags, uint32_t* status) {
-    if (threadIdx.x != 0) return;
-    wh::System<NB> s;
-    wh::Jacobi<NB> j;
-    load_sys(s, p, N);
-    const bool sync_only = (flags & kSyncOnly) != 0;
-    if (!sync_only && (flags & kFromInertial)) wh::to_jacobi(s, j, N, Na);
-    else load_jac(j, jac, cap, N);
-    // One drift call site (rolled passes) keeps one inlined copy of the Kepler solver:
-    // pass 0 = the opening drift (dt/2 when synchronized, dt when not) and the kick, or
-    // the synchronize drift; pass 1 = the closing drift of safe_mode.
-#pragma unroll 1
-    for (int pass = 0; pass < 2; pass++) {
-        if (pass == 1 && (sync_only || !(flags & kSyncAtEnd))) break;
-        const double d = (pass == 0 && !sync_only && !(flags & kFirstHalf)) ? dt : dt / 2.;
-        wh::kepler_step(j, s.m[0], G, d, N, Na, status);
-        wh::com_step(j, d);
-        wh::to_inertial(s, j, N, Na);
-        if (pass == 0 && !sync_only) {
-            double ax[NB], ay[NB], az[NB];
-            wh::gravity_01(s, ax, ay, az, G, eps2, N, Ng, tp);
-            wh::interaction_step(j, s, ax, ay, az, G, dt, N, Na);
-#pragma unroll
-            for (int i = 0; i < NB; i++) {
-                if (i >= N) break;
-                p.ax[i] = ax[i]; p.ay[i] = ay[i]; p.az[i] = az[i];
-            }
-        }
-    }
-    store_pos_vel(s, p, N);
-    store_jac(j, jac, cap, N);               // synchronize keeps the drifted coordinates, as the reference
-}
-
-typedef void (*PlainKernel)(ParticlesSoA, double*, size_t, int, int, int, int, double, double, double, int, uint32_t*);
-
-template <int NB>
-PlainKernel pick() { return whfast_plain<NB>; }
-
-PlainKernel kernel_for(int n) {
-    switch (n) {
-        case 1: case 2: return pick<2>();
-        case 3: return pick<3>();
-        case 4: return pick<4>();
-        case 5: return pick<5>();
-        case 6: return pick<6>();
-        case 7: return pick<7>();
-        case 8: return pick<8>();
-        case 9: return pick<9>();
-        case 10: return pick<10>();
-        case 11: return pick<11>();
-        case 12: return pick<12>();
-        case 13: case 14: return pick<14>();
-        case 15: case 16: return pick<16>();
-        default: return nullptr;
-    }
-}
 
 int ensure_jac(rgpu_sim* s) {
     if (!s->wh) s->wh = new WhfastBuffers();
@@ -80,23 +22,7 @@ int ensure_jac(rgpu_sim* s) {
     return RGPU_OK;
 }
 
-int launch(rgpu_sim* s, int flags) {
-    const int N = (int)s->N;
-    RGPU_TRY(ensure_jac(s));
-    if (s->cfg.whfast_coordinates == 1) return launch_dh(s, flags);
-    PlainKernel k = kernel_for(N);
-    if (!k) return set_error(s, RGPU_ERR_UNSUPPORTED, "WHFast on the GPU supports 2..16 particles per simulation");
-    const rgpu_config& c = s->cfg;
-    ktimer_begin(s);
-    k<<<1, 32, 0, s->stream>>>(s->p, s->wh->jac, s->cap, N, wh_active(s), (int)n_active(s), c.testparticle_type, c.G,
-                               c.softening * c.softening, c.dt, flags, s->d_status);
-    ktimer_end(s);
-    g_launches++;
-    RGPU_CUDA(s, cudaGetLastError());
-    return RGPU_OK;
-}
-
-// --- programs: correctors and the non-default kernels -------------------------
+// --- programs: every step and synchronize ---------------------------------------
 // The corrector coefficients of src/integrator_whfast.c:124-158 (Wisdom, Holman &
 // Touma 1996; Wisdom 2006), kept digit for digit: the products with dt must round
 // as the reference's do.
@@ -206,11 +132,6 @@ struct ProgramBuilder {
     }
 };
 
-bool uses_program(const rgpu_config& c) {
-    return c.whfast_corrector != 0 || c.whfast_corrector2 != 0 || c.whfast_kernel != kKernelDefault ||
-           c.whfast_coordinates >= 2 || c.gravity != RGPU_GRAVITY_BASIC;
-}
-
 int ensure_keep(rgpu_sim* s) {
     if (s->wh->keep && s->wh->keep_cap == s->wh->cap) return RGPU_OK;
     cudaFree(s->wh->keep);
@@ -291,19 +212,13 @@ int whfast_step(rgpu_sim* s) {
     RGPU_TRY(check_config(s));
     const int k = c.whfast_coordinates;                          // :929-938
     c.gravity_ignore_terms = k == 0 ? 1 : k == 3 ? 0 : 2;
-    int flags = 0;
+    bool from_inertial = false;
     if (c.whfast_safe_mode || s->did_modify) {
         if (!s->whfast_synchronized) RGPU_TRY(whfast_synchronize(s));
-        flags |= kFromInertial;
+        from_inertial = true;
     }
-    if (uses_program(c)) {
-        RGPU_TRY(ensure_jac(s));
-        RGPU_TRY(program_step(s, (flags & kFromInertial) != 0));
-    } else {
-        if (s->whfast_synchronized) flags |= kFirstHalf;
-        if (c.whfast_safe_mode) flags |= kSyncAtEnd;
-        RGPU_TRY(launch(s, flags));
-    }
+    RGPU_TRY(ensure_jac(s));
+    RGPU_TRY(program_step(s, from_inertial));
     s->whfast_synchronized = c.whfast_safe_mode != 0;
     c.t += c.dt / 2.;                                            // two half steps, as :1186 and :1244
     c.t += c.dt / 2.;
@@ -320,12 +235,10 @@ int whfast_synchronize(rgpu_sim* s) {
         RGPU_TRY(ensure_keep(s));
         RGPU_CUDA(s, cudaMemcpyAsync(s->wh->keep, s->wh->jac, bytes, cudaMemcpyDeviceToDevice, s->stream));
     }
-    if (uses_program(s->cfg)) {
+    {
         ProgramBuilder b(s);
         b.synchronize();
         RGPU_TRY(b.flush());
-    } else {
-        RGPU_TRY(launch(s, kSyncOnly));
     }
     if (keep) {                                                  // :1102-1104
         RGPU_CUDA(s, cudaMemcpyAsync(s->wh->jac, s->wh->keep, bytes, cudaMemcpyDeviceToDevice, s->stream));

@@ -1,6 +1,6 @@
-// Pieces shared by the plain (one simulation per call) WHFast kernels in
-// Jacobi (whfast.cu) and democratic heliocentric (whfast_dh.cu) coordinates:
-// the handle's coordinate buffer, the step flags and the load / store helpers.
+// Pieces shared by the plain (one simulation per call) WHFast path: the
+// handle's coordinate buffer, the operator program that whfast.cu builds and
+// whfast_prog.cu runs, and the load / store helpers.
 #pragma once
 #include "whfast_core.cuh"
 
@@ -12,10 +12,8 @@ struct WhfastBuffers {
 
 namespace wh_plain {
 
-enum : int { kFromInertial = 1, kFirstHalf = 2, kSyncAtEnd = 4, kSyncOnly = 8 };
-
-// Operators of a WHFast program: one step or synchronize with correctors or a
-// non-default kernel, laid out by the host in the reference's order.
+// Operators of a WHFast program: one step or synchronize, laid out by the host
+// in the reference's order.
 enum : uint8_t {
     kOpFromInertial = 0,  // inertial -> Jacobi coordinates (positions and velocities)
     kOpDrift,             // Kepler drift of every Jacobi body by d
@@ -91,9 +89,6 @@ __device__ void store_jac(const wh::Jacobi<NB>& j, double* jac, size_t cap, int 
 inline int wh_active(const rgpu_sim* s) {
     return (s->cfg.testparticle_type == 1 || s->cfg.N_active < 0) ? (int)s->N : (int)s->cfg.N_active;
 }
-
-// Democratic heliocentric step / synchronize on the handle (whfast_dh.cu).
-int launch_dh(rgpu_sim* s, int flags);
 
 // Runs one program on the handle's system (whfast_prog.cu).
 int launch_program(rgpu_sim* s, const Program& prog);
