@@ -617,6 +617,106 @@ size_t orc_collision_search_tree(orc_sim* r, orc_collision* out, size_t cap) {
     return b.n;
 }
 
+/* Do two straight paths over the last step (relative position d at its end,
+ * relative velocity dv, step dtl) come within rsum?  src/collision.c:149-173 and
+ * :512-534: the distances at the end, at the start and, when it falls inside
+ * the step, at closest approach. */
+static int paths_touch(double dx, double dy, double dz, double dvx, double dvy, double dvz, double dtl,
+                       double rsum) {
+    const double r_end = dx * dx + dy * dy + dz * dz;
+    const double sx = dx - dtl * dvx, sy = dy - dtl * dvy, sz = dz - dtl * dvz;
+    const double r_start = sx * sx + sy * sy + sz * sz;
+    const double tc = (dx * dvx + dy * dvy + dz * dvz) / (dvx * dvx + dvy * dvy + dvz * dvz);
+    double rmin2 = r_end < r_start ? r_end : r_start;
+    if (tc / dtl >= 0. && tc / dtl <= 1.) {
+        const double cx = dx - tc * dvx, cy = dy - tc * dvy, cz = dz - tc * dvz;
+        const double r_close = cx * cx + cy * cy + cz * cz;
+        rmin2 = rmin2 < r_close ? rmin2 : r_close;
+    }
+    return !(rmin2 > rsum * rsum);
+}
+
+/* REB_COLLISION_LINE (src/collision.c:125-196): ghost boxes of the inner ring,
+ * then i, then j > i. */
+size_t orc_collision_search_line(orc_sim* r, double dtl, orc_collision* out, size_t cap) {
+    const orc_particle* P = r->particles;
+    pairbuf b = {out, cap, 0};
+    const int nx = r->N_ghost_x > 1 ? 1 : r->N_ghost_x;
+    const int ny = r->N_ghost_y > 1 ? 1 : r->N_ghost_y;
+    const int nz = r->N_ghost_z > 1 ? 1 : r->N_ghost_z;
+    for (int gx = -nx; gx <= nx; gx++)
+    for (int gy = -ny; gy <= ny; gy++)
+    for (int gz = -nz; gz <= nz; gz++) {
+        double g0[6];
+        orc_boundary_ghostbox(r, gx, gy, gz, g0);
+        for (size_t i = 0; i < r->N; i++) {
+            const orc_particle p1 = P[i];
+            const double sx = g0[0] + p1.x, sy = g0[1] + p1.y, sz = g0[2] + p1.z;
+            const double svx = g0[3] + p1.vx, svy = g0[4] + p1.vy, svz = g0[5] + p1.vz;
+            for (size_t j = i + 1; j < r->N; j++) {
+                const orc_particle p2 = P[j];
+                if (paths_touch(sx - p2.x, sy - p2.y, sz - p2.z, svx - p2.vx, svy - p2.vy, svz - p2.vz, dtl,
+                                p1.r + p2.r))
+                    pair_push(&b, i, j, g0, 0);
+            }
+        }
+    }
+    return b.n;
+}
+
+static void tree_paths(const orc_sim* r, const double s[6], const double g0[6], int ri, double p1r,
+                       double p1r_dtv, double maxdrift, double dtl, size_t p1, const ocell* c,
+                       pairbuf* b) {                              /* collision.c:506-572 */
+    const orc_particle* P = r->particles;
+    if (c->pt >= 0) {
+        if ((size_t)c->pt == p1) return;
+        const orc_particle p2 = P[c->pt];
+        if (paths_touch(s[0] - p2.x, s[1] - p2.y, s[2] - p2.z, s[3] - p2.vx, s[4] - p2.vy, s[5] - p2.vz, dtl,
+                        p1r + p2.r))
+            pair_push(b, p1, (size_t)c->pt, g0, (size_t)ri);
+    } else {
+        const double dx = s[0] - c->x, dy = s[1] - c->y, dz = s[2] - c->z;
+        const double r2 = dx * dx + dy * dy + dz * dz;
+        const double rp = p1r_dtv + maxdrift + 0.86602540378443 * c->w;
+        if (r2 < rp * rp)
+            for (int o = 0; o < 8; o++)
+                if (c->oct[o]) tree_paths(r, s, g0, ri, p1r, p1r_dtv, maxdrift, dtl, p1, c->oct[o], b);
+    }
+}
+
+/* REB_COLLISION_LINETREE (src/collision.c:270-330): i, then ghost boxes, then roots. */
+size_t orc_collision_search_linetree(orc_sim* r, double dtl, orc_collision* out, size_t cap) {
+    pairbuf b = {out, cap, 0};
+    const orc_particle* P = r->particles;
+    double vmax2 = 0.;
+    for (size_t i = 0; i < r->N; i++) {
+        const double v2 = P[i].vx * P[i].vx + P[i].vy * P[i].vy + P[i].vz * P[i].vz;
+        vmax2 = vmax2 > v2 ? vmax2 : v2;
+    }
+    const double maxdrift = dtl * sqrt(vmax2);
+    otree t = {0};
+    if (tree_build(r, &t)) { tree_free(&t); return 0; }
+    const int nx = r->N_ghost_x > 1 ? 1 : r->N_ghost_x;
+    const int ny = r->N_ghost_y > 1 ? 1 : r->N_ghost_y;
+    const int nz = r->N_ghost_z > 1 ? 1 : r->N_ghost_z;
+    for (size_t i = 0; i < r->N; i++) {
+        const orc_particle p1 = P[i];
+        const double p1r_dtv = p1.r + dtl * sqrt(p1.vx * p1.vx + p1.vy * p1.vy + p1.vz * p1.vz);
+        for (int gx = -nx; gx <= nx; gx++)
+        for (int gy = -ny; gy <= ny; gy++)
+        for (int gz = -nz; gz <= nz; gz++) {
+            double g0[6], s[6];
+            orc_boundary_ghostbox(r, gx, gy, gz, g0);
+            s[0] = g0[0] + p1.x; s[1] = g0[1] + p1.y; s[2] = g0[2] + p1.z;
+            s[3] = g0[3] + p1.vx; s[4] = g0[4] + p1.vy; s[5] = g0[5] + p1.vz;
+            for (size_t k = 0; k < t.n_root; k++)
+                if (t.root[k]) tree_paths(r, s, g0, (int)k, p1.r, p1r_dtv, maxdrift, dtl, i, t.root[k], &b);
+        }
+    }
+    tree_free(&t);
+    return b.n;
+}
+
 /* Hardsphere resolution, src/collision.c:573-665, constant restitution eps. */
 void orc_collision_resolve_hardsphere(orc_sim* r, const orc_collision* c, double eps, double minvel) {
     orc_particle* P = r->particles;

@@ -100,6 +100,9 @@ def lib():
         L.orc_collision_search_direct.restype = ctypes.c_size_t
         L.orc_collision_search_tree.argtypes = [P, ctypes.c_void_p, ctypes.c_size_t]
         L.orc_collision_search_tree.restype = ctypes.c_size_t
+        for name in ("orc_collision_search_line", "orc_collision_search_linetree"):
+            getattr(L, name).argtypes = [P, ctypes.c_double, ctypes.c_void_p, ctypes.c_size_t]
+            getattr(L, name).restype = ctypes.c_size_t
         L.orc_tree_export.argtypes = [P, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
         L.orc_tree_export.restype = ctypes.c_int
         L.orc_energy.argtypes = [P]
@@ -224,14 +227,20 @@ class Sim:
     def energy(self):
         return lib().orc_energy(self.ref)
 
-    def collisions(self, mode="direct", cap=None):
+    def collisions(self, mode="direct", cap=None, dt_last_done=0.0):
+        """Pairs in discovery order; "line" / "linetree" test the paths over the last
+        step of length dt_last_done."""
         L = lib()
-        fn = L.orc_collision_search_direct if mode == "direct" else L.orc_collision_search_tree
         cap = cap or max(1024, 64 * len(self.p))
         out = np.zeros(cap, dtype=COLLISION_DTYPE)
-        n = fn(self.ref, out.ctypes.data, cap)
+        if mode in ("line", "linetree"):
+            fn = L.orc_collision_search_line if mode == "line" else L.orc_collision_search_linetree
+            n = fn(self.ref, float(dt_last_done), out.ctypes.data, cap)
+        else:
+            fn = L.orc_collision_search_direct if mode == "direct" else L.orc_collision_search_tree
+            n = fn(self.ref, out.ctypes.data, cap)
         if n > cap:
-            return self.collisions(mode, cap=int(n))
+            return self.collisions(mode, cap=int(n), dt_last_done=dt_last_done)
         return out[:n]
 
     def tree_cells(self):

@@ -284,3 +284,41 @@ def test_oracle_whfast_compensated_test_particles():
     s = O.Sim(g["comp1_start"], dt=1e-4, N_active=2, testparticle_type=1, whfast_gravity="compensated")
     s.whfast_integrate(10.)
     assert max_diff(s.p, g["comp1_end_whfast"]) == 0.0
+
+
+def shuffled_like_reference(pairs, seed):
+    """The post-search rand_r shuffle of src/collision.c:336-342 (C library rand_r)."""
+    import ctypes
+    libc = ctypes.CDLL(None)
+    libc.rand_r.argtypes = [ctypes.POINTER(ctypes.c_uint)]
+    out = pairs.copy()
+    s = ctypes.c_uint(int(seed))
+    for i in range(len(out)):
+        j = libc.rand_r(ctypes.byref(s)) % len(out)
+        tmp = out[i].copy()
+        out[i] = out[j]
+        out[j] = tmp
+    return out
+
+
+@pytest.mark.parametrize("scene", ["ring", "box"])
+@pytest.mark.parametrize("mode", ["line", "linetree"])
+def test_oracle_line_searches(scene, mode):
+    # LINE / LINETREE on the reference's post-step states: the reference's lists entry
+    # for entry after its shuffle
+    g = golden("collision_line.npz")
+    if scene == "ring":
+        G, OM, soft, dt, rs, nx, ny, nz, gx, gy, gz, oa2, t = golden("ring_patch.npz")["meta"]
+        s = O.Sim(g["ring_after1"], G=G, softening=soft, dt=dt, boundary="shear", root_size=rs,
+                  N_root=(int(nx), int(ny), int(nz)), N_ghost=(int(gx), int(gy), int(gz)), OMEGA=OM,
+                  t=t + dt)                                  # one step in: the shear offset moves with t
+    else:
+        dt = 0.3
+        s = O.Sim(g["box_after1"], dt=dt, boundary="periodic", root_size=10., N_ghost=(1, 1, 1))
+    got = shuffled_like_reference(s.collisions(mode, dt_last_done=dt), g["%s_seed_%s" % (scene, mode)])
+    ref = g["%s_pairs_%s" % (scene, mode)]
+    assert len(got) == len(ref) > 0
+    assert np.array_equal(got["p1"], ref["p1"]) and np.array_equal(got["p2"], ref["p2"])
+    assert np.array_equal(got["gb"], ref["gb"])
+    if mode == "linetree":
+        assert np.array_equal(got["ri"], ref["ri"])
