@@ -118,3 +118,70 @@ def test_snapshot_roundtrip_in_memory(gpu):
     # a buffer without the magic is refused with an error, not read
     bad = ctypes.create_string_buffer(b"XXXXXXXX" + buf.raw[8:w.value], w.value)
     assert L.rgpu_sim_snapshot_read(c._h, bad, w.value) != 0
+
+
+def copy_via_snapshot(gpu, sim):
+    """A second handle restored from a snapshot of `sim` (the reference's sim.copy())."""
+    twin = gpu.Simulation()
+    import ctypes
+    L = sim._L
+    n = ctypes.c_size_t(0)
+    assert L.rgpu_sim_snapshot_size(sim.handle, ctypes.byref(n)) == 0
+    buf = ctypes.create_string_buffer(n.value)
+    w = ctypes.c_size_t(0)
+    assert L.rgpu_sim_snapshot_write(sim.handle, buf, n.value, ctypes.byref(w)) == 0
+    assert L.rgpu_sim_snapshot_read(twin._h, buf, w.value) == 0
+    L.rgpu_sim_get_config(twin._h, ctypes.byref(twin._cfg))
+    twin._host = np.zeros(L.rgpu_sim_N(twin._h), dtype=gpu.PARTICLE_DTYPE)
+    twin._device_newer = True
+    return twin
+
+
+@pytest.mark.parametrize("c,c2,kernel", [(0, 0, "default"), (3, 0, "modifiedkick"), (3, 0, "composition"),
+                                         (3, 0, "default"), (3, 0, "lazy"), (3, 1, "lazy")])
+def test_whfast_restart_equals_continuation(gpu, c, c2, kernel):
+    # rebound/tests/test_whfast_advanced.py:113-125 (restart): one step, copy, one more
+    # step on each; both equal, and equal to the reference's two-step run when safe
+    g = golden("whfast_advanced.npz")
+    sim = gpu.Simulation()
+    sim.add(g["oss"])
+    sim.integrator = "whfast"
+    sim.ri_whfast.corrector = c
+    sim.ri_whfast.corrector2 = c2
+    sim.ri_whfast.kernel = kernel
+    sim.dt = float(g["dt"])
+    sim.steps(1)
+    sim2 = copy_via_snapshot(gpu, sim)
+    sim.steps(1)
+    sim2.steps(1)
+    assert sim.t == sim2.t
+    same(sim.particles, sim2.particles)
+
+
+def test_shearing_sheet_restart_bit_exact(gpu, tmp_path):
+    # the ring patch (SEI, shear, tree gravity, tree collisions, hardsphere): 3 steps,
+    # snapshot, 3 more steps on the original and on the restored handle
+    g = golden("ring_patch.npz")
+    G, OM, soft, dt, rs, nx, ny, nz, gx, gy, gz, oa2, t = g["meta"]
+
+    def ring():
+        sim = gpu.Simulation()
+        sim.G, sim.OMEGA, sim.softening, sim.dt, sim.t = G, OM, soft, dt, t
+        sim.configure_box(rs, int(nx), int(ny), int(nz))
+        sim.configure_ghostboxes(int(gx), int(gy), int(gz))
+        sim.opening_angle2 = oa2
+        sim.boundary, sim.gravity, sim.integrator = "shear", "tree", "sei"
+        sim.collision, sim.collision_resolve = "tree", "hardsphere"
+        sim.coefficient_of_restitution = 0.5
+        sim.rand_seed = int(g["after5_seed0"])
+        sim.add(g["particles"])
+        return sim
+
+    a = ring()
+    a.steps(3)
+    a.save_to_file(tmp_path / "ring.bin", delete_file=True)
+    b = gpu.Simulationarchive(tmp_path / "ring.bin")[-1]
+    a.steps(3)
+    b.steps(3)
+    assert a.t == b.t and a.rand_seed == b.rand_seed and a.collisions_log_n == b.collisions_log_n
+    same(a.particles, b.particles)
