@@ -20,7 +20,8 @@ from ._lib import PARTICLE_DTYPE, COLLISION_DTYPE, Config, check
 _CFG_FLOATS = ("G", "softening", "dt", "t", "OMEGA", "OMEGAZ", "root_size", "opening_angle2",
                "coefficient_of_restitution", "minimum_collision_velocity")
 _CFG_INTS = ("testparticle_type", "N_root_x", "N_root_y", "N_root_z", "N_ghost_x", "N_ghost_y",
-             "N_ghost_z", "rand_seed", "gravity_ignore_terms", "leapfrog_order", "tree_quadrupole")
+             "N_ghost_z", "rand_seed", "gravity_ignore_terms", "leapfrog_order", "tree_quadrupole",
+             "exact_finish_time")
 
 
 class Collision(Exception):
