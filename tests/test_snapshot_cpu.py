@@ -55,3 +55,27 @@ def test_missing_archive_is_an_error(tmp_path):
     L = _lib.load()
     n = ctypes.c_size_t(0)
     assert L.rgpu_archive_scan(str(tmp_path / "none.bin").encode(), None, None, 0, ctypes.byref(n)) != 0
+
+
+def test_archive_index_by_time(tmp_path):
+    # Simulationarchive's bookkeeping (rebound/simulationarchive.py:110-177): length,
+    # tmin / tmax, and the snapshot at or before a requested time
+    from rebound_gb300 import Simulationarchive
+    path = tmp_path / "a.bin"
+    path.write_bytes(b"".join(record(t, 2) for t in (0.0, 10.25, 20.5, 30.75)))
+    sa = Simulationarchive(path)
+    assert len(sa) == 4 and sa.tmin == 0.0 and sa.tmax == 30.75
+    assert [sa._snapshot_index(t) for t in (0.0, 5.0, 10.25, 20.49, 29.0, 30.75)] == [0, 0, 1, 1, 2, 3]
+    for bad in (-1.0, 31.0):
+        try:
+            sa._snapshot_index(bad)
+        except ValueError:
+            pass
+        else:
+            raise AssertionError("time outside the archive accepted")
+    try:
+        sa[4]
+    except IndexError:
+        pass
+    else:
+        raise AssertionError("index past the end accepted")
