@@ -162,7 +162,9 @@ int rgpu_integrate(rgpu_sim* sim, double tmax);
 /* WHFast: bring inertial particles up to date (src/integrator_whfast.c:1051-1111). */
 int rgpu_synchronize(rgpu_sim* sim);
 
-/* Total energy, unsoftened, test-particle aware (src/tools.c:108-162). */
+/* Total energy, unsoftened, test-particle aware (src/tools.c:108-162), of the
+ * synchronized state; a WHFast run with safe_mode 0 keeps its unsynchronized
+ * coordinates, so the call does not change the trajectory. */
 int rgpu_energy(rgpu_sim* sim, double* energy);
 
 /* Wait for the simulation's stream; returns the first device error, if any. */

@@ -628,7 +628,16 @@ int rgpu_synchronize(rgpu_sim* s) {
 
 int rgpu_energy(rgpu_sim* s, double* e) {
     if (!s || !e) return RGPU_ERR_ARG;
-    if (s->cfg.integrator == RGPU_INTEGRATOR_WHFAST) RGPU_TRY(whfast_synchronize(s));
+    if (s->cfg.integrator == RGPU_INTEGRATOR_WHFAST && !s->whfast_synchronized) {
+        // the energy of the synchronized state; with safe_mode 0 the integrator keeps
+        // its unsynchronized coordinates (keep_unsynchronized), so asking for the
+        // energy does not change the trajectory
+        const int keep = s->cfg.whfast_keep_unsynchronized;
+        if (!s->cfg.whfast_safe_mode) s->cfg.whfast_keep_unsynchronized = 1;
+        const int rc = whfast_synchronize(s);
+        s->cfg.whfast_keep_unsynchronized = keep;
+        RGPU_TRY(rc);
+    }
     RGPU_TRY(direct_energy(s, e));
     return read_status(s);
 }

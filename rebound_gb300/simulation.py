@@ -223,7 +223,21 @@ class Simulation:
     def _pull(self):
         if self._device_newer:
             if self._cfg.integrator == _lib.INTEGRATOR["whfast"]:
-                check(self._L.rgpu_synchronize(self._h), self._h)
+                # A read shows synchronized values but leaves the integrator where it was,
+                # as reading sim.particles does in the reference: with safe_mode 0 the
+                # synchronize runs as keep_unsynchronized (src/integrator_whfast.c:1060-1104).
+                dev = Config()
+                check(self._L.rgpu_sim_get_config(self._h, ctypes.byref(dev)))
+                if dev.whfast_safe_mode == 0 and not dev.whfast_keep_unsynchronized:
+                    tmp = Config.from_buffer_copy(dev)
+                    tmp.whfast_keep_unsynchronized = 1
+                    check(self._L.rgpu_sim_configure(self._h, ctypes.byref(tmp)), self._h)
+                    try:
+                        check(self._L.rgpu_synchronize(self._h), self._h)
+                    finally:
+                        check(self._L.rgpu_sim_configure(self._h, ctypes.byref(dev)), self._h)
+                else:
+                    check(self._L.rgpu_synchronize(self._h), self._h)
             check(self._L.rgpu_sim_get_particles(self._h, self._host.ctypes.data, len(self._host),
                                                  PARTICLE_DTYPE.itemsize), self._h)
             self._device_newer = False

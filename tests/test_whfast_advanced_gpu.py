@@ -159,3 +159,23 @@ def test_configuration_errors(gpu, setting, msg):
         setattr(sim.ri_whfast, k, v)
     with pytest.raises(gpu.RGPUError, match=msg):
         sim.steps(1)
+
+
+@pytest.mark.parametrize("c", [0, 5])
+def test_reading_mid_run_does_not_change_the_trajectory(gpu, c):
+    # safe_mode 0: reading particles or the energy between steps shows synchronized
+    # values but the run continues exactly as without the reads (the reference's
+    # sim.particles does not synchronize)
+    g = golden("whfast_advanced.npz")
+    a = make(gpu, g, c, 0, "default", safe=False)
+    b = make(gpu, g, c, 0, "default", safe=False)
+    for _ in range(4):
+        a.steps(5)
+        b.steps(5)
+        pa = a.particles
+        a.energy()
+        assert np.all(np.isfinite(pa["x"]))
+    a.synchronize()
+    b.synchronize()
+    same(a.particles, b.particles)
+    same(b.particles, g["traj_c%d_c20_default" % c])
