@@ -474,6 +474,14 @@ int rgpu_sim_configure(rgpu_sim* s, const rgpu_config* c) {
     if (c->N_root_x < 1 || c->N_root_y < 1 || c->N_root_z < 1) return set_error(s, RGPU_ERR_ARG, "N_root must be >= 1");
     if (c->N_ghost_x < 0 || c->N_ghost_y < 0 || c->N_ghost_z < 0) return set_error(s, RGPU_ERR_ARG, "N_ghost must be >= 0");
     if (c->integrator < 0 || c->integrator > 2) return set_error(s, RGPU_ERR_ARG, "unknown integrator");
+    if (c->boundary < 0 || c->boundary > 3) return set_error(s, RGPU_ERR_ARG, "unknown boundary");
+    if (c->collision != RGPU_COLLISION_NONE && c->collision != RGPU_COLLISION_DIRECT &&
+        c->collision != RGPU_COLLISION_TREE && c->collision != RGPU_COLLISION_LINE &&
+        c->collision != RGPU_COLLISION_LINETREE)
+        return set_error(s, RGPU_ERR_UNSUPPORTED, "Collision routine not implemented.");
+    if (c->collision_resolve < RGPU_RESOLVE_HALT || c->collision_resolve > RGPU_RESOLVE_NONE)
+        return set_error(s, RGPU_ERR_UNSUPPORTED,
+                         "collision_resolve: halt, hardsphere or none (resolvers that remove particles are not on the GPU path)");
     const bool integrator_changed = c->integrator != s->cfg.integrator;
     s->cfg = *c;
     if (integrator_changed) { s->did_modify = true; s->whfast_synchronized = true; }
