@@ -1,6 +1,8 @@
-// WHFast (Wisdom-Holman, Jacobi coordinates, DEFAULT kernel, no correctors)
-// for one small system held by one thread: src/integrator_whfast.c and
-// src/transformations.c of REBOUND 5.0.0.
+// WHFast building blocks for one small system: the Kepler solver, the Jacobi
+// and democratic heliocentric transforms, kicks, jumps and the full safe_mode
+// steps the ensembles run (src/integrator_whfast.c and src/transformations.c of
+// REBOUND 5.0.0).  The plain path's program kernel (whfast_prog.cu) composes
+// them with the other coordinate systems, kernels and correctors.
 //
 // Each function restates the reference routine it names with the same
 // sequence of floating-point operations, so a translation unit compiled with

@@ -1,11 +1,14 @@
-// WHFast programs on an rgpu_sim: the plain one-simulation-per-call path with a
-// first symplectic corrector of order 3, 5, 7, 11 or 17, the second corrector, the
-// kernels MODIFIEDKICK, COMPOSITION and LAZY, or WHDS / barycentric coordinates
+// WHFast programs on an rgpu_sim: the plain one-simulation-per-call path in any
+// coordinate system (Jacobi, democratic heliocentric, WHDS, barycentric), with a
+// first symplectic corrector of order 3, 5, 7, 11 or 17, the second corrector and
+// the kernels DEFAULT, MODIFIEDKICK, COMPOSITION and LAZY
 // (src/integrator_whfast.c:653-785, 1113-1259; Wisdom, Holman & Touma 1996;
 // Wisdom 2006; Rein, Tamayo & Brown 2019).  The host lays each call out as a list
-// of operators in the reference's order; one thread runs the list.  Every
-// operator has a single call site in the interpreter loop, so the Kepler solver
-// is inlined once per body count however long the corrector is.  Compiled with
+// of operators in the reference's order; lane 0 of one warp runs the list and
+// the Kepler drifts take one body per lane.  Every operator has a single call
+// site in the interpreter loop, so the Kepler solver is inlined once per body
+// count however long the corrector is.  Every plain WHFast step and synchronize
+// runs here, the default configuration included.  Compiled with
 // --fmad=false: bit-identical to the reference's serial build.
 #include "whfast_plain.cuh"
 
