@@ -322,3 +322,47 @@ def test_oracle_line_searches(scene, mode):
     assert np.array_equal(got["gb"], ref["gb"])
     if mode == "linetree":
         assert np.array_equal(got["ri"], ref["ri"])
+
+
+def test_oracle_reference_unit_scenarios():
+    # the reference's own unit-test runs (rebound/tests/test_leapfrog.py:14-22,
+    # test_whfast.py:20-69, 307-345): the oracle reaches the reference's energy
+    # errors exactly and its forward-backward end states bit for bit
+    import math
+    g = golden("reference_cases.npz")
+
+    def rel(a, b):
+        return abs((a - b) / b)
+
+    s = O.Sim(g["oss"], dt=1.0)
+    e0 = s.energy()
+    s.leapfrog(1000)
+    assert rel(e0, s.energy()) == float(g["oss_leapfrog_err"])
+    for start, dt, tmax, key in (("oss_raw", 0.005 * 12. * 2. * 3.1415, 1000. * 2. * 3.1415, "oss_whfast_err"),
+                                 ("hyper", 0.00512 * float(g["hyper_yr"]), 1e2 * float(g["hyper_yr"]), "hyper_err"),
+                                 ("two", 0.005123 * 2. * math.pi, 1e3 * 2. * math.pi, "two_err")):
+        s = O.Sim(g[start], dt=dt)
+        e0 = s.energy()
+        s.whfast_integrate(tmax)
+        assert rel(e0, s.energy()) == float(g[key]), start
+    for name in ("bf_hyper", "bf_ecc"):
+        s = O.Sim(g[name], dt=float(g[name + "_dt"]))
+        s.whfast(100)
+        s.s.dt *= -1
+        s.whfast(100)
+        s.whfast_synchronize()
+        assert max_diff(s.p, g[name + "_end"]) == 0.0, name
+
+
+@pytest.mark.parametrize("coords,safe,corrector", [("jacobi", 0, 0), ("jacobi", 1, 0), ("jacobi", 0, 5),
+                                                   ("jacobi", 1, 5), ("democraticheliocentric", 0, 0),
+                                                   ("democraticheliocentric", 1, 0), ("whds", 0, 0),
+                                                   ("whds", 1, 0)])
+def test_oracle_archive_scenarios(coords, safe, corrector):
+    # the uninterrupted runs of rebound/tests/test_simulationarchive.py:86-365 to
+    # t = 80 with exact_finish_time = 0: the reference's end state and time
+    g = golden("archive_cases.npz")
+    tag = "%s_safe%d_c%d" % (coords, safe, corrector)
+    s = O.Sim(g["start"], dt=0.1313, safe_mode=safe, coordinates=coords, corrector=corrector)
+    s.whfast_integrate(80., exact_finish_time=0)
+    assert max_diff(s.p, g["end_" + tag]) == 0.0 and s.s.t == float(g["t_" + tag])
