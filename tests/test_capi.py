@@ -9,6 +9,7 @@ import os
 import re
 
 import numpy as np
+import pytest
 
 from conftest import REPO, golden
 
@@ -89,3 +90,27 @@ def test_no_gpu_create_fails_loudly():
         assert e.code == 2
     else:
         raise AssertionError("creating a simulation without a GPU must raise")
+
+
+def test_config_layout_matches_header(tmp_path):
+    # the ctypes mirror of rgpu_config must have the C header's size and field offsets
+    import shutil
+    import subprocess
+    from rebound_gb300._lib import Config
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    names = [f[0] for f in Config._fields_]
+    src = tmp_path / "layout.c"
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "rebound_gb300.h"', 'int main(void) {',
+             '  printf("size %zu\\n", sizeof(rgpu_config));']
+    lines += ['  printf("%s %%zu\\n", offsetof(rgpu_config, %s));' % (n, n) for n in names]
+    lines += ['  return 0;', '}']
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.check_call([cc, "-I", inc, str(src), "-o", str(exe)])
+    out = dict(line.split() for line in subprocess.check_output([str(exe)], text=True).splitlines())
+    assert int(out["size"]) == ctypes.sizeof(Config)
+    for n in names:
+        assert int(out[n]) == getattr(Config, n).offset, n
