@@ -92,25 +92,42 @@ def test_no_gpu_create_fails_loudly():
         raise AssertionError("creating a simulation without a GPU must raise")
 
 
-def test_config_layout_matches_header(tmp_path):
-    # the ctypes mirror of rgpu_config must have the C header's size and field offsets
+def _c_layout(tmp_path, struct, names):
+    """Size and field offsets of a struct of include/rebound_gb300.h, from a compiled probe."""
     import shutil
     import subprocess
-    from rebound_gb300._lib import Config
     cc = shutil.which("gcc") or shutil.which("cc")
     if cc is None:
         pytest.skip("no C compiler")
-    names = [f[0] for f in Config._fields_]
-    src = tmp_path / "layout.c"
+    src = tmp_path / ("%s.c" % struct)
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "rebound_gb300.h"', 'int main(void) {',
-             '  printf("size %zu\\n", sizeof(rgpu_config));']
-    lines += ['  printf("%s %%zu\\n", offsetof(rgpu_config, %s));' % (n, n) for n in names]
+             '  printf("size %%zu\\n", sizeof(%s));' % struct]
+    lines += ['  printf("%s %%zu\\n", offsetof(%s, %s));' % (n, struct, n) for n in names]
     lines += ['  return 0;', '}']
     src.write_text("\n".join(lines) + "\n")
-    exe = tmp_path / "layout"
+    exe = tmp_path / struct
     inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
     subprocess.check_call([cc, "-I", inc, str(src), "-o", str(exe)])
-    out = dict(line.split() for line in subprocess.check_output([str(exe)], text=True).splitlines())
-    assert int(out["size"]) == ctypes.sizeof(Config)
+    return {k: int(v) for k, v in (line.split() for line in subprocess.check_output([str(exe)], text=True).splitlines())}
+
+
+@pytest.mark.parametrize("struct", ["rgpu_config", "rgpu_server_config", "rgpu_server_stats"])
+def test_struct_layout_matches_header(tmp_path, struct):
+    # the ctypes mirrors must have the C header's size and field offsets
+    from rebound_gb300 import _lib
+    cls = {"rgpu_config": _lib.Config, "rgpu_server_config": _lib.ServerConfig,
+           "rgpu_server_stats": _lib.ServerStats}[struct]
+    names = [f[0] for f in cls._fields_]
+    out = _c_layout(tmp_path, struct, names)
+    assert out["size"] == ctypes.sizeof(cls)
     for n in names:
-        assert int(out[n]) == getattr(Config, n).offset, n
+        assert out[n] == getattr(cls, n).offset, n
+
+
+def test_collision_record_matches_header(tmp_path):
+    # the numpy record used for pair lists is struct rgpu_collision (and reb_collision)
+    from rebound_gb300._lib import COLLISION_DTYPE
+    out = _c_layout(tmp_path, "rgpu_collision", ["p1", "p2", "gb", "ri"])
+    assert out["size"] == COLLISION_DTYPE.itemsize
+    for n in ("p1", "p2", "gb", "ri"):
+        assert out[n] == COLLISION_DTYPE.fields[n][1], n
