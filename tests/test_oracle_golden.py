@@ -366,3 +366,27 @@ def test_oracle_archive_scenarios(coords, safe, corrector):
     s = O.Sim(g["start"], dt=0.1313, safe_mode=safe, coordinates=coords, corrector=corrector)
     s.whfast_integrate(80., exact_finish_time=0)
     assert max_diff(s.p, g["end_" + tag]) == 0.0 and s.s.t == float(g["t_" + tag])
+
+
+def test_oracle_sim_layout_matches_header(tmp_path):
+    # the checker's own ctypes mirror of orc_sim must match oracle/oracle.h
+    import ctypes
+    import os
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    names = [f[0] for f in O.OrcSim._fields_]
+    src = tmp_path / "orc.c"
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "oracle.h"', 'int main(void) {',
+             '  printf("size %zu\\n", sizeof(orc_sim));']
+    lines += ['  printf("%s %%zu\\n", offsetof(orc_sim, %s));' % (n, n) for n in names]
+    lines += ['  return 0;', '}']
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "orc"
+    subprocess.check_call([cc, "-I", os.path.dirname(os.path.abspath(O.__file__)), str(src), "-o", str(exe)])
+    out = {k: int(v) for k, v in (l.split() for l in subprocess.check_output([str(exe)], text=True).splitlines())}
+    assert out["size"] == ctypes.sizeof(O.OrcSim)
+    for n in names:
+        assert out[n] == getattr(O.OrcSim, n).offset, n
