@@ -123,13 +123,14 @@ def oracle_cpu_rate(particles, seconds=10.0, label="sample"):
     from oracle import oracle as O
     n = len(particles)
     s = O.Sim(particles, softening=SOFTENING)
+    T = O.lib_timing()
     rows = 512
     t0 = time.perf_counter()
-    O.lib().orc_gravity_basic_omp_rows(s.ref, 0, rows)
+    T.orc_gravity_basic_omp_rows(s.ref, 0, rows)
     dt = time.perf_counter() - t0
     rows = int(min(n, max(512, rows * seconds / max(dt, 1e-6))))
     t0 = time.perf_counter()
-    O.lib().orc_gravity_basic_omp_rows(s.ref, 0, rows)
+    T.orc_gravity_basic_omp_rows(s.ref, 0, rows)
     dt = time.perf_counter() - t0
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     return rows * (n - 1) / dt / 1e9, cores, f"{rows} of {n} i-rows x {n} j-bodies, FP64 BASIC gather ({dt:.1f} s)"
@@ -152,7 +153,7 @@ def run_reference(args):
     # Inputs from the reference's own Plummer construction (restated in the oracle harness).
     p = plummer_oracle(args.n)
     s = O.Sim(p, softening=SOFTENING)
-    L = O.lib()
+    L = O.lib_timing()
     n = args.n
     rows = 256
     t0 = time.perf_counter()
@@ -243,19 +244,19 @@ def run_gb300(args):
     ms_step = total_ms / args.steps
     kernel_ms = kms.value / max(1, kn.value)
 
-    # FP64 pipe peak measured live (DFMA lane-ops/s x 2 flops).
+    # FP64 pipe: nominal issue rate at the sampled clock, and the live DFMA probe
+    # (lane-ops/s x 2 flops); FP32 and integer-ALU probes.
     rate = ctypes.c_double(0.)
     L.rgpu_probe_rate(0, ctypes.byref(rate))
-    fp64_peak = 2 * rate.value / 1e12
+    fp64_probe = 2 * rate.value / 1e12
     L.rgpu_probe_rate(1, ctypes.byref(rate))
     fp32_peak = 2 * rate.value / 1e12
     L.rgpu_probe_rate(4, ctypes.byref(rate))
     alu_peak = rate.value / 1e12
+    sm_count = torch.cuda.get_device_properties(local).multi_processor_count
+    fp64_nominal = nominal_fp64_tflops(sm_count, (clk or {}).get("sm_mhz"))
     pair_rate = pairs / (kernel_ms * 1e-3)
-    prof = profiled_counts()
-    traffic = prof.get("traffic_bytes_per_launch")
-    alu_ipp = prof.get("alu_inst_per_pair")
-    fp64_ipp = prof.get("fp64_inst_per_pair")
+    counts = profiled_counts()
     fp64_equiv = FLOPS_PER_PAIR * pair_rate / 1e12
 
     # Accuracy and speed of the other forms (force evaluation at step 0).
@@ -313,6 +314,14 @@ def run_gb300(args):
            "h2d_bytes_per_step": n * 112, "d2h_bytes_per_step": n * 88}
 
     extra = {}
+    if args.precision and rank == 0 and not args.lite:
+        for key, fn in (("c1", lambda: c1_summary(cpu_seconds=2.0 if args.quick else 8.0)),
+                        ("c2_drift", lambda: c2_drift_summary(steps=10 if args.quick else 100)),
+                        ("c5_cluster_drift", lambda: c5_cluster_drift(steps=200 if args.quick else 1000))):
+            try:
+                extra[key] = fn()
+            except Exception as ex:
+                extra[key] = {"error": repr(ex)}
     if args.ensemble and rank == 0 and not args.lite:
         try:
             from rebound_gb300 import ensemble as E
@@ -341,8 +350,8 @@ def run_gb300(args):
                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Plummer sphere)",
                "config": config_block(n, world),
                "e2e": e2e, "gpu_launches": int(launches),
-               "roofline": roofline_block(alu_ipp, fp64_ipp, pair_rate, alu_peak, fp64_peak, fp32_peak,
-                                          fp64_equiv, traffic, kernel_ms),
+               "roofline": roofline_block(counts, pair_rate, alu_peak, fp64_probe, fp64_nominal, fp32_peak,
+                                          fp64_equiv, kernel_ms),
                "forms": forms,
                "cpu_baseline": {"value": cpu_val, "unit": "Gpair-int/s", "cores": cores, "kind": "port",
                                 "sample": sample},
@@ -429,7 +438,7 @@ def tree_summary(quick=False, steps=2):
                 N_ghost=(2, 2, 0), OMEGA=omega, opening_angle2=0.25)
     rows = 64 if quick else 256
     t0 = time.perf_counter()
-    O.lib().orc_gravity_tree_rows(orc.ref, 0, rows)
+    O.lib_timing().orc_gravity_tree_rows(orc.ref, 0, rows)
     cpu_rows_s = time.perf_counter() - t0
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     cpu_grav_step_s = cpu_rows_s / rows * len(p)
@@ -444,6 +453,85 @@ def tree_summary(quick=False, steps=2):
                              "sample": f"{rows} of {len(p)} particles walked (oracle tree, OpenMP), scaled to N"},
             "gravity_speedup_vs_cpu": cpu_grav_step_s / grav_s,
             "split_gravity_speedup_vs_cpu": cpu_grav_step_s / split_s}
+
+
+def form_drift(p, softening, dt, steps, forms=("basic", "compensated", "mixed", "mixed_split")):
+    """Each force form integrated `steps` leapfrog steps from the same state:
+    relative energy error (REBOUND's unsoftened energy, src/tools.c:108-162),
+    device time per step, and for the mixed forms the final energy against the
+    FP64 BASIC run's."""
+    import rebound_gb300 as R
+    L = R.load()
+    out, e_final, e0 = {}, {}, None
+    for form in forms:
+        sim = R.Simulation()
+        sim.softening, sim.dt, sim.gravity, sim.integrator = softening, dt, form, "leapfrog"
+        sim.add(p)
+        e_start = sim.energy()
+        e0 = e_start if e0 is None else e0
+        h = sim.handle
+        ms = ctypes.c_double(0.)
+        R._lib.check(L.rgpu_sim_time_steps(h, steps, ctypes.byref(ms)), h)
+        e1 = sim.energy()
+        e_final[form] = e1
+        n = len(p)
+        out[form] = {"energy_rel_err": abs((e1 - e_start) / e_start), "ms_per_step": ms.value / steps,
+                     "gpair_per_s": n * (n - 1.0) * steps / (ms.value * 1e-3) / 1e9}
+        del sim
+    for form in forms:
+        if form.startswith("mixed") and "basic" in e_final:
+            out[form]["energy_vs_fp64"] = abs(e_final[form] - e_final["basic"]) / abs(e0)
+    return out
+
+
+def c1_summary(cpu_seconds=10.0):
+    """Configuration 1: Plummer N = 4,096, softening 0.01, leapfrog dt = 1e-3,
+    1,000 steps.  GPU forms with their energy errors; the CPU baseline is the
+    oracle's port of the reference's OpenMP BASIC leapfrog on every host core,
+    run over all 1,000 steps when that fits `cpu_seconds`, else over a prefix."""
+    import rebound_gb300 as R
+    from oracle import oracle as O
+    n, soft, dt, steps = 4096, 0.01, 1e-3, 1000
+    p = R.ics.plummer(n, seed=SEED)
+    forms = form_drift(p, soft, dt, steps)
+    T = O.lib_timing()
+    s = O.Sim(p, softening=soft, dt=dt)
+    e0 = T.orc_energy(s.ref)
+    t0 = time.perf_counter()
+    T.orc_leapfrog_step_order(s.ref, O.GRAVITY["basic_omp"], 2)
+    one = time.perf_counter() - t0
+    cpu_steps = int(max(1, min(steps - 1, cpu_seconds / max(one, 1e-6)))) + 1
+    t0 = time.perf_counter()
+    for _ in range(cpu_steps - 1):
+        T.orc_leapfrog_step_order(s.ref, O.GRAVITY["basic_omp"], 2)
+    el = one + time.perf_counter() - t0
+    cpu = {"s_per_step": el / cpu_steps, "steps": cpu_steps, "cores": os.cpu_count() or 1, "kind": "port",
+           "gpair_per_s": n * (n - 1.0) * cpu_steps / el / 1e9}
+    if cpu_steps == steps:
+        cpu["energy_rel_err"] = abs((T.orc_energy(s.ref) - e0) / e0)
+    gpu_s = forms["basic"]["ms_per_step"] * 1e-3
+    return {"workload": f"Plummer N={n}, softening {soft}, leapfrog dt={dt}, {steps} steps", "forms": forms,
+            "cpu_baseline": cpu, "basic_speedup_vs_cpu": cpu["s_per_step"] / gpu_s}
+
+
+def c2_drift_summary(steps=100):
+    """Configuration 2 over its 100 steps: energy error of FP64 BASIC, COMPENSATED
+    and the mixed forms from the same Plummer N = 262,144 state."""
+    import rebound_gb300 as R
+    p = R.ics.plummer(N_DEFAULT, seed=SEED)
+    return {"workload": f"Plummer N={N_DEFAULT}, softening {SOFTENING}, leapfrog dt={DT}, {steps} steps",
+            "forms": form_drift(p, SOFTENING, DT, steps, forms=("basic", "mixed", "mixed_split"))}
+
+
+def c5_cluster_drift(steps=1000):
+    """Served-stream clusters (Plummer, N in [256, 8192], softening 0.01, leapfrog
+    dt = 1e-3) under the mixed forms against FP64 BASIC."""
+    import rebound_gb300 as R
+    out = {}
+    for n in (256, 1024, 4096, 8192):
+        p = R.ics.plummer(n, seed=1000 + n)
+        out[str(n)] = form_drift(p, 0.01, 1e-3, steps, forms=("basic", "mixed", "mixed_split"))
+    return {"steps": steps, "clusters": out}
 
 
 def ensemble_only(args):
@@ -468,7 +556,7 @@ def ensemble_cpu_baseline(seconds=8.0, seed=3, steps=10000):
     from oracle import oracle as O
     from rebound_gb300 import ics
     O.build()
-    L = O.lib()
+    L = O.lib_timing()
     cores = os.cpu_count() or 1
     probe = 2 * cores
     systems, periods = ics.planetary_systems(probe, seed=seed)
@@ -489,51 +577,85 @@ def ensemble_cpu_baseline(seconds=8.0, seed=3, steps=10000):
                       f"one thread per core ({el:.1f} s)"}
 
 
+COUNTS_FILE = os.path.join(REPO, "profiles", "direct_kernel_counts.json")
+
+
+def sources_digest(paths):
+    import hashlib
+    h = hashlib.sha256()
+    for rel in paths:
+        with open(os.path.join(REPO, rel), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()
+
+
 def profiled_counts():
     """Per-launch DRAM bytes and per-pair instruction counts of the dominant kernel,
-    from the committed ncu summary (key: value lines)."""
-    path = os.path.join(REPO, "profiles", "direct_basic_fp64.md")
-    out = {}
+    measured by ncu and recorded with the SHA-256 of the kernel's sources.  When the
+    sources have changed since the capture the counts no longer describe the kernel:
+    every count is then None and `stale` says so."""
     try:
-        for line in open(path):
-            k, sep, v = line.partition(":")
-            if sep and k in ("traffic_bytes_per_launch", "alu_inst_per_pair", "inst_per_pair", "fp64_inst_per_pair"):
-                out[k] = float(v)
-    except OSError:
-        pass
-    return out
+        with open(COUNTS_FILE) as f:
+            rec = json.load(f)
+    except (OSError, ValueError):
+        return {"stale": "no counts file"}
+    if sources_digest(rec["sources"]) != rec["sha256"]:
+        return {"stale": "kernel sources changed since the ncu capture (sha256 mismatch)"}
+    return {k: rec.get(k) for k in ("traffic_bytes_per_launch", "alu_inst_per_pair", "inst_per_pair",
+                                    "fp64_inst_per_pair")}
 
 
-def roofline_block(alu_ipp, fp64_ipp, pair_rate, alu_peak, fp64_peak, fp32_peak, fp64_equiv, traffic, kernel_ms):
+# FP64 pipe issue rate of GB300 (ncu's peak for sm__pipe_fp64_cycles_active):
+# 0.5 lanes per clock per SM sub-partition, 4 sub-partitions per SM.
+FP64_LANES_PER_CLK_PER_SMSP = 0.5
+
+
+def nominal_fp64_tflops(sm_count, sm_mhz):
+    """DFMA-equivalent TFLOP/s of the FP64 pipe at the sampled SM clock."""
+    if not sm_count or not sm_mhz:
+        return None
+    return 2 * FP64_LANES_PER_CLK_PER_SMSP * 4 * sm_count * sm_mhz * 1e6 / 1e12
+
+
+def roofline_block(counts, pair_rate, alu_peak, fp64_probe, fp64_nominal, fp32_peak, fp64_equiv, kernel_ms):
     """Roofline of the FP64 pair kernel against the pipe that binds it.  The kernel
-    issues fp64_ipp FP64 instructions and alu_ipp integer-ALU instructions per pair
-    (ncu counts, size-independent); each pipe's achieved rate is that count times the
-    live pair rate, against its live probe (rgpu_probe_rate 0 and 4).  FP64 rates are
-    in DFMA-equivalent TFLOP/s (2 flops per pipe instruction).  The plain-FP64 view
-    (20 flops per pair at the DFMA peak) rides alongside."""
+    issues fp64_inst_per_pair FP64 instructions and alu_inst_per_pair integer-ALU
+    instructions per pair (ncu counts, size-independent, valid only while the
+    kernel's sources hash to the recorded digest); each pipe's achieved rate is that
+    count times the live pair rate.  The FP64 pipe's peak is its nominal issue rate
+    at the sampled clock (0.5 lanes/clock/SMSP x 4 x SMs); the live DFMA probe
+    (rgpu_probe_rate 0) sustains less and is reported beside it.  FP64 rates are
+    DFMA-equivalent TFLOP/s (2 flops per pipe instruction).  The plain-FP64 view
+    (20 flops per pair at the FP64 peak) rides alongside."""
+    fp64_ipp, alu_ipp = counts.get("fp64_inst_per_pair"), counts.get("alu_inst_per_pair")
+    traffic = counts.get("traffic_bytes_per_launch")
     pipes = {}
+    fp64_peak = fp64_nominal or fp64_probe
     if fp64_ipp and fp64_peak:
         a = 2 * fp64_ipp * pair_rate / 1e12
         pipes["fp64"] = {"achieved": a, "peak": fp64_peak, "unit": "TFLOP/s (DFMA-equivalent)",
                          "frac": a / fp64_peak, "inst_per_pair": fp64_ipp,
-                         "peak_source": "live DFMA probe (rgpu_probe_rate 0); measured-peaks file has no FP64 figure"}
+                         "peak_source": ("nominal FP64 pipe rate at the sampled SM clock" if fp64_nominal else
+                                         "live DFMA probe (no clock sample)"),
+                         "probe_peak": fp64_probe, "frac_of_probe": a / fp64_probe if fp64_probe else None}
     if alu_ipp and alu_peak:
         a = alu_ipp * pair_rate / 1e12
         pipes["alu"] = {"achieved": a, "peak": alu_peak, "unit": "Tinst/s (integer ALU lane-ops)",
                         "frac": a / alu_peak, "inst_per_pair": alu_ipp,
                         "peak_source": "live integer-ALU probe (rgpu_probe_rate 4)"}
     plain = {"flops_per_pair": FLOPS_PER_PAIR, "equivalent_tflops": fp64_equiv, "fp64_peak_tflops": fp64_peak,
-             "equivalent_over_peak": fp64_equiv / fp64_peak if fp64_peak else None}
+             "equivalent_over_peak": fp64_equiv / fp64_peak if fp64_peak else None,
+             "fp64_probe_tflops": fp64_probe}
+    kernel = "direct_kernel<BASIC> (int64 fixed-point pair, FP64 accumulate)"
     if not pipes:
-        return {"bound": "fp64", "achieved": fp64_equiv, "peak": fp64_peak, "unit": "TFLOP/s",
-                "frac": fp64_equiv / fp64_peak if fp64_peak else None, "traffic": traffic,
-                "kernel": "direct_kernel<BASIC>", "kernel_ms": kernel_ms, "plain_fp64_view": plain}
+        return {"bound": "fp64", "achieved": None, "peak": fp64_peak, "unit": "TFLOP/s", "frac": None,
+                "traffic": traffic, "kernel": kernel, "kernel_ms": kernel_ms, "pair_rate_per_s": pair_rate,
+                "counts": counts.get("stale", "missing"), "plain_fp64_view": plain, "fp32_peak_tflops": fp32_peak}
     bound = max(pipes, key=lambda k: pipes[k]["frac"])
     b = pipes[bound]
     return {"bound": bound, "achieved": b["achieved"], "peak": b["peak"], "unit": b["unit"], "frac": b["frac"],
-            "traffic": traffic, "kernel": "direct_kernel<BASIC> (int64 fixed-point pair, FP64 accumulate)",
-            "kernel_ms": kernel_ms, "pair_rate_per_s": pair_rate, "pipes": pipes, "plain_fp64_view": plain,
-            "fp32_peak_tflops": fp32_peak}
+            "traffic": traffic, "kernel": kernel, "kernel_ms": kernel_ms, "pair_rate_per_s": pair_rate,
+            "pipes": pipes, "plain_fp64_view": plain, "fp32_peak_tflops": fp32_peak}
 
 
 def main():
@@ -548,6 +670,8 @@ def main():
     ap.add_argument("--no-ensemble", dest="ensemble", action="store_false")
     ap.add_argument("--no-serve", dest="serve", action="store_false")
     ap.add_argument("--no-tree", dest="tree", action="store_false")
+    ap.add_argument("--no-precision", dest="precision", action="store_false",
+                    help="skip configuration 1 and the energy drift of every form (configurations 1, 2, 5)")
     ap.add_argument("--quick", action="store_true")
     ap.add_argument("--only", choices=["tree", "ensemble", "serve"], default=None,
                     help="run one secondary workload alone and print its summary")

@@ -93,6 +93,8 @@ typedef struct rgpu_config {
     int32_t exact_finish_time;  /* src/rebound.h: 1 (default) lands integrate exactly on tmax */
     int32_t tree_quadrupole;    /* 1: tree cells carry mass quadrupoles, as the reference built with
                                    -DQUADRUPOLE (src/tree.c:147-320, src/Makefile.defs:90-91) */
+    double collisions_plog;     /* src/rebound.h:346: y-momentum transferred by hardsphere collisions
+                                   (src/collision.c:655-662), accumulated by the resolve */
 } rgpu_config;
 
 /* One overlapping, approaching pair: same layout as struct reb_collision
@@ -114,10 +116,20 @@ int  rgpu_sim_create(rgpu_sim** out);
 void rgpu_sim_free(rgpu_sim* sim);
 const char* rgpu_sim_last_error(const rgpu_sim* sim);
 
-/* Set / read the hot-path configuration (t, status, rand_seed and
- * collisions_log_n are updated by the steppers). */
+/* Set / read the hot-path configuration (t, status, rand_seed,
+ * collisions_log_n and collisions_plog are updated by the steppers). */
 int rgpu_sim_configure(rgpu_sim* sim, const rgpu_config* cfg);
 int rgpu_sim_get_config(const rgpu_sim* sim, rgpu_config* cfg);
+/* Velocity-dependent coefficient of restitution for the hardsphere resolve:
+ * fn(user, v) is called on the host for each resolved pair with the normal
+ * relative velocity v, as REBOUND calls r->coefficient_of_restitution(r, v)
+ * (src/collision.c:603-606); fn == NULL restores the constant
+ * cfg.coefficient_of_restitution. */
+int rgpu_sim_set_restitution_fn(rgpu_sim* sim, double (*fn)(void* user, double v), void* user);
+/* Host wall time spent in the collision resolve stage (shuffle, gather of the
+ * touched particles, hardsphere, scatter) since the handle was created, and the
+ * number of resolves.  No reference counterpart (diagnostic). */
+int rgpu_sim_resolve_time(rgpu_sim* sim, double* ms, int64_t* calls);
 
 /* Upload / download particles.  `particles` points at N records of `stride`
  * bytes whose first 11 doubles are x,y,z,vx,vy,vz,ax,ay,az,m,r -- the layout of
@@ -219,8 +231,19 @@ int rgpu_set_kernel_variant(int rinv_variant, int mixed_cvt);
  * and (r^2+eps^2)^(-3/2) on the integer pipes, FP64 for G m f and the sums;
  * 1 = fixed-point displacement (equal to the FP64 subtraction for coordinates
  * >= 2^-8 of the largest) with FP64 r^2 and m/r^3; 0 = FP64 throughout.
- * No reference counterpart (tuning only). */
+ * In modes 1 and 2 BASIC and COMPENSATED keep the FP64 result on every input:
+ * an exactness guard bounds, per particle, the force error that rounding
+ * smaller coordinates onto the fixed-point grid can cause, and recomputes in
+ * FP64 (the FP64 subtraction) every particle whose bound exceeds 5e-15 of its
+ * force -- or every particle, when more than a quarter of the bodies are off
+ * the grid.  No reference counterpart (tuning only). */
 int rgpu_set_displacement_mode(int mode);
+/* Counters of the exactness guard from the handle's last BASIC/COMPENSATED
+ * fixed-point evaluation (synchronises the handle's stream): bodies with a
+ * coordinate off the fixed-point grid, and particles recomputed in FP64
+ * (N when all were).  Both -1 before the first such evaluation.
+ * No reference counterpart (diagnostic). */
+int rgpu_sim_guard_stats(rgpu_sim* sim, int64_t* n_inexact, int64_t* n_redo);
 /* Count of this library's kernel launches since load. */
 int64_t rgpu_launch_count(void);
 /* Measured sustained lane-operation rate (ops/s) of one instruction class on
@@ -254,8 +277,11 @@ int rgpu_kepler_solve(const void* bodies, size_t stride, const double* mu, const
  * Scratch lives in a fixed 10 MiB device array inside the library (held by
  * every GPU that loads it until exit): n <= 65,536, else RGPU_ERR_CAPACITY.
  * The first call on each device looks up that array's address with the device
- * current; make it before any stream capture.  Calls share the array: calls
- * that overlap on the GPU race and must be serialised by the caller. */
+ * current; make it before any stream capture.  The address is kept for the life
+ * of the process, so a cudaDeviceReset (or any teardown of the device's primary
+ * context) invalidates it: do not call this entry point after one.  Calls share
+ * the array: calls that overlap on the GPU race and must be serialised by the
+ * caller. */
 int rgpu_direct_accel_noalloc(const double* x, const double* y, const double* z, const double* m,
                               double* ax, double* ay, double* az, int64_t n, double G, double softening,
                               int gravity, void* stream);
@@ -278,10 +304,21 @@ void rgpu_ensemble_free(rgpu_ensemble* ens);
 const char* rgpu_ensemble_last_error(const rgpu_ensemble* ens);
 /* CTA size (32/64/128) of the persistent grid and steps fused per kernel launch. */
 int  rgpu_ensemble_set_launch(rgpu_ensemble* ens, int block, int64_t steps_per_launch);
+/* How systems map onto threads: RGPU_ENSEMBLE_THREAD (one thread advances one
+ * system; the throughput mapping for many systems) or RGPU_ENSEMBLE_WARP (one warp
+ * per system, lane i holding body i; the latency mapping, FMA flavour only).
+ * No reference counterpart (the reference runs one simulation per call). */
+enum { RGPU_ENSEMBLE_THREAD = 0, RGPU_ENSEMBLE_WARP = 1 };
+int  rgpu_ensemble_set_mapping(rgpu_ensemble* ens, int mapping);
+/* The mapping, CTA size and steps per launch in effect (after an autotune). */
+int  rgpu_ensemble_get_launch(const rgpu_ensemble* ens, int* mapping, int* block, int64_t* steps_per_launch);
 /* Advance every system by n steps (CUDA-graph replays of fused chunks). */
 int  rgpu_ensemble_steps(rgpu_ensemble* ens, int64_t n);
 int  rgpu_ensemble_time_steps(rgpu_ensemble* ens, int64_t n, double* ms);
-/* Time probe_steps for each CTA size, keep the fastest; set steps per launch. */
+/* Autotuner on the live ensemble (its probe steps advance the state): times
+ * every mapping x CTA size over probe_steps, then max_steps_per_launch / 16, / 4
+ * and itself as steps per launch, and keeps the fastest combination (read it
+ * back with rgpu_ensemble_get_launch). */
 int  rgpu_ensemble_autotune(rgpu_ensemble* ens, int64_t probe_steps, int64_t max_steps_per_launch,
                             int* best_block, double* best_ms_per_step);
 /* Write positions, velocities and masses back into the caller's records. */

@@ -515,9 +515,14 @@ int orc_tree_export(orc_sim* r, orc_cell* out, size_t cap, size_t* n_out) {
  * Collision search: src/collision.c:49-124 (DIRECT), :197-269 and :422-503
  * (TREE).  Pairs are emitted in discovery order; the caller sorts.
  * ---------------------------------------------------------------------- */
-typedef struct pairbuf { orc_collision* out; size_t cap, n; } pairbuf;
+typedef struct pairbuf { orc_collision* out; size_t cap, n; int grow; } pairbuf;
 
 static void pair_push(pairbuf* b, size_t p1, size_t p2, const double gb[6], size_t ri) {
+    if (b->grow && b->n == b->cap) {            /* growable per-thread buffers of the OpenMP search */
+        const size_t nc = b->cap ? 2 * b->cap : 1024;
+        orc_collision* o = (orc_collision*)realloc(b->out, nc * sizeof(orc_collision));
+        if (o) { b->out = o; b->cap = nc; }
+    }
     if (b->n < b->cap) {
         orc_collision* c = &b->out[b->n];
         c->p1 = p1; c->p2 = p2; c->ri = ri;
@@ -615,6 +620,60 @@ size_t orc_collision_search_tree(orc_sim* r, orc_collision* out, size_t cap) {
     }
     tree_free(&t);
     return b.n;
+}
+
+/* The same search with the particle loop split over OpenMP threads: thread t
+ * takes a contiguous block of particles in increasing order and collects its
+ * pairs in its own buffer, and the buffers are joined in thread order, so the
+ * list (and its order) equals the serial search above. */
+size_t orc_collision_search_tree_omp(orc_sim* r, orc_collision* out, size_t cap) {
+    otree t = {0};
+    if (tree_build(r, &t)) { tree_free(&t); return 0; }
+    const int nx = r->N_ghost_x > 1 ? 1 : r->N_ghost_x;
+    const int ny = r->N_ghost_y > 1 ? 1 : r->N_ghost_y;
+    const int nz = r->N_ghost_z > 1 ? 1 : r->N_ghost_z;
+    const double r2nd = second_largest_radius(r);
+    const orc_particle* P = r->particles;
+    int nt = 1;
+#ifdef _OPENMP
+    nt = omp_get_max_threads();
+#endif
+    pairbuf* bufs = (pairbuf*)calloc((size_t)nt, sizeof(pairbuf));
+    if (!bufs) { tree_free(&t); return 0; }
+#pragma omp parallel num_threads(nt)
+    {
+        int th = 0, T = 1;
+#ifdef _OPENMP
+        th = omp_get_thread_num();
+        T = omp_get_num_threads();
+#endif
+        pairbuf* b = &bufs[th];
+        b->grow = 1;
+        const size_t lo = r->N * (size_t)th / (size_t)T, hi = r->N * (size_t)(th + 1) / (size_t)T;
+        for (size_t i = lo; i < hi; i++) {
+            const orc_particle p1 = P[i];
+            for (int gx = -nx; gx <= nx; gx++)
+            for (int gy = -ny; gy <= ny; gy++)
+            for (int gz = -nz; gz <= nz; gz++) {
+                double g0[6], s[6];
+                orc_boundary_ghostbox(r, gx, gy, gz, g0);
+                s[0] = g0[0] + p1.x; s[1] = g0[1] + p1.y; s[2] = g0[2] + p1.z;
+                s[3] = g0[3] + p1.vx; s[4] = g0[4] + p1.vy; s[5] = g0[5] + p1.vz;
+                for (size_t k = 0; k < t.n_root; k++)
+                    if (t.root[k]) tree_nn(r, s, g0, (int)k, p1.r, r2nd, i, t.root[k], b);
+            }
+        }
+    }
+    size_t n = 0;
+    for (int th = 0; th < nt; th++) {
+        for (size_t k = 0; k < bufs[th].n && k < bufs[th].cap; k++)
+            if (n + k < cap) out[n + k] = bufs[th].out[k];
+        n += bufs[th].n;
+        free(bufs[th].out);
+    }
+    free(bufs);
+    tree_free(&t);
+    return n;
 }
 
 /* Do two straight paths over the last step (relative position d at its end,

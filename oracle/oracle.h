@@ -99,6 +99,7 @@ void orc_boundary_ghostbox(const orc_sim* r, int i, int j, int k, double gb[6]);
  * (which may exceed cap; only cap are written). */
 size_t orc_collision_search_direct(orc_sim* r, orc_collision* out, size_t cap);
 size_t orc_collision_search_tree(orc_sim* r, orc_collision* out, size_t cap);
+size_t orc_collision_search_tree_omp(orc_sim* r, orc_collision* out, size_t cap);
 size_t orc_collision_search_line(orc_sim* r, double dt_last_done, orc_collision* out, size_t cap);
 size_t orc_collision_search_linetree(orc_sim* r, double dt_last_done, orc_collision* out, size_t cap);
 

@@ -59,60 +59,88 @@ def _elf_matches_host(path):
     return head[:4] == b"\x7fELF" and want is not None and int.from_bytes(head[18:20], "little") == want
 
 
-def build(force=False):
-    """Compile oracle.c into liboracle.so (serial + OpenMP, no FP contraction)."""
+# Timing build: the compiler's default floating-point contraction (FMA where the
+# target has it), as the reference's own OpenMP build is compiled.  Used only for
+# the CPU-baseline timings; every parity check uses LIB (no contraction).
+LIB_TIMING = os.path.join(HERE, "liboracle_timing.so")
+
+
+def _build_one(out, contract_off, force):
     src = os.path.join(HERE, "oracle.c")
     hdr = os.path.join(HERE, "oracle.h")
-    if not force and _elf_matches_host(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(src), os.path.getmtime(hdr)):
-        return LIB
+    if not force and _elf_matches_host(out) and os.path.getmtime(out) >= max(os.path.getmtime(src), os.path.getmtime(hdr)):
+        return out
     cc = os.environ.get("CC", "gcc")
-    cmd = [cc, "-std=gnu99", "-O3", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp",
-           "-D_GNU_SOURCE", src, "-o", LIB + ".tmp", "-lm"]
+    cmd = [cc, "-std=gnu99", "-O3", "-fPIC", "-shared"] + (["-ffp-contract=off"] if contract_off else []) + [
+        "-fopenmp", "-D_GNU_SOURCE", src, "-o", out + ".tmp", "-lm"]
     subprocess.check_call(cmd)
-    os.replace(LIB + ".tmp", LIB)
-    return LIB
+    os.replace(out + ".tmp", out)
+    return out
+
+
+def build(force=False):
+    """Compile oracle.c into liboracle.so (serial + OpenMP, no FP contraction: the
+    parity build) and liboracle_timing.so (default contraction: the CPU-baseline build)."""
+    _build_one(LIB_TIMING, False, force)
+    return _build_one(LIB, True, force)
 
 
 _lib = None
+_lib_timing = None
+
+
+def lib_timing():
+    """The oracle compiled with default contraction, for CPU-baseline timing only."""
+    global _lib_timing
+    if _lib_timing is None:
+        build()
+        _lib_timing = _bind(ctypes.CDLL(LIB_TIMING))
+    return _lib_timing
 
 
 def lib():
     global _lib
     if _lib is None:
         build()
-        L = ctypes.CDLL(LIB)
-        P = ctypes.POINTER(OrcSim)
-        for name in ("orc_gravity_basic_serial", "orc_gravity_basic_omp", "orc_gravity_compensated_serial",
-                     "orc_gravity_compensated_omp", "orc_gravity_tree", "orc_boundary_check",
-                     "orc_whfast_step", "orc_whfast_synchronize"):
-            getattr(L, name).argtypes = [P]
-            getattr(L, name).restype = None
-        L.orc_gravity_basic_omp_rows.argtypes = [P, ctypes.c_size_t, ctypes.c_size_t]
-        L.orc_gravity_compensated_omp_rows.argtypes = [P, ctypes.c_size_t, ctypes.c_size_t]
-        L.orc_gravity_tree_rows.argtypes = [P, ctypes.c_size_t, ctypes.c_size_t]
-        L.orc_whfast_steps.argtypes = [P, ctypes.c_long]
-        L.orc_whfast_steps.restype = None
-        L.orc_leapfrog_step.argtypes = [P, ctypes.c_int]
-        L.orc_leapfrog_step_order.argtypes = [P, ctypes.c_int, ctypes.c_int]
-        L.orc_leapfrog_step_order.restype = ctypes.c_int
-        L.orc_sei_step.argtypes = [P, ctypes.c_int]
-        L.orc_collision_search_direct.argtypes = [P, ctypes.c_void_p, ctypes.c_size_t]
-        L.orc_collision_search_direct.restype = ctypes.c_size_t
-        L.orc_collision_search_tree.argtypes = [P, ctypes.c_void_p, ctypes.c_size_t]
-        L.orc_collision_search_tree.restype = ctypes.c_size_t
-        for name in ("orc_collision_search_line", "orc_collision_search_linetree"):
-            getattr(L, name).argtypes = [P, ctypes.c_double, ctypes.c_void_p, ctypes.c_size_t]
-            getattr(L, name).restype = ctypes.c_size_t
-        L.orc_tree_export.argtypes = [P, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
-        L.orc_tree_export.restype = ctypes.c_int
-        L.orc_energy.argtypes = [P]
-        L.orc_energy.restype = ctypes.c_double
-        L.orc_whfast_kepler_solver.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double]
-        L.orc_ic_plummer.argtypes = [ctypes.c_uint, ctypes.c_size_t, ctypes.c_double, ctypes.c_double,
-                                     ctypes.c_double, ctypes.c_void_p]
-        L.orc_collision_resolve_hardsphere.argtypes = [P, ctypes.c_void_p, ctypes.c_double, ctypes.c_double]
-        _lib = L
+        _lib = _bind(ctypes.CDLL(LIB))
     return _lib
+
+
+def _bind(L):
+    """Argument and result types of the oracle's entry points."""
+    P = ctypes.POINTER(OrcSim)
+    for name in ("orc_gravity_basic_serial", "orc_gravity_basic_omp", "orc_gravity_compensated_serial",
+                 "orc_gravity_compensated_omp", "orc_gravity_tree", "orc_boundary_check",
+                 "orc_whfast_step", "orc_whfast_synchronize"):
+        getattr(L, name).argtypes = [P]
+        getattr(L, name).restype = None
+    L.orc_gravity_basic_omp_rows.argtypes = [P, ctypes.c_size_t, ctypes.c_size_t]
+    L.orc_gravity_compensated_omp_rows.argtypes = [P, ctypes.c_size_t, ctypes.c_size_t]
+    L.orc_gravity_tree_rows.argtypes = [P, ctypes.c_size_t, ctypes.c_size_t]
+    L.orc_whfast_steps.argtypes = [P, ctypes.c_long]
+    L.orc_whfast_steps.restype = None
+    L.orc_leapfrog_step.argtypes = [P, ctypes.c_int]
+    L.orc_leapfrog_step_order.argtypes = [P, ctypes.c_int, ctypes.c_int]
+    L.orc_leapfrog_step_order.restype = ctypes.c_int
+    L.orc_sei_step.argtypes = [P, ctypes.c_int]
+    L.orc_collision_search_direct.argtypes = [P, ctypes.c_void_p, ctypes.c_size_t]
+    L.orc_collision_search_direct.restype = ctypes.c_size_t
+    L.orc_collision_search_tree.argtypes = [P, ctypes.c_void_p, ctypes.c_size_t]
+    L.orc_collision_search_tree.restype = ctypes.c_size_t
+    L.orc_collision_search_tree_omp.argtypes = [P, ctypes.c_void_p, ctypes.c_size_t]
+    L.orc_collision_search_tree_omp.restype = ctypes.c_size_t
+    for name in ("orc_collision_search_line", "orc_collision_search_linetree"):
+        getattr(L, name).argtypes = [P, ctypes.c_double, ctypes.c_void_p, ctypes.c_size_t]
+        getattr(L, name).restype = ctypes.c_size_t
+    L.orc_tree_export.argtypes = [P, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+    L.orc_tree_export.restype = ctypes.c_int
+    L.orc_energy.argtypes = [P]
+    L.orc_energy.restype = ctypes.c_double
+    L.orc_whfast_kepler_solver.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double]
+    L.orc_ic_plummer.argtypes = [ctypes.c_uint, ctypes.c_size_t, ctypes.c_double, ctypes.c_double,
+                                 ctypes.c_double, ctypes.c_void_p]
+    L.orc_collision_resolve_hardsphere.argtypes = [P, ctypes.c_void_p, ctypes.c_double, ctypes.c_double]
+    return L
 
 
 GRAVITY = {"none": 0, "basic": 1, "compensated": 2, "tree": 3, "basic_omp": 101, "compensated_omp": 102}
@@ -237,7 +265,8 @@ class Sim:
             fn = L.orc_collision_search_line if mode == "line" else L.orc_collision_search_linetree
             n = fn(self.ref, float(dt_last_done), out.ctypes.data, cap)
         else:
-            fn = L.orc_collision_search_direct if mode == "direct" else L.orc_collision_search_tree
+            fn = {"direct": L.orc_collision_search_direct, "tree": L.orc_collision_search_tree,
+                  "tree_omp": L.orc_collision_search_tree_omp}[mode]
             n = fn(self.ref, out.ctypes.data, cap)
         if n > cap:
             return self.collisions(mode, cap=int(n), dt_last_done=dt_last_done)

@@ -2,7 +2,7 @@
 # files, in place where they lie, into oracle/_ref/.  Test infrastructure only:
 # the product never links or loads anything built here.
 #
-#   make -f oracle/ref.mk REF=/root/reference
+#   make -f oracle/ref.mk REF=<reference checkout>
 #
 # Outputs (git-ignored):
 #   oracle/_ref/librebound$(EXT_SUFFIX)   serial, -ffp-contract=off (parity build;
@@ -15,7 +15,9 @@
 #
 # The recipe compiles every src/*.c like the reference's setup.py does, without
 # the HTTP server (-DSERVER is omitted) and without OpenGL.
-REF ?= /root/reference
+ifndef REF
+$(error REF=<reference checkout> is required)
+endif
 OUT := oracle/_ref
 EXT_SUFFIX := $(shell python3 -c "import sysconfig;print(sysconfig.get_config_var('EXT_SUFFIX') or '.so')")
 SRCS := $(filter-out $(REF)/src/server.c,$(sort $(wildcard $(REF)/src/*.c)))

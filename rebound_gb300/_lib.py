@@ -48,7 +48,8 @@ class Config(ctypes.Structure):
         ("leapfrog_order", ctypes.c_int32), ("whfast_coordinates", ctypes.c_int32),
         ("whfast_corrector", ctypes.c_int32), ("whfast_corrector2", ctypes.c_int32),
         ("whfast_kernel", ctypes.c_int32), ("whfast_keep_unsynchronized", ctypes.c_int32),
-        ("exact_finish_time", ctypes.c_int32), ("tree_quadrupole", ctypes.c_int32)]
+        ("exact_finish_time", ctypes.c_int32), ("tree_quadrupole", ctypes.c_int32),
+        ("collisions_plog", ctypes.c_double)]
 
 
 class ServerConfig(ctypes.Structure):
@@ -80,6 +81,8 @@ SIGNATURES = {
     "rgpu_sim_last_error": (ctypes.c_char_p, [_P]),
     "rgpu_sim_configure": (ctypes.c_int, [_P, ctypes.POINTER(Config)]),
     "rgpu_sim_get_config": (ctypes.c_int, [_P, ctypes.POINTER(Config)]),
+    "rgpu_sim_set_restitution_fn": (ctypes.c_int, [_P, _P, _P]),
+    "rgpu_sim_resolve_time": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)]),
     "rgpu_sim_set_particles": (ctypes.c_int, [_P, _P, ctypes.c_size_t, ctypes.c_size_t]),
     "rgpu_sim_get_particles": (ctypes.c_int, [_P, _P, ctypes.c_size_t, ctypes.c_size_t]),
     "rgpu_sim_N": (ctypes.c_size_t, [_P]),
@@ -106,6 +109,7 @@ SIGNATURES = {
     "rgpu_l2_flush": (ctypes.c_int, [_P, ctypes.c_size_t]),
     "rgpu_set_kernel_variant": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     "rgpu_set_displacement_mode": (ctypes.c_int, [ctypes.c_int]),
+    "rgpu_sim_guard_stats": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
     "rgpu_probe_rate": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "rgpu_selftest_exactfp": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_longlong)]),
     "rgpu_direct_accel_noalloc": (ctypes.c_int, [_P] * 7 + [ctypes.c_int64, ctypes.c_double, ctypes.c_double,
@@ -116,6 +120,9 @@ SIGNATURES = {
     "rgpu_ensemble_free": (None, [_P]),
     "rgpu_ensemble_last_error": (ctypes.c_char_p, [_P]),
     "rgpu_ensemble_set_launch": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int64]),
+    "rgpu_ensemble_set_mapping": (ctypes.c_int, [_P, ctypes.c_int]),
+    "rgpu_ensemble_get_launch": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                                ctypes.POINTER(ctypes.c_int64)]),
     "rgpu_ensemble_steps": (ctypes.c_int, [_P, ctypes.c_int64]),
     "rgpu_ensemble_time_steps": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.POINTER(ctypes.c_double)]),
     "rgpu_ensemble_autotune": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(ctypes.c_int),

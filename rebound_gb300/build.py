@@ -55,7 +55,9 @@ def _compile(src, objdir):
         return obj
     flags = list(COMMON)
     if src in NO_FMAD:
-        flags.append("--fmad=false")
+        # no contraction in device code, nor in the host code that restates the
+        # reference's arithmetic (hardsphere, SEI coefficients, ghost boxes)
+        flags += ["--fmad=false", "-Xcompiler", "-ffp-contract=off"]
     if src.endswith(".cpp"):
         cmd = [nvcc(), "-x", "cu"] + ARCH + flags + ["-c", path, "-o", obj]
     else:

@@ -10,6 +10,7 @@
 // device and host.  Compiled with --fmad=false (exact pair tests).
 #include "rgpu_internal.cuh"
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdlib>
 #include <unordered_map>
@@ -123,10 +124,15 @@ __global__ void scatter_velocities(ParticlesSoA p, const int* __restrict__ ids, 
 
 struct Body { double x, y, z, vx, vy, vz, m, r; };
 
-// reb_collision_resolve_hardsphere (src/collision.c:573-665), constant restitution.
-void hardsphere(Body& p1, Body& p2, const double gb[6], double eps, double minvel, int64_t& log_n) {
+// reb_collision_resolve_hardsphere (src/collision.c:573-665): the restitution
+// coefficient is the constant eps, or eps_fn(eps_user, v) of the normal relative
+// velocity when a callback is set; plog accumulates the y-momentum transferred
+// to the outer particle (src/collision.c:655-662).
+void hardsphere(Body& p1, Body& p2, const double gb[6], double eps, double (*eps_fn)(void*, double), void* eps_user,
+                double minvel, int64_t& log_n, double& plog) {
     const double x21 = p1.x + gb[0] - p2.x, y21 = p1.y + gb[1] - p2.y, z21 = p1.z + gb[2] - p2.z;
     const double rp = p1.r + p2.r;
+    const double oldvyouter = x21 > 0 ? p1.vy : p2.vy;
     if (rp * rp < x21 * x21 + y21 * y21 + z21 * z21) return;
     const double vx21 = p1.vx + gb[3] - p2.vx, vy21 = p1.vy + gb[4] - p2.vy, vz21 = p1.vz + gb[5] - p2.vz;
     if (vx21 * x21 + vy21 * y21 + vz21 * z21 > 0) return;
@@ -135,6 +141,7 @@ void hardsphere(Body& p1, Body& p2, const double gb[6], double eps, double minve
     const double y21n = cth * y21 + sth * z21;
     const double ph = atan2(y21n, x21), cph = cos(ph), sph = sin(ph);
     const double vx21nn = cph * vx21 + sph * vy21n;
+    if (eps_fn) eps = eps_fn(eps_user, vx21nn);
     double dvx2 = -(1.0 + eps) * vx21nn;
     const double minr = (p1.r > p2.r) ? p2.r : p1.r;
     const double maxr = (p1.r < p2.r) ? p2.r : p1.r;
@@ -149,6 +156,8 @@ void hardsphere(Body& p1, Body& p2, const double gb[6], double eps, double minve
     p2.vx -= p2pf * dvx2n; p2.vy -= p2pf * dvy2nn; p2.vz -= p2pf * dvz2nn;
     const double p1pf = p2.m / (p1.m + p2.m);
     p1.vx += p1pf * dvx2n; p1.vy += p1pf * dvy2nn; p1.vz += p1pf * dvz2nn;
+    if (x21 > 0) plog += -fabs(x21) * (oldvyouter - p1.vy) * p1.m;
+    else plog += -fabs(x21) * (oldvyouter - p2.vy) * p2.m;
     log_n++;
 }
 
@@ -207,11 +216,37 @@ int direct_collisions(rgpu_sim* s, rgpu_collision* out, size_t cap, size_t* n_fo
     return read_status(s);
 }
 
-// Shuffle (src/collision.c:336-342) and resolve (:343-404) the pairs of the last search.
+static int resolve_pairs(rgpu_sim* s);
+
+// Host wall time of the resolve stage (shuffle, gather, hardsphere, scatter).
 int resolve_collisions_device(rgpu_sim* s) {
-    rgpu_config& c = s->cfg;
     const size_t n = s->n_pairs;
     if (n == 0) return RGPU_OK;
+    const auto t0 = std::chrono::steady_clock::now();
+    const int rc = resolve_pairs(s);
+    s->resolve_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    s->resolve_calls++;
+    return rc;
+}
+
+extern "C" int rgpu_sim_set_restitution_fn(rgpu_sim* s, double (*fn)(void*, double), void* user) {
+    if (!s) return RGPU_ERR_ARG;
+    s->eps_fn = fn;
+    s->eps_user = user;
+    return RGPU_OK;
+}
+
+extern "C" int rgpu_sim_resolve_time(rgpu_sim* s, double* ms, int64_t* calls) {
+    if (!s || !ms || !calls) return RGPU_ERR_ARG;
+    *ms = s->resolve_ms;
+    *calls = s->resolve_calls;
+    return RGPU_OK;
+}
+
+// Shuffle (src/collision.c:336-342) and resolve (:343-404) the pairs of the last search.
+static int resolve_pairs(rgpu_sim* s) {
+    rgpu_config& c = s->cfg;
+    const size_t n = s->n_pairs;
     std::vector<rgpu_collision> pairs(n);
     RGPU_CUDA(s, cudaMemcpyAsync(pairs.data(), s->dev_pairs, sizeof(rgpu_collision) * n, cudaMemcpyDeviceToHost, s->stream));
     RGPU_CUDA(s, cudaStreamSynchronize(s->stream));
@@ -244,8 +279,8 @@ int resolve_collisions_device(rgpu_sim* s) {
     cudaMemcpyAsync(b.data(), d_buf, sizeof(double) * 8 * nt, cudaMemcpyDeviceToHost, s->stream);
     cudaStreamSynchronize(s->stream);
     for (const auto& q : pairs)
-        hardsphere(b[slot[(int)q.p1]], b[slot[(int)q.p2]], q.gb, c.coefficient_of_restitution,
-                   c.minimum_collision_velocity, c.collisions_log_n);
+        hardsphere(b[slot[(int)q.p1]], b[slot[(int)q.p2]], q.gb, c.coefficient_of_restitution, s->eps_fn,
+                   s->eps_user, c.minimum_collision_velocity, c.collisions_log_n, c.collisions_plog);
     cudaMemcpyAsync(d_buf, b.data(), sizeof(double) * 8 * nt, cudaMemcpyHostToDevice, s->stream);
     scatter_velocities<<<(nt + 127) / 128, 128, 0, s->stream>>>(s->p, d_ids, nt, d_buf);
     g_launches += 2;

@@ -116,14 +116,19 @@ struct __align__(32) FixBody {
     double gm;
 };
 
-// Per-evaluation scale words, written by pack_fix and read by every pair thread.
+// Per-evaluation scale words, written by pack_fix and read by every pair thread,
+// and the counters of the exactness guard (see "Exactness guard" below).
 struct __align__(16) FixScale {
     unsigned long long dmax;               // max |coordinate| as double bits (atomicMax target)
     int shift;                             // s
     int two_s;                             // 2 s
     unsigned long long e0, e1, e2;         // eps^2 2^2s = e0 + e1 2^32 + e2 2^62 (e0 < 2^32, e1 < 2^30)
+    int n_inexact;                         // bodies with a coordinate off the 2^-s grid
+    int n_redo;                            // particles whose force is recomputed in FP64
+    int all;                               // 1: every particle is recomputed in FP64
+    int eps_off;                           // eps^2 is not exact on the 2^-2s grid
+    float delta;                           // bound on the FP32 displacement error of the bound kernels
 };
-static_assert(sizeof(FixScale) <= 256 * 2 * sizeof(float4), "FixScale lives in the jsplit buffer (>= 256 bodies)");
 
 __global__ void max_abs_coord(ParticlesSoA p, int N, unsigned long long* __restrict__ out) {
     __shared__ double red[256];
@@ -139,15 +144,63 @@ __global__ void max_abs_coord(ParticlesSoA p, int N, unsigned long long* __restr
     if (threadIdx.x == 0) atomicMax(out, (unsigned long long)__double_as_longlong(red[0]));  // positive doubles order as integers
 }
 
-__global__ void pack_fix(ParticlesSoA p, int N, double G, double eps2, FixScale* __restrict__ sc,
-                         FixBody* __restrict__ out) {
+// Blocks of pack_fix and fix_scatter: 256 bodies each.
+constexpr int kGuardBlock = 256;
+
+// Fixed-point records of every body.  With `err` set (BASIC / COMPENSATED) it
+// also writes, for the exactness guard, each body's rounding error
+// |x - X 2^-s| (Euclidean, rounded up to float; +inf for a non-finite body),
+// its FP32 position and G m, and the number of inexact bodies of each
+// 256-body block (bcnt).
+__global__ void __launch_bounds__(kGuardBlock) pack_fix(ParticlesSoA p, int N, double G, double eps2,
+                                                        FixScale* __restrict__ sc, FixBody* __restrict__ out,
+                                                        float* __restrict__ err, float4* __restrict__ fpos,
+                                                        int* __restrict__ bcnt) {
     const double mx = __longlong_as_double((long long)sc->dmax);
     int s = (mx > 0. && isfinite(mx)) ? 60 - ilogb(mx) : 60;
     if (eps2 > 0. && isfinite(eps2)) s = min(s, (123 - ilogb(eps2)) >> 1);
     s = min(s, 1022);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool inexact = false;
+    if (i < N) {
+        const double x = p.x[i], y = p.y[i], z = p.z[i];
+        FixBody b;
+        b.x = __double2ll_rn(scalbn(x, s));
+        b.y = __double2ll_rn(scalbn(y, s));
+        b.z = __double2ll_rn(scalbn(z, s));
+        b.gm = G * p.m[i];
+        out[i] = b;
+        if (err) {
+            // x - X 2^-s is exact: X converts back exactly (below 2^53 as an integer,
+            // above it x 2^s already was one) and x lies within half a grid step of it.
+            const double rx = x - scalbn((double)b.x, -s);
+            const double ry = y - scalbn((double)b.y, -s);
+            const double rz = z - scalbn((double)b.z, -s);
+            const double e = sqrt(fma(rx, rx, fma(ry, ry, rz * rz))) * (1.0 + 0x1p-20);
+            const float ef = e <= 3.0e38 ? (float)e : __int_as_float(0x7f800000);   // NaN / overflow -> +inf
+            err[i] = ef;
+            fpos[i] = make_float4((float)x, (float)y, (float)z, (float)b.gm);
+            inexact = ef != 0.f;
+        }
+    }
+    if (bcnt) {
+        __shared__ int wsum[kGuardBlock / 32];
+        const unsigned bal = __ballot_sync(0xffffffffu, inexact);
+        if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = __popc(bal);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int t = 0;
+            for (int w = 0; w < kGuardBlock / 32; w++) t += wsum[w];
+            bcnt[blockIdx.x] = t;
+        }
+    }
     if (i == 0) {
+        sc->n_inexact = 0;
+        sc->n_redo = 0;
+        sc->all = 0;
+        sc->delta = isfinite(mx) ? (float)scalbn(mx, -20) : __int_as_float(0x7f800000);
         unsigned long long hi = 0, lo = 0;
+        bool eps_off = false;
         if (eps2 > 0. && isfinite(eps2)) {
             int ee;
             const double fr = frexp(eps2, &ee);                        // eps2 = fr 2^ee, fr in [0.5, 1)
@@ -156,20 +209,17 @@ __global__ void pack_fix(ParticlesSoA p, int N, double G, double eps2, FixScale*
             if (sh >= 64) { hi = m53 << (sh - 64); }
             else if (sh > 0) { hi = m53 >> (64 - sh); lo = m53 << sh; }
             else if (sh > -64) { lo = m53 >> (-sh); }
+            // eps^2 off the 2^-2s grid (a softening below ~2^-31 max|x|): r^2 + eps^2 is
+            // then not exact and the guard sends every particle to the FP64 kernel
+            eps_off = sh <= -64 || (sh < 0 && (m53 & ((1ull << (-sh)) - 1ull)) != 0ull);
         }
+        sc->eps_off = eps_off ? 1 : 0;
         sc->shift = s;
         sc->two_s = 2 * s;
         sc->e0 = lo & 0xFFFFFFFFull;
         sc->e1 = (lo >> 32) & 0x3FFFFFFFull;
         sc->e2 = (lo >> 62) | (hi << 2);
     }
-    if (i >= N) return;
-    FixBody b;
-    b.x = __double2ll_rn(scalbn(p.x[i], s));
-    b.y = __double2ll_rn(scalbn(p.y[i], s));
-    b.z = __double2ll_rn(scalbn(p.z[i], s));
-    b.gm = G * p.m[i];
-    out[i] = b;
 }
 
 struct DirectArgs {
@@ -210,6 +260,8 @@ template <int MODE, bool GENERAL, int RV, bool CVT, int FIX = 0>
 __global__ void __launch_bounds__(kBlock) direct_kernel(DirectArgs a, const GhostList* __restrict__ ghosts) {
     __shared__ double4_32a tile[(MODE == kMixedSplit) ? 1 : kBlock];
     __shared__ float4 tile_s[(MODE == kMixedSplit) ? 2 * kBlock : 1];
+    // the exactness guard sent every particle to the FP64 recomputation
+    if ((MODE == kBasic || MODE == kComp) && FIX && a.fix->all) return;
     const int i = blockIdx.x * kBlock + threadIdx.x;
     const bool live = i < a.N;
     const int jmax_cta = (a.tp && (int)(blockIdx.x * kBlock) < a.Na) ? a.N : a.Na;
@@ -405,6 +457,148 @@ __global__ void reduce_partials(const double* __restrict__ P, int splits, size_t
     ax[i] = out[0]; ay[i] = out[1]; az[i] = out[2];
 }
 
+// --- Mixed-precision pair kernel (MIXED, MIXED_SPLIT; all particles active, no
+// ghost boxes) --------------------------------------------------------------------
+// Each coordinate is held as a two-float split x = xh + xl (xh = (float)x, xl =
+// (float)(x - xh), exact), so the displacement (xh_j - xh_i) + (xl_j - xl_i) is
+// the FP64 displacement to ~2^-48 of the coordinates before its final rounding
+// to FP32 (the high difference is exact whenever it cancels).  r^2, rsqrt and
+// G m / r^3 are FP32.  The arithmetic runs on Blackwell's packed FP32x2 FMA pipe
+// (__fadd2_rn / __ffma2_rn / __fmul2_rn): every lane evaluates two j-bodies per
+// instruction, 9 packed instructions for the displacements, 3 for r^2, 3 for
+// G m / r^3 and 3 for the accumulation per two pairs, plus one MUFU rsqrt per
+// pair.  Pair terms are summed in FP32 over 32 j-pairs (64 terms) and each such
+// sum is folded into the per-particle accumulator: FP64 (MIXED, the FP64
+// accumulation of the mixed form) or a compensated FP32 pair (MIXED_SPLIT).
+// j-bodies are stored in pairs, 64 B each: (xh0, xh1, yh0, yh1),
+// (zh0, zh1, Gm0, Gm1), (xl0, xl1, yl0, yl1), (zl0, zl1, 0, 0).
+struct __align__(16) SplitPair {
+    float4 a, b, c, d;
+};
+
+__global__ void pack_split2(ParticlesSoA p, int N, double G, SplitPair* __restrict__ out) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (N + 1) / 2) return;
+    float xh[2], yh[2], zh[2], gm[2], xl[2], yl[2], zl[2];
+    for (int k = 0; k < 2; k++) {
+        const int i = 2 * q + k;
+        if (i < N) {
+            const double x = p.x[i], y = p.y[i], z = p.z[i];
+            xh[k] = (float)x; yh[k] = (float)y; zh[k] = (float)z;
+            xl[k] = (float)(x - (double)xh[k]); yl[k] = (float)(y - (double)yh[k]); zl[k] = (float)(z - (double)zh[k]);
+            gm[k] = (float)(G * p.m[i]);
+        } else {   // the partner of the last body of an odd N: massless, at the origin
+            xh[k] = yh[k] = zh[k] = xl[k] = yl[k] = zl[k] = gm[k] = 0.f;
+        }
+    }
+    SplitPair P;
+    P.a = make_float4(xh[0], xh[1], yh[0], yh[1]);
+    P.b = make_float4(zh[0], zh[1], gm[0], gm[1]);
+    P.c = make_float4(xl[0], xl[1], yl[0], yl[1]);
+    P.d = make_float4(zl[0], zl[1], 0.f, 0.f);
+    out[q] = P;
+}
+
+constexpr int kSubPairs = 32;   // j-pairs summed in FP32 before a fold
+
+// MUFU reciprocal square root with subnormal inputs flushed to zero: one
+// instruction (rsqrtf adds the scaling that keeps subnormal inputs exact).
+// Used where the argument is at least eps^2 > 0.
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// ACC: 0 = compensated FP32 pair (MIXED_SPLIT), 1 = FP64 (MIXED).  SOFT: eps^2 > 0,
+// so the self pair (d = 0) contributes exactly 0 and needs no test.
+template <int ACC, bool SOFT>
+__global__ void __launch_bounds__(kBlock) direct_split2(DirectArgs a, const SplitPair* __restrict__ jp) {
+    __shared__ SplitPair tile[kBlock / 2];
+    const int i = blockIdx.x * kBlock + threadIdx.x;
+    const bool live = i < a.N;
+    const int chunk = (((a.N + a.splits - 1) / a.splits) + kBlock - 1) / kBlock * kBlock;
+    const int j0 = blockIdx.y * chunk;
+    const int j1 = min(a.N, j0 + chunk);
+
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    SplitPair P;
+    P.a = P.b = P.c = P.d = z4;
+    if (live) P = jp[i >> 1];
+    const bool odd = i & 1;
+    const float xh = odd ? P.a.y : P.a.x, yh = odd ? P.a.w : P.a.z, zh = odd ? P.b.y : P.b.x;
+    const float xl = odd ? P.c.y : P.c.x, yl = odd ? P.c.w : P.c.z, zl = odd ? P.d.y : P.d.x;
+    const float2 nxh = make_float2(-xh, -xh), nyh = make_float2(-yh, -yh), nzh = make_float2(-zh, -zh);
+    const float2 nxl = make_float2(-xl, -xl), nyl = make_float2(-yl, -yl), nzl = make_float2(-zl, -zl);
+    const float ef = (float)a.eps2;
+    const float2 e2 = make_float2(ef, ef);
+
+    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;   // ACC 0
+    double dx64 = 0., dy64 = 0., dz64 = 0.;                               // ACC 1
+
+    for (int jt = j0; jt < j1; jt += kBlock) {
+        const int nj = min(kBlock, j1 - jt);
+        const int nq = (nj + 1) >> 1;
+        __syncthreads();
+        {
+            const float4* src = reinterpret_cast<const float4*>(jp + (jt >> 1));
+            float4* dst = reinterpret_cast<float4*>(tile);
+            for (int u = threadIdx.x; u < 2 * kBlock; u += kBlock) dst[u] = u < 4 * nq ? src[u] : z4;
+        }
+        __syncthreads();
+        for (int qs = 0; qs < nq; qs += kSubPairs) {
+            const int qe = min(nq, qs + kSubPairs);
+            float2 ax = make_float2(0.f, 0.f), ay = ax, az = ax;
+#pragma unroll 4
+            for (int q = qs; q < qe; q++) {
+                const SplitPair J = tile[q];
+                const float2 dx = __fadd2_rn(__fadd2_rn(make_float2(J.a.x, J.a.y), nxh),
+                                             __fadd2_rn(make_float2(J.c.x, J.c.y), nxl));
+                const float2 dy = __fadd2_rn(__fadd2_rn(make_float2(J.a.z, J.a.w), nyh),
+                                             __fadd2_rn(make_float2(J.c.z, J.c.w), nyl));
+                const float2 dz = __fadd2_rn(__fadd2_rn(make_float2(J.b.x, J.b.y), nzh),
+                                             __fadd2_rn(make_float2(J.d.x, J.d.y), nzl));
+                const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
+                const float2 ri = SOFT ? make_float2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y))
+                                       : make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+                float2 s = __fmul2_rn(__fmul2_rn(ri, ri), __fmul2_rn(make_float2(J.b.z, J.b.w), ri));
+                if (!SOFT) {
+                    const int j = jt + 2 * q;
+                    s.x = (j == i || j >= j1) ? 0.f : s.x;
+                    s.y = (j + 1 == i || j + 1 >= j1) ? 0.f : s.y;
+                }
+                ax = __ffma2_rn(s, dx, ax);
+                ay = __ffma2_rn(s, dy, ay);
+                az = __ffma2_rn(s, dz, az);
+            }
+            const float tx = ax.x + ax.y, ty = ay.x + ay.y, tz = az.x + az.y;
+            if (ACC == 1) {
+                dx64 += (double)tx;
+                dy64 += (double)ty;
+                dz64 += (double)tz;
+            } else {
+                float t, y;
+                y = tx - cx; t = sx + y; cx = (t - sx) - y; sx = t;
+                y = ty - cy; t = sy + y; cy = (t - sy) - y; sy = t;
+                y = tz - cz; t = sz + y; cz = (t - sz) - y; sz = t;
+            }
+        }
+    }
+    if (!live) return;
+    double ox, oy, oz;
+    if (ACC == 1) {
+        ox = dx64; oy = dy64; oz = dz64;
+    } else {
+        ox = (double)sx - (double)cx; oy = (double)sy - (double)cy; oz = (double)sz - (double)cz;
+    }
+    if (a.splits == 1) {
+        a.ax[i] = ox; a.ay[i] = oy; a.az[i] = oz;
+    } else {
+        double* Pp = a.partial + (size_t)blockIdx.y * 3 * a.cap;
+        Pp[i] = ox; Pp[a.cap + i] = oy; Pp[2 * a.cap + i] = oz;
+    }
+}
+
 // Pack (x, y, z, G*m) and, when requested, the float split used by MIXED_SPLIT.
 __global__ void pack_j(ParticlesSoA p, int N, double G, double4_32a* __restrict__ jpos, float4* __restrict__ jsplit) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -415,6 +609,435 @@ __global__ void pack_j(ParticlesSoA p, int N, double G, double4_32a* __restrict_
         const float xh = (float)x, yh = (float)y, zh = (float)z;
         jsplit[2 * i] = make_float4(xh, yh, zh, (float)gm);
         jsplit[2 * i + 1] = make_float4((float)(x - (double)xh), (float)(y - (double)yh), (float)(z - (double)zh), 0.f);
+    }
+}
+
+// --- Exactness guard for the fixed-point forms ---------------------------------
+// A coordinate below 2^-8 max|x| has bits under the 2^-s grid and is rounded to
+// it (error e_b <= 2^-s-1 per component), so a pair of bodies can be displaced
+// by up to |e_i| + |e_j| from where the FP64 subtraction puts them.  The force
+// G m d / (d^2 + eps^2)^(3/2) has a Jacobian of norm at most
+// 2 G m / (r^2 + eps^2)^(3/2) (r the smallest distance on the segment between
+// the two displacements), so the fixed-point force on particle i is off by at
+// most
+//     B_i = 2 sum_j s_ij (|e_i| + |e_j|) = 2 (|e_i| S_i + T_i),
+//     S_i = sum_j s_ij,   T_i = sum_j s_ij |e_j|,   s_ij >= G m_j / (r^2 + eps^2)^(3/2),
+// where s_ij is evaluated in FP32 at the distance lowered by a bound on its
+// FP32 error (delta = 2^-20 max|x|), so it is an upper bound.  S_i is needed
+// only for inexact i and T_i only runs over inexact j, so on the inputs this
+// kernel is built for (a Plummer sphere: about 6 % of the bodies inexact) the
+// two bound sums cost a few percent of the FP64 pair kernel.  Every particle
+// with B_i > kGuardTau |a_i| (or a non-finite a_i or B_i) is recomputed by an
+// FP64 kernel (the FP64 subtraction, as the reference forms it); more than a
+// quarter of the bodies inexact, or eps^2 off the grid, sends every particle
+// there and the fixed-point kernel returns at once.  Everything is decided on
+// the device from counters in FixScale; the host launches a fixed sequence.
+// Results are deterministic: the inexact list is compacted in index order,
+// each bound and each recomputed force is summed by one thread in a fixed order.
+constexpr double kGuardTau = 5e-15;
+constexpr int kGuardSplitMax = 16;         // j-chunks of the S_i sums
+
+// Exclusive scan of the per-block inexact counts (one CTA of 1024 threads);
+// sets n_inexact and the all-FP64 switch.
+__global__ void __launch_bounds__(1024) fix_scan(int* __restrict__ bcnt, int nb, int N, FixScale* __restrict__ sc) {
+    __shared__ int wtot[32];
+    __shared__ int carry;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < nb; base += 1024) {
+        const int k = base + threadIdx.x;
+        const int v = k < nb ? bcnt[k] : 0;
+        int x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wtot[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            int t = wtot[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, t, o);
+                if (lane >= o) t += y;
+            }
+            wtot[lane] = t;
+        }
+        __syncthreads();
+        const int excl = carry + (warp ? wtot[warp - 1] : 0) + x - v;
+        if (k < nb) bcnt[k] = excl;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = excl + v;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        sc->n_inexact = carry;
+        sc->n_redo = 0;
+        sc->all = (sc->eps_off || (long long)carry * 4 > (long long)N) ? 1 : 0;
+    }
+}
+
+// The inexact bodies in index order.
+__global__ void __launch_bounds__(kGuardBlock) fix_scatter(const float* __restrict__ err, const int* __restrict__ boff,
+                                                           int N, const FixScale* __restrict__ sc, int* __restrict__ list) {
+    if (sc->all) return;
+    __shared__ int wsum[kGuardBlock / 32];
+    const int i = blockIdx.x * kGuardBlock + threadIdx.x;
+    const bool inexact = i < N && err[i] != 0.f;
+    const unsigned bal = __ballot_sync(0xffffffffu, inexact);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) wsum[warp] = __popc(bal);
+    __syncthreads();
+    int off = boff[blockIdx.x];
+    for (int w = 0; w < warp; w++) off += wsum[w];
+    if (inexact) list[off + __popc(bal & ((1u << lane) - 1u))] = i;
+}
+
+// Upper bound on G m_j / (r^2 + eps^2)^(3/2) for two j-bodies at once (packed
+// FP32x2), from FP32 displacements.  R = sqrt(r_f^2 + eps^2) is within delta of
+// its exact value (the map r -> sqrt(r^2 + eps^2) is 1-Lipschitz and the FP32
+// distance r_f is within delta of the exact one), so the term is at most
+// G m / (R - delta)^3 = G m y^3 / (1 - delta y)^3 <= G m y^3 (1 + 4 delta y) for
+// delta y <= 1/8 (y = 1/R; the FP32 rounding of r^2 and rsqrt stays inside the
+// 5 % slack of the final bound).  t4 = 4 delta y is returned for the range check.
+__device__ __forceinline__ float2 s_upper2(float2 dx, float2 dy, float2 dz, float2 gm, float2 e2, float2 d4, float2& t4) {
+    const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
+    const float2 y = make_float2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));   // a flushed r^2 gives +inf: flagged
+    t4 = __fmul2_rn(d4, y);
+    const float2 s0 = __fmul2_rn(__fmul2_rn(y, y), __fmul2_rn(gm, y));
+    return __ffma2_rn(t4, s0, s0);
+}
+
+// Pair-layout tile of FP32 positions for the bound kernels: j-bodies 2q, 2q+1
+// as (x0, x1, y0, y1), (z0, z1, g0, g1), (e0, e1, id0, id1) with g = G m and, in
+// the T kernel, e = the body's rounding error and id its index.
+struct __align__(16) BoundPair {
+    float4 a, b, c;
+};
+
+// Accumulate one tile's two-body terms into S (W = false) or T (W = true: the
+// terms weighted by e).  The pair holding particle `self` is excluded; `tm`
+// collects the largest 4 delta y of the included pairs.
+template <bool W>
+__device__ __forceinline__ void bound_tile(const BoundPair* __restrict__ tile, int nj, int qself_or_idx, bool by_index,
+                                           int self, float2 nx, float2 ny, float2 nz, float2 e2, float2 d4,
+                                           float2& acc, float& tm) {
+    const int nq = (nj + 1) >> 1;
+#pragma unroll 4
+    for (int q = 0; q < nq; q++) {
+        const BoundPair J = tile[q];
+        const float2 dx = __fadd2_rn(make_float2(J.a.x, J.a.y), nx);
+        const float2 dy = __fadd2_rn(make_float2(J.a.z, J.a.w), ny);
+        const float2 dz = __fadd2_rn(make_float2(J.b.x, J.b.y), nz);
+        float2 t4;
+        float2 su = s_upper2(dx, dy, dz, make_float2(J.b.z, J.b.w), e2, d4, t4);
+        bool x0, x1;   // excluded halves
+        if (by_index) {
+            x0 = __float_as_int(J.c.z) == self;
+            x1 = __float_as_int(J.c.w) == self;
+        } else {
+            x0 = q == qself_or_idx && !(self & 1);
+            x1 = q == qself_or_idx && (self & 1);
+        }
+        x1 = x1 || 2 * q + 1 >= nj;   // the empty half of an odd tile's last pair
+        su.x = x0 ? 0.f : su.x;
+        su.y = x1 ? 0.f : su.y;
+        tm = fmaxf(tm, fmaxf(x0 ? 0.f : t4.x, x1 ? 0.f : t4.y));
+        acc = W ? __ffma2_rn(su, make_float2(J.c.x, J.c.y), acc) : __fadd2_rn(acc, su);
+    }
+}
+
+// S_i for the inexact particles: chunk y of the j-range per work item, written
+// to spart[y][i] (+inf when a pair left the range of the bound).
+__global__ void __launch_bounds__(kBlock) fix_bound_S(const float4* __restrict__ fpos, const int* __restrict__ list,
+                                                      const FixScale* __restrict__ sc, int N, float eps2f, int ny,
+                                                      float* __restrict__ spart, size_t cap) {
+    if (sc->all) return;
+    __shared__ BoundPair tile[kBlock / 2];
+    const int ni = sc->n_inexact;
+    const int nbi = (ni + kBlock - 1) / kBlock;
+    const int chunk = ((N + ny - 1) / ny + kBlock - 1) / kBlock * kBlock;
+    const float d4f = 4.f * sc->delta;
+    const float2 d4 = make_float2(d4f, d4f), e2 = make_float2(eps2f, eps2f);
+    for (int w = blockIdx.x; w < nbi * ny; w += gridDim.x) {
+        const int b = w % nbi, y = w / nbi;
+        const int pos = b * kBlock + threadIdx.x;
+        const int i = pos < ni ? list[pos] : -1;
+        const float4 pi = i >= 0 ? fpos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float2 nx = make_float2(-pi.x, -pi.x), nyv = make_float2(-pi.y, -pi.y), nz = make_float2(-pi.z, -pi.z);
+        const int j0 = y * chunk, j1 = min(N, j0 + chunk);
+        float2 S = make_float2(0.f, 0.f);
+        float tm = 0.f;
+        for (int jt = j0; jt < j1; jt += kBlock) {
+            __syncthreads();
+            {
+                const int jl = jt + threadIdx.x;
+                const float4 q = jl < j1 ? fpos[jl] : make_float4(0.f, 0.f, 0.f, 0.f);
+                float* t = reinterpret_cast<float*>(&tile[threadIdx.x >> 1]);
+                const int h = threadIdx.x & 1;
+                t[0 + h] = q.x; t[2 + h] = q.y; t[4 + h] = q.z; t[6 + h] = q.w;
+            }
+            __syncthreads();
+            const int d = i - jt;   // self inside this tile when 0 <= d < kBlock
+            bound_tile<false>(tile, min(kBlock, j1 - jt), (d >= 0 && d < kBlock) ? (d >> 1) : -1, false, d, nx, nyv,
+                              nz, e2, d4, S, tm);
+        }
+        if (i >= 0) {
+            const float Sv = S.x + S.y;
+            spart[(size_t)y * cap + i] = tm <= 0.5f ? Sv : __int_as_float(0x7f800000);
+        }
+    }
+}
+
+// T_i over the inexact bodies for every particle, the bound B_i, and the list
+// of particles to recompute.
+__global__ void __launch_bounds__(kBlock) fix_bound_flag(const float4* __restrict__ fpos, const float* __restrict__ err,
+                                                         const int* __restrict__ list, FixScale* __restrict__ sc, int N,
+                                                         float eps2f, int ny, const float* __restrict__ spart, size_t cap,
+                                                         const double* __restrict__ ax, const double* __restrict__ ay,
+                                                         const double* __restrict__ az, int* __restrict__ redo) {
+    if (sc->all) return;
+    const int ni = sc->n_inexact;
+    if (ni == 0) return;                  // every coordinate on the grid: the fixed-point sums are exact
+    __shared__ BoundPair tile[kBlock / 2];
+    const float d4f = 4.f * sc->delta;
+    const float2 d4 = make_float2(d4f, d4f), e2 = make_float2(eps2f, eps2f);
+    const int nb = (N + kBlock - 1) / kBlock;
+    for (int b = blockIdx.x; b < nb; b += gridDim.x) {
+        const int i = b * kBlock + threadIdx.x;
+        const bool live = i < N;
+        const float4 pi = live ? fpos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float2 nx = make_float2(-pi.x, -pi.x), ny2 = make_float2(-pi.y, -pi.y), nz = make_float2(-pi.z, -pi.z);
+        float2 T = make_float2(0.f, 0.f);
+        float tm = 0.f;
+        for (int jt = 0; jt < ni; jt += kBlock) {
+            __syncthreads();
+            {
+                const int k = jt + threadIdx.x;
+                float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+                float e = 0.f;
+                int j = -1;
+                if (k < ni) { j = list[k]; q = fpos[j]; e = err[j]; }
+                float* t = reinterpret_cast<float*>(&tile[threadIdx.x >> 1]);
+                const int h = threadIdx.x & 1;
+                t[0 + h] = q.x; t[2 + h] = q.y; t[4 + h] = q.z; t[6 + h] = q.w;
+                t[8 + h] = e; t[10 + h] = __int_as_float(j);
+            }
+            __syncthreads();
+            bound_tile<true>(tile, min(kBlock, ni - jt), -1, true, i, nx, ny2, nz, e2, d4, T, tm);
+        }
+        if (live) {
+            const float Ei = err[i];
+            float S = 0.f;
+            if (Ei != 0.f)
+                for (int y = 0; y < ny; y++) S += spart[(size_t)y * cap + i];
+            // 2 (|e_i| S_i + T_i) with 5 % slack for the FP32 evaluation
+            double B = 2.1 * ((double)Ei * (double)S + (double)(T.x + T.y));
+            if (!(tm <= 0.5f)) B = __longlong_as_double(0x7ff0000000000000ll);
+            const double amag = sqrt(ax[i] * ax[i] + ay[i] * ay[i] + az[i] * az[i]);
+            if (!(B <= kGuardTau * amag)) redo[atomicAdd(&sc->n_redo, 1)] = i;
+        }
+    }
+}
+
+// FP64 pair term of the recomputation: the FP64 subtraction (src/gravity.c:215-233),
+// r^2 and m/r^3 as in the FP64 kernel.
+__device__ __forceinline__ double redo_term(double xj, double yj, double zj, double gmj, double xi, double yi,
+                                            double zi, double eps2, double& dx, double& dy, double& dz) {
+    dx = xj - xi; dy = yj - yi; dz = zj - zi;
+    const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, eps2)));
+    return m_rinv3<kRinvSeriesInt>(r2, gmj);
+}
+
+// Short recomputation lists (kRedoWarpMax particles or fewer): one warp per
+// (particle, j-chunk), the lanes striding over the chunk's bodies (all lanes
+// busy however few particles there are), Kahan sums per lane combined across
+// the warp in a fixed order; chunk sums go to part[(c * 3 + comp) * nr + p].
+constexpr int kRedoWarpMax = 2048;
+
+struct WarpSplit {
+    int nr, J, chunk;
+};
+__device__ __forceinline__ WarpSplit warp_split(const FixScale* sc, int N, int target) {
+    WarpSplit w;
+    w.nr = sc->all ? 0 : sc->n_redo;
+    if (w.nr > kRedoWarpMax) w.nr = 0;
+    const int maxJ = max(1, (N + 63) / 64);          // at least two bodies per lane
+    int J = w.nr ? (target + w.nr - 1) / w.nr : 1;
+    w.J = max(1, min(J, maxJ));
+    w.chunk = ((N + w.J - 1) / w.J + 31) / 32 * 32;
+    return w;
+}
+
+// (s, c) + (t, d) for Kahan pairs, as a TwoSum of the sums plus the compensations.
+__device__ __forceinline__ void kahan_merge(double& s, double& c, double t, double d) {
+    const double u = s + t;
+    const double bp = u - s;
+    const double e = (s - (u - bp)) + (t - bp);
+    s = u;
+    c = c + d - e;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kBlock) fix_redo_warp(ParticlesSoA p, int N, double G, double eps2,
+                                                        const FixScale* __restrict__ sc, const int* __restrict__ redo,
+                                                        int target, double* __restrict__ part) {
+    const WarpSplit ws = warp_split(sc, N, target);
+    if (ws.nr == 0) return;
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (kBlock / 32);
+    for (int w = blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5); w < ws.nr * ws.J; w += warps) {
+        const int pidx = w % ws.nr, c = w / ws.nr;
+        const int i = redo[pidx];
+        const double xi = p.x[i], yi = p.y[i], zi = p.z[i];
+        const int j0 = c * ws.chunk, j1 = min(N, j0 + ws.chunk);
+        double s[3] = {0., 0., 0.}, k[3] = {0., 0., 0.};     // Kahan sum and compensation
+        for (int j = j0 + lane; j < j1; j += 32) {
+            double dx, dy, dz;
+            double f = redo_term(p.x[j], p.y[j], p.z[j], G * p.m[j], xi, yi, zi, eps2, dx, dy, dz);
+            f = (j == i) ? 0.0 : f;
+            const double v[3] = {f * dx, f * dy, f * dz};
+            for (int q = 0; q < 3; q++) {
+                const double y = v[q] - k[q];
+                const double t = s[q] + y;
+                k[q] = (t - s[q]) - y;
+                s[q] = t;
+            }
+        }
+        // fixed-order butterfly over the lanes
+        for (int o = 16; o > 0; o >>= 1)
+            for (int q = 0; q < 3; q++) {
+                const double t = __shfl_down_sync(0xffffffffu, s[q], o);
+                const double d = __shfl_down_sync(0xffffffffu, k[q], o);
+                kahan_merge(s[q], k[q], t, d);
+            }
+        if (lane == 0)
+            for (int q = 0; q < 3; q++) part[((size_t)c * 3 + q) * ws.nr + pidx] = s[q] - k[q];
+    }
+    (void)MODE;
+}
+
+__global__ void fix_redo_warp_reduce(const double* __restrict__ part, const FixScale* __restrict__ sc,
+                                     const int* __restrict__ redo, int N, int target,
+                                     double* __restrict__ ax, double* __restrict__ ay, double* __restrict__ az) {
+    const WarpSplit ws = warp_split(sc, N, target);
+    if (ws.nr == 0) return;
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (blockDim.x / 32);
+    for (int pidx = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); pidx < ws.nr; pidx += warps) {
+        double s[3] = {0., 0., 0.}, k[3] = {0., 0., 0.};
+        for (int c = lane; c < ws.J; c += 32)
+            for (int q = 0; q < 3; q++) kahan_merge(s[q], k[q], part[((size_t)c * 3 + q) * ws.nr + pidx], 0.);
+        for (int o = 16; o > 0; o >>= 1)
+            for (int q = 0; q < 3; q++) {
+                const double t = __shfl_down_sync(0xffffffffu, s[q], o);
+                const double d = __shfl_down_sync(0xffffffffu, k[q], o);
+                kahan_merge(s[q], k[q], t, d);
+            }
+        if (lane == 0) {
+            const int i = redo[pidx];
+            ax[i] = s[0] - k[0]; ay[i] = s[1] - k[1]; az[i] = s[2] - k[2];
+        }
+    }
+}
+
+// Long recomputation lists (more than kRedoWarpMax particles, or every particle):
+// 256-particle blocks against shared-memory tiles of j-bodies, the j-range cut
+// into J chunks so that about `target` work items exist.
+struct RedoSplit {
+    int nr, nb, J, chunk;
+    size_t stride;
+};
+__device__ __forceinline__ RedoSplit redo_split(const FixScale* sc, int N, int target) {
+    RedoSplit r;
+    r.nr = sc->all ? N : sc->n_redo;
+    if (!sc->all && r.nr <= kRedoWarpMax) r.nr = 0;
+    r.nb = (r.nr + kBlock - 1) / kBlock;
+    const int ntile = (N + kBlock - 1) / kBlock;
+    int J = r.nb ? (target + r.nb - 1) / r.nb : 1;
+    J = max(1, min(J, ntile));
+    r.J = J;
+    r.chunk = (ntile + J - 1) / J * kBlock;
+    r.stride = (size_t)r.nb * kBlock;
+    return r;
+}
+
+// BASIC sums each 256-body tile with FMAs and folds it with Kahan compensation,
+// COMPENSATED compensates every term (src/gravity.c:325-343).  One chunk's
+// sums go to part[c][3][pos].
+template <int MODE>
+__global__ void __launch_bounds__(kBlock) fix_redo(ParticlesSoA p, int N, double G, double eps2,
+                                                   const FixScale* __restrict__ sc, const int* __restrict__ redo,
+                                                   int target, double* __restrict__ part) {
+    const RedoSplit rs = redo_split(sc, N, target);
+    if (rs.nr == 0) return;
+    const bool all = sc->all != 0;
+    __shared__ double4_32a tile[kBlock];
+    for (int w = blockIdx.x; w < rs.nb * rs.J; w += gridDim.x) {
+        const int b = w % rs.nb, c = w / rs.nb;
+        const int pos = b * kBlock + threadIdx.x;
+        const int i = pos < rs.nr ? (all ? pos : redo[pos]) : -1;
+        double xi = 0., yi = 0., zi = 0.;
+        if (i >= 0) { xi = p.x[i]; yi = p.y[i]; zi = p.z[i]; }
+        const int j0 = c * rs.chunk, j1 = min(N, j0 + rs.chunk);
+        double sx = 0., sy = 0., sz = 0., cx = 0., cy = 0., cz = 0.;
+        for (int jt = j0; jt < j1; jt += kBlock) {
+            __syncthreads();
+            const int jl = jt + threadIdx.x;
+            tile[threadIdx.x] = jl < j1 ? make_double4_32a(p.x[jl], p.y[jl], p.z[jl], G * p.m[jl])
+                                        : make_double4_32a(0., 0., 0., 0.);
+            __syncthreads();
+            const int nt = min(kBlock, j1 - jt);
+            double tx = 0., ty = 0., tz = 0.;
+            for (int k = 0; k < nt; k++) {
+                const double4_32a q = tile[k];
+                double dx, dy, dz;
+                double s = redo_term(q.x, q.y, q.z, q.w, xi, yi, zi, eps2, dx, dy, dz);
+                s = (jt + k == i) ? 0.0 : s;
+                if (MODE == kBasic) {
+                    tx = fma(s, dx, tx); ty = fma(s, dy, ty); tz = fma(s, dz, tz);
+                } else {
+                    double t, y;
+                    y = s * dx - cx; t = sx + y; cx = (t - sx) - y; sx = t;
+                    y = s * dy - cy; t = sy + y; cy = (t - sy) - y; sy = t;
+                    y = s * dz - cz; t = sz + y; cz = (t - sz) - y; sz = t;
+                }
+            }
+            if (MODE == kBasic) {
+                double t, y;
+                y = tx - cx; t = sx + y; cx = (t - sx) - y; sx = t;
+                y = ty - cy; t = sy + y; cy = (t - sy) - y; sy = t;
+                y = tz - cz; t = sz + y; cz = (t - sz) - y; sz = t;
+            }
+        }
+        if (i >= 0) {
+            double* P = part + (size_t)c * 3 * rs.stride;
+            P[pos] = sx - cx; P[rs.stride + pos] = sy - cy; P[2 * rs.stride + pos] = sz - cz;
+        }
+    }
+}
+
+// Sum the recomputation's chunks in chunk order (TwoSum carries) into a[i].
+__global__ void fix_redo_reduce(const double* __restrict__ part, const FixScale* __restrict__ sc,
+                                const int* __restrict__ redo, int N, int target,
+                                double* __restrict__ ax, double* __restrict__ ay, double* __restrict__ az) {
+    const RedoSplit rs = redo_split(sc, N, target);
+    const bool all = sc->all != 0;
+    for (int pos = blockIdx.x * blockDim.x + threadIdx.x; pos < rs.nr; pos += gridDim.x * blockDim.x) {
+        const int i = all ? pos : redo[pos];
+        double out[3];
+        for (int comp = 0; comp < 3; comp++) {
+            double s = 0., e = 0.;
+            for (int c = 0; c < rs.J; c++) {
+                const double v = part[((size_t)c * 3 + comp) * rs.stride + pos];
+                const double t = s + v;
+                const double bp = t - s;
+                e += (s - (t - bp)) + (v - bp);
+                s = t;
+            }
+            out[comp] = s + e;
+        }
+        ax[i] = out[0]; ay[i] = out[1]; az[i] = out[2];
     }
 }
 
@@ -498,6 +1121,19 @@ int g_rinv_variant = kRinvSeriesInt;
 bool g_mixed_cvt = false;
 int g_disp_mode = 2;
 
+// MIXED / MIXED_SPLIT without ghost boxes or pair exclusions: the packed
+// FP32x2 kernel over j-bodies packed by pack_split2.
+void launch_split2(int mode, dim3 grid, cudaStream_t st, const DirectArgs& a, const SplitPair* jp) {
+    const bool soft = (float)a.eps2 >= 1.17549435e-38f;   // eps^2 a normal float: r^2 never subnormal
+    if (mode == kMixed) {
+        if (soft) direct_split2<1, true><<<grid, kBlock, 0, st>>>(a, jp);
+        else direct_split2<1, false><<<grid, kBlock, 0, st>>>(a, jp);
+    } else {
+        if (soft) direct_split2<0, true><<<grid, kBlock, 0, st>>>(a, jp);
+        else direct_split2<0, false><<<grid, kBlock, 0, st>>>(a, jp);
+    }
+}
+
 template <int MODE, bool GEN>
 void launch_mode(dim3 grid, cudaStream_t st, const DirectArgs& a) {
     if constexpr ((MODE == kBasic || MODE == kComp) && !GEN) {
@@ -506,12 +1142,6 @@ void launch_mode(dim3 grid, cudaStream_t st, const DirectArgs& a) {
                 direct_kernel<MODE, false, kRinvSeriesInt, true, 1><<<grid, kBlock, 0, st>>>(a, g_ghost_dev);
             else
                 direct_kernel<MODE, false, kRinvSeriesInt, true, 2><<<grid, kBlock, 0, st>>>(a, g_ghost_dev);
-            return;
-        }
-    }
-    if constexpr (MODE == kMixed && !GEN) {
-        if (a.fix) {
-            direct_kernel<kMixed, false, kRinvSeries, false, 1><<<grid, kBlock, 0, st>>>(a, g_ghost_dev);
             return;
         }
     }
@@ -555,6 +1185,76 @@ int ensure_partial(rgpu_sim* s, size_t splits) {
     return RGPU_OK;
 }
 
+// Device buffers of the exactness guard, sized for `cap` particles.
+struct FixGuard {
+    size_t cap = 0;
+    void* block = nullptr;      // one allocation holding everything below
+    FixScale* sc = nullptr;
+    float* err = nullptr;       // [cap] rounding error per body
+    float4* fpos = nullptr;     // [cap] FP32 position and G m
+    int* list = nullptr;        // [cap] inexact bodies in index order
+    int* redo = nullptr;        // [cap] particles recomputed in FP64
+    int* bcnt = nullptr;        // [cap / 256 + 1] per-block counts, then offsets
+    float* spart = nullptr;     // [kGuardSplitMax][cap] S_i chunk sums
+    double* rpart = nullptr;    // recomputation chunk sums
+    size_t rpart_len = 0;
+};
+
+// Work items of the FP64 recomputation: tiled (about two per resident CTA) and
+// warp-per-particle (about two per resident warp), and the grid of both.
+static int redo_target() { return sm_count() * 8; }
+static int redo_warp_target() { return sm_count() * 64; }
+static int redo_grid() { return sm_count() * 4; }
+
+static int ensure_fixguard(rgpu_sim* s) {
+    if (s->fixg && s->fixg->cap >= s->cap) return RGPU_OK;
+    direct_free(s);
+    FixGuard* g = new FixGuard();
+    const size_t cap = s->cap;
+    const size_t nb = cap / kGuardBlock + 1;
+    g->rpart_len = std::max((size_t)(redo_target() + nb) * 3 * kBlock,
+                            (size_t)(redo_warp_target() + kRedoWarpMax) * 3);
+    auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+    const size_t bytes = al(sizeof(FixScale)) + al(cap * 4) + al(cap * 16) + 2 * al(cap * 4) + al(nb * 4) +
+                         al(kGuardSplitMax * cap * 4) + al(g->rpart_len * 8);
+    if (cudaMalloc(&g->block, bytes) != cudaSuccess) {
+        delete g;
+        return check_cuda(s, cudaGetLastError(), "cudaMalloc exactness guard");
+    }
+    char* q = (char*)g->block;
+    g->sc = (FixScale*)q; q += al(sizeof(FixScale));
+    g->err = (float*)q; q += al(cap * 4);
+    g->fpos = (float4*)q; q += al(cap * 16);
+    g->list = (int*)q; q += al(cap * 4);
+    g->redo = (int*)q; q += al(cap * 4);
+    g->bcnt = (int*)q; q += al(nb * 4);
+    g->spart = (float*)q; q += al(kGuardSplitMax * cap * 4);
+    g->rpart = (double*)q;
+    g->cap = cap;
+    s->fixg = g;
+    return RGPU_OK;
+}
+
+void direct_free(rgpu_sim* s) {
+    if (!s->fixg) return;
+    cudaFree(s->fixg->block);
+    delete s->fixg;
+    s->fixg = nullptr;
+}
+
+extern "C" int rgpu_sim_guard_stats(rgpu_sim* s, int64_t* n_inexact, int64_t* n_redo) {
+    if (!s || !n_inexact || !n_redo) return RGPU_ERR_ARG;
+    *n_inexact = -1;
+    *n_redo = -1;
+    if (!s->fixg) return RGPU_OK;
+    FixScale h;
+    RGPU_CUDA(s, cudaMemcpyAsync(&h, s->fixg->sc, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
+    RGPU_CUDA(s, cudaStreamSynchronize(s->stream));
+    *n_inexact = h.n_inexact;
+    *n_redo = h.all ? (int64_t)s->N : h.n_redo;
+    return RGPU_OK;
+}
+
 int direct_accel(rgpu_sim* s, int gravity) {
     const int N = (int)s->N;
     if (N == 0) return RGPU_OK;
@@ -588,18 +1288,36 @@ int direct_accel(rgpu_sim* s, int gravity) {
         RGPU_CUDA(s, cudaMemcpyAsync(g_ghost_dev, &gl, sizeof(GhostList), cudaMemcpyHostToDevice, s->stream));
     }
 
-    // BASIC, COMPENSATED and MIXED without ghosts or pair exclusions form the
-    // displacement on the integer pipe from fixed-point positions; the scale
-    // words (FixScale) live in the jsplit buffer, which only MIXED_SPLIT uses.
-    const bool fix = g_disp_mode != 0 && (mode == kBasic || mode == kComp || mode == kMixed) && !general;
+    // BASIC and COMPENSATED without ghosts or pair exclusions form the pair on the
+    // integer pipes from fixed-point positions; MIXED and MIXED_SPLIT without them
+    // run the packed FP32x2 kernel over two-float splits.
+    const bool fix = g_disp_mode != 0 && (mode == kBasic || mode == kComp) && !general;
+    const bool split2 = (mode == kMixed || mode == kMixedSplit) && !general;
+    // BASIC and COMPENSATED promise the FP64 result: the exactness guard checks
+    // the grid rounding and recomputes the particles it could affect.
+    const bool guard = fix;
     FixScale* fsc = nullptr;
+    FixGuard* fg = nullptr;
+    const int nbg = (int)grid_for(N, kGuardBlock);
     if (fix) {
-        fsc = reinterpret_cast<FixScale*>(s->jsplit);
+        RGPU_TRY(ensure_fixguard(s));
+        fg = s->fixg;
+        fsc = fg->sc;
         RGPU_CUDA(s, cudaMemsetAsync(&fsc->dmax, 0, sizeof(unsigned long long), s->stream));
         max_abs_coord<<<std::min<int>(grid_for(N, 256), 2 * 152), 256, 0, s->stream>>>(s->p, N, &fsc->dmax);
-        pack_fix<<<grid_for(N, 256), 256, 0, s->stream>>>(s->p, N, c.G, c.softening * c.softening, fsc,
-                                                          reinterpret_cast<FixBody*>(s->jpos));
+        pack_fix<<<nbg, kGuardBlock, 0, s->stream>>>(s->p, N, c.G, c.softening * c.softening, fsc,
+                                                     reinterpret_cast<FixBody*>(s->jpos), guard ? fg->err : nullptr,
+                                                     guard ? fg->fpos : nullptr, guard ? fg->bcnt : nullptr);
         g_launches += 2;
+        if (guard) {
+            fix_scan<<<1, 1024, 0, s->stream>>>(fg->bcnt, nbg, N, fsc);
+            fix_scatter<<<nbg, kGuardBlock, 0, s->stream>>>(fg->err, fg->bcnt, N, fsc, fg->list);
+            g_launches += 2;
+        }
+    } else if (split2) {
+        pack_split2<<<grid_for((N + 1) / 2, 256), 256, 0, s->stream>>>(s->p, N, c.G,
+                                                                      reinterpret_cast<SplitPair*>(s->jsplit));
+        g_launches++;
     } else {
         pack_j<<<grid_for(N, 256), 256, 0, s->stream>>>(s->p, N, c.G, s->jpos, mode == kMixedSplit ? s->jsplit : nullptr);
         g_launches++;
@@ -621,7 +1339,8 @@ int direct_accel(rgpu_sim* s, int gravity) {
     const dim3 grid(nbi, splits);
 
     ktimer_begin(s);
-    switch (mode) {
+    if (split2) launch_split2(mode, grid, s->stream, a, reinterpret_cast<const SplitPair*>(s->jsplit));
+    else switch (mode) {
         case kBasic: general ? launch_mode<kBasic, true>(grid, s->stream, a) : launch_mode<kBasic, false>(grid, s->stream, a); break;
         case kComp: general ? launch_mode<kComp, true>(grid, s->stream, a) : launch_mode<kComp, false>(grid, s->stream, a); break;
         case kMixed: general ? launch_mode<kMixed, true>(grid, s->stream, a) : launch_mode<kMixed, false>(grid, s->stream, a); break;
@@ -636,6 +1355,33 @@ int direct_accel(rgpu_sim* s, int gravity) {
         else
             reduce_partials<false><<<grid_for(N, 256), 256, 0, s->stream>>>(s->partial, splits, s->cap, N, s->p.ax, s->p.ay, s->p.az);
         g_launches++;
+    }
+    if (guard) {
+        const float eps2f = (float)(c.softening * c.softening) * (1.f - 0x1p-22f);
+        const int ny = std::max(1, std::min(kGuardSplitMax, (int)grid_for(N, kBlock)));
+        const int persist = std::min<int>(sm_count() * 8, (int)grid_for(N, kBlock) * ny);
+        fix_bound_S<<<persist, kBlock, 0, s->stream>>>(fg->fpos, fg->list, fsc, N, eps2f, ny, fg->spart, fg->cap);
+        fix_bound_flag<<<std::min<int>(sm_count() * 8, (int)grid_for(N, kBlock)), kBlock, 0, s->stream>>>(
+            fg->fpos, fg->err, fg->list, fsc, N, eps2f, ny, fg->spart, fg->cap, s->p.ax, s->p.ay, s->p.az, fg->redo);
+        const double eps2 = c.softening * c.softening;
+        // short lists: a warp per (particle, chunk); long lists: 256-particle tiles
+        if (mode == kComp) {
+            fix_redo_warp<kComp><<<redo_grid(), kBlock, 0, s->stream>>>(s->p, N, c.G, eps2, fsc, fg->redo,
+                                                                       redo_warp_target(), fg->rpart);
+            fix_redo<kComp><<<redo_grid(), kBlock, 0, s->stream>>>(s->p, N, c.G, eps2, fsc, fg->redo, redo_target(),
+                                                                  fg->rpart);
+        } else {
+            fix_redo_warp<kBasic><<<redo_grid(), kBlock, 0, s->stream>>>(s->p, N, c.G, eps2, fsc, fg->redo,
+                                                                        redo_warp_target(), fg->rpart);
+            fix_redo<kBasic><<<redo_grid(), kBlock, 0, s->stream>>>(s->p, N, c.G, eps2, fsc, fg->redo, redo_target(),
+                                                                   fg->rpart);
+        }
+        fix_redo_warp_reduce<<<64, 256, 0, s->stream>>>(fg->rpart, fsc, fg->redo, N, redo_warp_target(), s->p.ax,
+                                                        s->p.ay, s->p.az);
+        fix_redo_reduce<<<std::min<int>(sm_count() * 4, (int)grid_for(N, 256)), 256, 0, s->stream>>>(
+            fg->rpart, fsc, fg->redo, N, redo_target(), s->p.ax, s->p.ay, s->p.az);
+        g_launches += 6;
+        RGPU_CUDA(s, cudaGetLastError());
     }
     return RGPU_OK;
 }
@@ -746,7 +1492,9 @@ extern "C" int rgpu_direct_accel_noalloc(const double* x, const double* y, const
     ParticlesSoA p{};
     p.x = const_cast<double*>(x); p.y = const_cast<double*>(y); p.z = const_cast<double*>(z);
     p.m = const_cast<double*>(m);
-    pack_j<<<grid_for(N, 256), 256, 0, st>>>(p, N, G, jpos, mode == kMixedSplit ? jsplit : nullptr);
+    const bool split2 = mode == kMixed || mode == kMixedSplit;
+    if (split2) pack_split2<<<grid_for((N + 1) / 2, 256), 256, 0, st>>>(p, N, G, reinterpret_cast<SplitPair*>(jsplit));
+    else pack_j<<<grid_for(N, 256), 256, 0, st>>>(p, N, G, jpos, nullptr);
     const int nbi = (N + kBlock - 1) / kBlock;
     int splits = choose_splits(nbi, N);
     if (splits > kNoAllocMaxSplits) splits = kNoAllocMaxSplits;
@@ -761,8 +1509,7 @@ extern "C" int rgpu_direct_accel_noalloc(const double* x, const double* y, const
     switch (mode) {
         case kBasic: launch_mode<kBasic, false>(grid, st, a); break;
         case kComp: launch_mode<kComp, false>(grid, st, a); break;
-        case kMixed: launch_mode<kMixed, false>(grid, st, a); break;
-        default: launch_mode<kMixedSplit, false>(grid, st, a); break;
+        default: launch_split2(mode, grid, st, a, reinterpret_cast<const SplitPair*>(jsplit)); break;
     }
     if (splits > 1) {
         if (mode == kComp)

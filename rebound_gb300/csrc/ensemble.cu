@@ -8,10 +8,18 @@
 // GPU's resident capacity drains a queue of 32-system work units ordered
 // largest body count first, so every SM stays busy until the cheapest units at
 // the end.  A chunk of `steps_per_launch` steps (counter reset + persistent
-// launch) is captured once into a CUDA graph and replayed.  An autotuner picks
-// the CTA size by timing short runs.
+// launch) is captured once into a CUDA graph and replayed.
+//
+// Second mapping, warp per system (whfast_warp.cuh, FMA flavour): lane i holds
+// body i, so one system's Kepler drifts and force rows run in parallel; a
+// persistent grid hands out single systems, largest first.  It wins when there
+// are too few systems to fill the GPU thread-per-system.  The autotuner times
+// both mappings (thread per system at 32 / 64 / 128 threads per CTA, warp per
+// system) and a set of steps-per-launch values on the live ensemble and keeps
+// the fastest combination.
 #define ENSEMBLE_NS ens_fast
 #include "ensemble_kernels.cuh"
+#include "whfast_warp.cuh"
 #include <algorithm>
 #include <cstring>
 #include <map>
@@ -32,6 +40,56 @@ struct EnsBucket {
     cudaStream_t stream = nullptr;
 };
 
+// One system for the warp mapping.
+struct WarpSys {
+    double* st;
+    const double* dt;
+    double* t;
+    int count, nb, sid, pad;
+};
+
+namespace {
+
+template <int NB>
+__device__ __noinline__ void warp_system(const WarpSys& S, int n_steps, double G, uint32_t* status) {
+    const double h = S.dt[S.sid];
+    whw::warp_steps<NB>(S.st, S.count, S.sid, n_steps, h, G, status);
+    if ((threadIdx.x & 31) == 0) S.t[S.sid] += h * n_steps;
+}
+
+// Persistent warp-per-system scheduler: each warp takes the next system from a
+// global counter (systems ordered by decreasing body count).
+__global__ void __launch_bounds__(128) persistent_warp_kernel(const WarpSys* __restrict__ sys, int n, int n_steps,
+                                                              double G, unsigned int* counter, uint32_t* status) {
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned int u = 0;
+        if (lane == 0) u = atomicAdd(counter, 1u);
+        u = __shfl_sync(0xffffffffu, u, 0);
+        if (u >= (unsigned)n) return;
+        const WarpSys S = sys[u];
+        switch (S.nb) {
+            case 2: warp_system<2>(S, n_steps, G, status); break;
+            case 3: warp_system<3>(S, n_steps, G, status); break;
+            case 4: warp_system<4>(S, n_steps, G, status); break;
+            case 5: warp_system<5>(S, n_steps, G, status); break;
+            case 6: warp_system<6>(S, n_steps, G, status); break;
+            case 7: warp_system<7>(S, n_steps, G, status); break;
+            case 8: warp_system<8>(S, n_steps, G, status); break;
+            case 9: warp_system<9>(S, n_steps, G, status); break;
+            case 10: warp_system<10>(S, n_steps, G, status); break;
+            case 11: warp_system<11>(S, n_steps, G, status); break;
+            case 12: warp_system<12>(S, n_steps, G, status); break;
+            case 13: warp_system<13>(S, n_steps, G, status); break;
+            case 14: warp_system<14>(S, n_steps, G, status); break;
+            case 15: warp_system<15>(S, n_steps, G, status); break;
+            default: warp_system<16>(S, n_steps, G, status); break;
+        }
+    }
+}
+
+}  // namespace
+
 struct rgpu_ensemble {
     std::vector<EnsBucket> b;
     std::vector<int64_t> offsets;      // n_systems + 1 particle offsets
@@ -40,7 +98,9 @@ struct rgpu_ensemble {
     int exact = 0;               // 1: no FMA contraction (bit-identical to the reference)
     int dh = 0;                  // 1: democratic heliocentric coordinates (implies exact)
     int block = 128;
+    int mapping = RGPU_ENSEMBLE_THREAD;  // RGPU_ENSEMBLE_THREAD or RGPU_ENSEMBLE_WARP
     int64_t steps_per_launch = 256;
+    WarpSys* d_wsys = nullptr;           // systems for the warp mapping, largest first
     cudaStream_t stream = nullptr;
     uint32_t* d_status = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr, fork = nullptr;
@@ -51,6 +111,7 @@ struct rgpu_ensemble {
     cudaGraphExec_t graph = nullptr;
     int64_t graph_steps = -1;
     int graph_block = -1;
+    int graph_mapping = -1;
     std::string msg;
 };
 
@@ -81,10 +142,24 @@ PersistentFn persistent_fn(const rgpu_ensemble* e) {
 // Enqueue one chunk of `n` steps for every system: the unit counter is reset and
 // a persistent grid (all SMs, occupancy-limited) drains the unit queue.
 int enqueue_chunk(rgpu_ensemble* e, int n) {
-    PersistentFn f = persistent_fn(e);
     int dev = 0, nsm = 1, per_sm = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e->mapping == RGPU_ENSEMBLE_WARP) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent_warp_kernel, 128, 0) != cudaSuccess ||
+            per_sm < 1) {
+            cudaGetLastError();
+            per_sm = 1;
+        }
+        const int ns = (int)e->n_systems;
+        const int grid = std::max(1, std::min(nsm * per_sm, (ns + 3) / 4));
+        ENS_CUDA(e, cudaMemsetAsync(e->d_counter, 0, sizeof(unsigned int), e->stream));
+        persistent_warp_kernel<<<grid, 128, 0, e->stream>>>(e->d_wsys, ns, n, e->G, e->d_counter, e->d_status);
+        g_launches++;
+        ENS_CUDA(e, cudaGetLastError());
+        return RGPU_OK;
+    }
+    PersistentFn f = persistent_fn(e);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, e->block, 0) != cudaSuccess || per_sm < 1) {
         cudaGetLastError();
         per_sm = 1;
@@ -101,7 +176,8 @@ int enqueue_chunk(rgpu_ensemble* e, int n) {
 }
 
 int build_graph(rgpu_ensemble* e, int64_t n) {
-    if (e->graph && e->graph_steps == n && e->graph_block == e->block) return RGPU_OK;
+    if (e->graph && e->graph_steps == n && e->graph_block == e->block && e->graph_mapping == e->mapping)
+        return RGPU_OK;
     if (e->graph) { cudaGraphExecDestroy(e->graph); e->graph = nullptr; }
     cudaGraph_t g;
     ENS_CUDA(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
@@ -114,6 +190,7 @@ int build_graph(rgpu_ensemble* e, int64_t n) {
     ENS_CUDA(e, ie);
     e->graph_steps = n;
     e->graph_block = e->block;
+    e->graph_mapping = e->mapping;
     return RGPU_OK;
 }
 
@@ -212,11 +289,16 @@ int rgpu_ensemble_create(rgpu_ensemble** out, const void* particles, size_t stri
             for (int f = 0; f < it->count; f += 32)
                 units.push_back(ens_fast::Unit{it->st, it->dt, it->t, it->count, it->nb, f, 0});
         e->n_units = (int)units.size();
+        std::vector<WarpSys> ws;
+        for (auto it = e->b.rbegin(); it != e->b.rend(); ++it)
+            for (int q = 0; q < it->count; q++) ws.push_back(WarpSys{it->st, it->dt, it->t, it->count, it->nb, q, 0});
         if (cudaMalloc(&e->d_units, sizeof(ens_fast::Unit) * units.size()) != cudaSuccess ||
+            cudaMalloc(&e->d_wsys, sizeof(WarpSys) * ws.size()) != cudaSuccess ||
             cudaMalloc(&e->d_counter, sizeof(unsigned int)) != cudaSuccess) {
             rc = RGPU_ERR_NOMEM;
         } else {
             cudaMemcpy(e->d_units, units.data(), sizeof(ens_fast::Unit) * units.size(), cudaMemcpyHostToDevice);
+            cudaMemcpy(e->d_wsys, ws.data(), sizeof(WarpSys) * ws.size(), cudaMemcpyHostToDevice);
         }
     }
     if (rc) { rgpu_ensemble_free(e); return rc; }
@@ -235,6 +317,7 @@ void rgpu_ensemble_free(rgpu_ensemble* e) {
     }
     for (auto j : e->joins) cudaEventDestroy(j);
     cudaFree(e->d_units);
+    cudaFree(e->d_wsys);
     cudaFree(e->d_counter);
     if (e->fork) cudaEventDestroy(e->fork);
     if (e->e0) cudaEventDestroy(e->e0);
@@ -250,6 +333,22 @@ int rgpu_ensemble_set_launch(rgpu_ensemble* e, int block, int64_t steps_per_laun
     if (!e || (block != 32 && block != 64 && block != 128) || steps_per_launch < 1) return RGPU_ERR_ARG;
     e->block = block;
     e->steps_per_launch = steps_per_launch;
+    return RGPU_OK;
+}
+
+int rgpu_ensemble_set_mapping(rgpu_ensemble* e, int mapping) {
+    if (!e || (mapping != RGPU_ENSEMBLE_THREAD && mapping != RGPU_ENSEMBLE_WARP)) return RGPU_ERR_ARG;
+    if (mapping == RGPU_ENSEMBLE_WARP && (e->exact || e->dh))
+        return ens_err(e, RGPU_ERR_UNSUPPORTED, "the warp-per-system mapping runs the FMA flavour (Jacobi) only");
+    e->mapping = mapping;
+    return RGPU_OK;
+}
+
+int rgpu_ensemble_get_launch(const rgpu_ensemble* e, int* mapping, int* block, int64_t* steps_per_launch) {
+    if (!e || !mapping || !block || !steps_per_launch) return RGPU_ERR_ARG;
+    *mapping = e->mapping;
+    *block = e->block;
+    *steps_per_launch = e->steps_per_launch;
     return RGPU_OK;
 }
 
@@ -271,28 +370,48 @@ int rgpu_ensemble_time_steps(rgpu_ensemble* e, int64_t n, double* ms) {
     return read_status(e);
 }
 
-// Autotuner: time `probe_steps` steps for each CTA size and keep the fastest;
-// then pick the largest steps-per-launch not above `max_steps_per_launch`
-// (more steps per launch amortise launches; the cap bounds time-to-first-result).
-// The probed steps advance the state (callers tune on a scratch copy).
+// Autotuner, on the live ensemble (the probed steps advance the state: callers
+// that need the initial state tune a scratch copy of the same systems).
+// 1. mapping and CTA size: thread per system at 32 / 64 / 128 threads per CTA,
+//    and warp per system (FMA flavour only), each timed over `probe_steps` steps
+//    after one untimed run (graph build);
+// 2. steps per launch for the winner: `max_steps_per_launch` / 16, / 4 and itself
+//    (at least 1), each timed over max_steps_per_launch steps; the fastest wins,
+//    the smaller value on a tie within 2 % (it bounds time-to-first-result).
 int rgpu_ensemble_autotune(rgpu_ensemble* e, int64_t probe_steps, int64_t max_steps_per_launch,
                            int* best_block, double* best_ms_per_step) {
     if (!e || probe_steps < 1 || max_steps_per_launch < 1) return RGPU_ERR_ARG;
-    const int blocks[3] = {32, 64, 128};
+    struct Choice { int mapping, block; };
+    std::vector<Choice> cands = {{RGPU_ENSEMBLE_THREAD, 32}, {RGPU_ENSEMBLE_THREAD, 64}, {RGPU_ENSEMBLE_THREAD, 128}};
+    if (!e->exact && !e->dh) cands.push_back({RGPU_ENSEMBLE_WARP, 128});
     double best = 1e300;
-    int bb = e->block;
-    for (int k = 0; k < 3; k++) {
-        e->block = blocks[k];
+    Choice bc = {e->mapping, e->block};
+    for (const Choice& c : cands) {
+        e->mapping = c.mapping;
+        e->block = c.block;
         e->steps_per_launch = probe_steps;
         double ms = 0.;
         RGPU_TRY(rgpu_ensemble_time_steps(e, probe_steps, &ms));   // includes graph build
         RGPU_TRY(rgpu_ensemble_time_steps(e, probe_steps, &ms));
-        if (ms < best) { best = ms; bb = blocks[k]; }
+        if (ms < best) { best = ms; bc = c; }
     }
-    e->block = bb;
-    e->steps_per_launch = max_steps_per_launch;
-    if (best_block) *best_block = bb;
-    if (best_ms_per_step) *best_ms_per_step = best / (double)probe_steps;
+    e->mapping = bc.mapping;
+    e->block = bc.block;
+    const int64_t spls[3] = {std::max<int64_t>(1, max_steps_per_launch / 16),
+                             std::max<int64_t>(1, max_steps_per_launch / 4), max_steps_per_launch};
+    double best_spl_ms = 1e300;
+    int64_t bspl = max_steps_per_launch;
+    for (int k = 0; k < 3; k++) {
+        if (k > 0 && spls[k] == spls[k - 1]) continue;
+        e->steps_per_launch = spls[k];
+        double ms = 0.;
+        RGPU_TRY(rgpu_ensemble_time_steps(e, spls[k], &ms));       // graph build
+        RGPU_TRY(rgpu_ensemble_time_steps(e, max_steps_per_launch, &ms));
+        if (ms < best_spl_ms * 0.98) { best_spl_ms = ms; bspl = spls[k]; }
+    }
+    e->steps_per_launch = bspl;
+    if (best_block) *best_block = bc.block;
+    if (best_ms_per_step) *best_ms_per_step = best_spl_ms / (double)max_steps_per_launch;
     return RGPU_OK;
 }
 

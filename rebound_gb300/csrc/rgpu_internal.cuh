@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stddef.h>
+#include <atomic>
 #include <string>
 #include <vector>
 #include "../../include/rebound_gb300.h"
@@ -25,6 +26,7 @@ struct ParticlesSoA {
 };
 
 struct TreeBuffers;      // tree.cu
+struct FixGuard;         // direct.cu
 struct SeiCache { double lastdt = 0., sindt = 0., tandt = 0., sindtz = 0., tandtz = 0.; };  // src/integrator_sei.c:91-101
 struct WhfastBuffers;    // whfast.cu
 
@@ -38,6 +40,7 @@ struct rgpu_sim {
     float4* jsplit = nullptr;          // (hi, lo) float split of x,y,z and G*m: 2 float4 per particle
     double* partial = nullptr;         // j-split partial accelerations [splits][3][cap]
     size_t partial_cap = 0;
+    FixGuard* fixg = nullptr;          // fixed-point exactness guard buffers (direct.cu)
     void* stage = nullptr;             // device staging for AoS upload/download
     size_t stage_cap = 0;
     uint32_t* d_status = nullptr;      // device error word
@@ -71,10 +74,17 @@ struct rgpu_sim {
     size_t dp_cap = 0;
     TreeBuffers* tree = nullptr;
     WhfastBuffers* wh = nullptr;
+    // velocity-dependent restitution for the hardsphere resolve (host callback)
+    double (*eps_fn)(void*, double) = nullptr;
+    void* eps_user = nullptr;
+    double resolve_ms = 0.;             // host wall time spent in the collision resolve
+    int64_t resolve_calls = 0;
     std::string msg;
 };
 
-extern int64_t g_launches;
+// Kernel launches of this library since load (worker threads and host callers
+// count concurrently, hence atomic).
+extern std::atomic<int64_t> g_launches;
 
 int set_error(rgpu_sim* s, int code, const std::string& what);
 int check_cuda(rgpu_sim* s, cudaError_t e, const char* what);
@@ -87,6 +97,7 @@ void ktimer_end(rgpu_sim* s);
 // direct.cu
 int direct_accel(rgpu_sim* s, int mode);
 int direct_energy(rgpu_sim* s, double* e);
+void direct_free(rgpu_sim* s);
 // tree.cu
 int tree_accel(rgpu_sim* s);
 int tree_collisions(rgpu_sim* s, rgpu_collision* out, size_t cap, size_t* n_found, bool device_only,

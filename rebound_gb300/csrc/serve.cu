@@ -14,7 +14,7 @@
 //    SoA, one CTA per (cluster, 256-particle tile), each thread summing its
 //    cluster's j-range in a fixed order.
 // Per-request results do not depend on which other requests share a tick.
-#include "whfast_core.cuh"
+#include "whfast_warp.cuh"
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -62,43 +62,7 @@ __global__ void __launch_bounds__(128) wh_slots_kernel(double* __restrict__ st, 
     remaining[sid] = rem - n;
 }
 
-// --- warp per system ---------------------------------------------------------------
-// The same WHFast step (safe_mode = 1, Jacobi coordinates, DEFAULT kernel) with
-// lane i of a warp holding body i, for latency: the Kepler drifts of all bodies
-// and each body's row of pair forces run side by side, and the Jacobi transforms
-// become mass-weighted prefix / suffix sums across lanes.  With C_i the centre of
-// mass of bodies 0..i-1, eta_i their mass and X the centre of mass of all bodies:
-//     q_i = x_i - C_i,    x_i = q_i + X - sum_{k >= i} (m_k / eta_{k+1}) q_k,
-// the closed forms of the recurrences of src/transformations.c:34-81 and :178-226
-// (summed in tree order here, so results agree with the serial form to rounding).
-constexpr unsigned kFull = 0xffffffffu;
-
-template <int NB>
-__device__ __forceinline__ double lane_prefix(double v, int lane) {     // inclusive, lanes >= NB hold 0
-#pragma unroll
-    for (int d = 1; d < NB; d <<= 1) {
-        const double t = __shfl_up_sync(kFull, v, d);
-        if (lane >= d) v += t;
-    }
-    return v;
-}
-
-template <int NB>
-__device__ __forceinline__ double lane_suffix(double v, int lane) {     // inclusive, lanes >= NB hold 0
-#pragma unroll
-    for (int d = 1; d < NB; d <<= 1) {
-        const double t = __shfl_down_sync(kFull, v, d);
-        if (lane + d < 32) v += t;
-    }
-    return v;
-}
-
-template <int NB>
-__device__ __forceinline__ double lane_exclusive(double v, int lane) {  // sum over lanes < lane
-    const double e = __shfl_up_sync(kFull, lane_prefix<NB>(v, lane), 1);
-    return lane == 0 ? 0. : e;
-}
-
+// --- warp per system (whfast_warp.cuh) -------------------------------------------
 // Advance WHFast slot `sid` of one bucket by up to `chunk` steps; called by a whole warp.
 template <int NB>
 __device__ __noinline__ void warp_advance(double* __restrict__ st, const double* __restrict__ dt,
@@ -108,105 +72,7 @@ __device__ __noinline__ void warp_advance(double* __restrict__ st, const double*
     const int64_t rem = remaining[sid];
     if (rem <= 0) return;
     const int nsteps = (int)(rem < chunk ? rem : chunk);
-    const size_t f = (size_t)NB * cap;
-    const bool on = lane < NB;
-    const size_t o = (size_t)(on ? lane : 0) * cap + sid;
-    double x = 0., y = 0., z = 0., vx = 0., vy = 0., vz = 0., m = 0.;
-    if (on) {
-        x = st[o]; y = st[f + o]; z = st[2 * f + o];
-        vx = st[3 * f + o]; vy = st[4 * f + o]; vz = st[5 * f + o]; m = st[6 * f + o];
-    }
-    const double h = dt[sid], h2 = h / 2.;
-    // masses are constant over a request: the prefix masses once
-    const double eta_in = lane_prefix<NB>(m, lane);                  // sum_{k <= i} m_k
-    const double up = __shfl_up_sync(kFull, eta_in, 1);                // every lane takes part in the shuffle
-    const double eta_ex = lane == 0 ? 0. : up;
-    const double Mi = 1. / __shfl_sync(kFull, eta_in, NB - 1);
-    const bool jac = on && lane > 0;                                 // lanes holding a Jacobi body
-    const double ei = jac ? 1. / eta_ex : 0.;
-    const double wf = jac ? m / eta_in : 0.;
-    const double mu = G * eta_in;
-    double mj[NB];
-#pragma unroll
-    for (int j = 0; j < NB; j++) mj[j] = __shfl_sync(kFull, m, j);
-    for (int k = 0; k < nsteps; k++) {
-        // inertial -> Jacobi (lane 0: centre of mass)
-        double qx, qy, qz, ux, uy, uz;
-        {
-            const double Px = lane_prefix<NB>(m * x, lane), Py = lane_prefix<NB>(m * y, lane),
-                         Pz = lane_prefix<NB>(m * z, lane);
-            const double Pvx = lane_prefix<NB>(m * vx, lane), Pvy = lane_prefix<NB>(m * vy, lane),
-                         Pvz = lane_prefix<NB>(m * vz, lane);
-            const double Ex = __shfl_up_sync(kFull, Px, 1), Ey = __shfl_up_sync(kFull, Py, 1),
-                         Ez = __shfl_up_sync(kFull, Pz, 1);
-            const double Evx = __shfl_up_sync(kFull, Pvx, 1), Evy = __shfl_up_sync(kFull, Pvy, 1),
-                         Evz = __shfl_up_sync(kFull, Pvz, 1);
-            const double Tx = __shfl_sync(kFull, Px, NB - 1), Ty = __shfl_sync(kFull, Py, NB - 1),
-                         Tz = __shfl_sync(kFull, Pz, NB - 1);
-            const double Tvx = __shfl_sync(kFull, Pvx, NB - 1), Tvy = __shfl_sync(kFull, Pvy, NB - 1),
-                         Tvz = __shfl_sync(kFull, Pvz, NB - 1);
-            if (lane == 0) {
-                qx = Tx * Mi; qy = Ty * Mi; qz = Tz * Mi; ux = Tvx * Mi; uy = Tvy * Mi; uz = Tvz * Mi;
-            } else {
-                qx = x - Ex * ei; qy = y - Ey * ei; qz = z - Ez * ei;
-                ux = vx - Evx * ei; uy = vy - Evy * ei; uz = vz - Evz * ei;
-            }
-        }
-        // drift dt/2: Kepler per Jacobi body, free drift of the centre of mass
-        if (jac) wh::kepler_solver(qx, qy, qz, ux, uy, uz, mu, h2, status);
-        else if (lane == 0) { qx += h2 * ux; qy += h2 * uy; qz += h2 * uz; }
-        // Jacobi -> inertial positions
-        {
-            const double Xc = __shfl_sync(kFull, qx, 0), Yc = __shfl_sync(kFull, qy, 0), Zc = __shfl_sync(kFull, qz, 0);
-            const double Wx = lane_suffix<NB>(wf * qx, lane), Wy = lane_suffix<NB>(wf * qy, lane),
-                         Wz = lane_suffix<NB>(wf * qz, lane);
-            x = (jac ? qx : 0.) + Xc - Wx; y = (jac ? qy : 0.) + Yc - Wy; z = (jac ? qz : 0.) + Zc - Wz;
-        }
-        // inertial accelerations, all pairs except (0, 1), no softening (src/gravity.c:195-257)
-        double ax = 0., ay = 0., az = 0.;
-#pragma unroll
-        for (int j = 0; j < NB; j++) {
-            const double xj = __shfl_sync(kFull, x, j), yj = __shfl_sync(kFull, y, j), zj = __shfl_sync(kFull, z, j);
-            if (on && j != lane && lane + j != 1) {
-                const double dx = x - xj, dy = y - yj, dz = z - zj;
-                const double r = sqrt(dx * dx + dy * dy + dz * dz);
-                const double pfj = -(G / (r * r * r)) * mj[j];
-                ax += pfj * dx; ay += pfj * dy; az += pfj * dz;
-            }
-        }
-        // kick in Jacobi coordinates (src/transformations.c:147-176, src/integrator_whfast.c:447-472)
-        {
-            const double Sx = lane_exclusive<NB>(m * ax, lane), Sy = lane_exclusive<NB>(m * ay, lane),
-                         Sz = lane_exclusive<NB>(m * az, lane);
-            if (jac) {
-                ux += h * (ax - Sx * ei); uy += h * (ay - Sy * ei); uz += h * (az - Sz * ei);
-                if (lane > 1) {
-                    const double rj2i = 1. / (qx * qx + qy * qy + qz * qz);
-                    const double pf = h * (sqrt(rj2i) * rj2i * G * eta_in);
-                    ux += pf * qx; uy += pf * qy; uz += pf * qz;
-                }
-            }
-        }
-        // drift dt/2
-        if (jac) wh::kepler_solver(qx, qy, qz, ux, uy, uz, mu, h2, status);
-        else if (lane == 0) { qx += h2 * ux; qy += h2 * uy; qz += h2 * uz; }
-        // Jacobi -> inertial positions and velocities
-        {
-            const double Xc = __shfl_sync(kFull, qx, 0), Yc = __shfl_sync(kFull, qy, 0), Zc = __shfl_sync(kFull, qz, 0);
-            const double Vx = __shfl_sync(kFull, ux, 0), Vy = __shfl_sync(kFull, uy, 0), Vz = __shfl_sync(kFull, uz, 0);
-            const double Wx = lane_suffix<NB>(wf * qx, lane), Wy = lane_suffix<NB>(wf * qy, lane),
-                         Wz = lane_suffix<NB>(wf * qz, lane);
-            const double Wvx = lane_suffix<NB>(wf * ux, lane), Wvy = lane_suffix<NB>(wf * uy, lane),
-                         Wvz = lane_suffix<NB>(wf * uz, lane);
-            x = (jac ? qx : 0.) + Xc - Wx; y = (jac ? qy : 0.) + Yc - Wy; z = (jac ? qz : 0.) + Zc - Wz;
-            vx = (jac ? ux : 0.) + Vx - Wvx; vy = (jac ? uy : 0.) + Vy - Wvy; vz = (jac ? uz : 0.) + Vz - Wvz;
-        }
-        if (!on) { x = y = z = vx = vy = vz = 0.; }
-    }
-    if (on) {
-        st[o] = x; st[f + o] = y; st[2 * f + o] = z;
-        st[3 * f + o] = vx; st[4 * f + o] = vy; st[5 * f + o] = vz;
-    }
+    whw::warp_steps<NB>(st, cap, sid, nsteps, dt[sid], G, status);
     if (lane == 0) remaining[sid] = rem - nsteps;
 }
 
@@ -712,24 +578,54 @@ void cluster_worker(rgpu_server* s) {
         }
         const std::vector<int64_t> tick_ids = resident;
         lk.unlock();
+        bool ok = true;
         if ((int)items.size() > s->items_cap) {
             cudaFree(s->d_items);
-            s->items_cap = (int)items.size() * 2;
-            cudaMalloc(&s->d_items, sizeof(ClusterItem) * s->items_cap);
+            s->d_items = nullptr;
+            s->items_cap = 0;
+            if (cudaMalloc(&s->d_items, sizeof(ClusterItem) * items.size() * 2) == cudaSuccess) {
+                s->items_cap = (int)items.size() * 2;
+            } else {
+                cudaGetLastError();
+                ok = false;
+            }
         }
-        cudaMemcpyAsync(s->d_items, items.data(), sizeof(ClusterItem) * items.size(), cudaMemcpyHostToDevice, st);
-        const dim3 grid(max_tiles, (unsigned)items.size());
-        for (int k = 0; k < max_steps; k++) {
-            cl_drift<<<grid, kT, 0, st>>>(s->pool, s->d_items, k, 0.5);
-            cl_split<<<grid, kT, 0, st>>>(s->pool, s->d_items, k);
-            cl_force<<<grid, kT, 0, st>>>(s->pool, s->d_items, k);
-            cl_kick_drift<<<grid, kT, 0, st>>>(s->pool, s->d_items, k);
-            g_launches += 4;
+        if (ok) {
+            ok = cudaMemcpyAsync(s->d_items, items.data(), sizeof(ClusterItem) * items.size(), cudaMemcpyHostToDevice,
+                                 st) == cudaSuccess;
+            const dim3 grid(max_tiles, (unsigned)items.size());
+            for (int k = 0; ok && k < max_steps; k++) {
+                cl_drift<<<grid, kT, 0, st>>>(s->pool, s->d_items, k, 0.5);
+                cl_split<<<grid, kT, 0, st>>>(s->pool, s->d_items, k);
+                cl_force<<<grid, kT, 0, st>>>(s->pool, s->d_items, k);
+                cl_kick_drift<<<grid, kT, 0, st>>>(s->pool, s->d_items, k);
+                g_launches += 4;
+                ok = cudaGetLastError() == cudaSuccess;
+            }
         }
-        cudaStreamSynchronize(st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) {
+            cudaGetLastError();
+            ok = false;
+        }
         std::vector<Request*> done_now;
         lk.lock();
         s->ticks++;
+        if (!ok) {
+            // the tick did not run: its requests fail with RGPU_ERR_CUDA and give back their pool range
+            s->msg = "cluster tick failed (device allocation, launch or stream error)";
+            std::vector<int64_t> keep;
+            for (int64_t id : resident)
+                if (std::find(tick_ids.begin(), tick_ids.end(), id) == tick_ids.end()) keep.push_back(id);
+            resident.swap(keep);
+            for (int64_t id : tick_ids) {
+                Request& r = s->req[id];
+                r.status = RGPU_ERR_CUDA;
+                pool_release(s, r.pool_off, r.n);
+                finish(s, r);
+            }
+            s->cv_done.notify_all();
+            continue;
+        }
         std::vector<int64_t> still;
         for (size_t q = 0; q < tick_ids.size(); q++) {
             Request& r = s->req[tick_ids[q]];

@@ -11,7 +11,7 @@
 #include <cstring>
 #include <new>
 
-int64_t g_launches = 0;
+std::atomic<int64_t> g_launches{0};
 
 int set_error(rgpu_sim* s, int code, const std::string& what) {
     if (s) s->msg = what;
@@ -447,6 +447,7 @@ void rgpu_sim_free(rgpu_sim* s) {
     tree_free(s);
     whfast_free(s);
     collide_free(s);
+    direct_free(s);
     cudaFree(s->soa_block);
     cudaFree(s->jpos);
     cudaFree(s->jsplit);
@@ -664,7 +665,7 @@ double rgpu_sim_last_kernel_ms(const rgpu_sim* s) {
     return (double)ms;
 }
 
-int64_t rgpu_launch_count(void) { return g_launches; }
+int64_t rgpu_launch_count(void) { return g_launches.load(); }
 
 int rgpu_sim_kernel_timer(rgpu_sim* s, int enable) {
     if (!s) return RGPU_ERR_ARG;

@@ -3,8 +3,8 @@
 Each system is what the reference runs as one `rebound.Simulation` with
 `integrator = "whfast"` (Jacobi coordinates, DEFAULT kernel, safe_mode = 1,
 src/integrator_whfast.c).  `Ensemble` packs them into the batched kernel of
-librebound_gb300 (thread per system, systems grouped by body count, chunks of
-steps captured in CUDA graphs, autotuned launch shape).
+librebound_gb300 (thread or warp per system, systems grouped by body count,
+chunks of steps captured in CUDA graphs, autotuned mapping and launch shape).
 """
 import ctypes
 import time
@@ -48,7 +48,21 @@ class Ensemble:
     def set_launch(self, block=128, steps_per_launch=256):
         self._check(self._L.rgpu_ensemble_set_launch(self._h, block, steps_per_launch))
 
+    MAPPINGS = {"thread": 0, "warp": 1}
+
+    def set_mapping(self, mapping):
+        """"thread": one thread per system (throughput); "warp": one warp per system (latency)."""
+        self._check(self._L.rgpu_ensemble_set_mapping(self._h, self.MAPPINGS[mapping]))
+
+    def launch(self):
+        """(mapping, CTA size, steps per launch) in effect."""
+        m, b, spl = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int64(0)
+        self._check(self._L.rgpu_ensemble_get_launch(self._h, ctypes.byref(m), ctypes.byref(b), ctypes.byref(spl)))
+        return {v: k for k, v in self.MAPPINGS.items()}[m.value], b.value, spl.value
+
     def autotune(self, probe_steps=16, max_steps_per_launch=512):
+        """Time every mapping x CTA size, then the steps per launch, on this ensemble
+        (advancing it) and keep the fastest; returns (CTA size, ms per step)."""
         b = ctypes.c_int(0)
         ms = ctypes.c_double(0)
         self._check(self._L.rgpu_ensemble_autotune(self._h, probe_steps, max_steps_per_launch,
@@ -126,27 +140,42 @@ def bench_summary(quick=False, n_systems=65536, steps=10000, seed=3):
     systems, periods = ics.planetary_systems(n_systems, seed=seed)
     dts = periods / 20.0
     e0 = np.array([energy_host(p) for p in systems[:512]])
-    ens = Ensemble(systems, dts)
-    # Autotune on a scratch copy (the probe steps advance the state).
-    scratch = Ensemble(systems[: min(n_systems, 8192)], dts[: min(n_systems, 8192)])
-    block, _ = scratch.autotune(probe_steps=8, max_steps_per_launch=500)
+    # Autotune (mapping, CTA size, steps per launch) on a scratch copy of the same
+    # systems (its probe steps advance the state), then run the tuned shape.
+    scratch = Ensemble(systems, dts)
+    scratch.autotune(probe_steps=8, max_steps_per_launch=500)
+    mapping, block, spl = scratch.launch()
     del scratch
-    ens.set_launch(block, 500)
-    ens.steps(10)                              # warm-up (graph build)
     ens = Ensemble(systems, dts)
-    ens.set_launch(block, 500)
+    ens.set_mapping(mapping)
+    ens.set_launch(block, spl)
     ms = ens.time_steps(steps)
     rate = n_systems * steps / (ms * 1e-3)
     e1 = ens.energies()[:512]
     rel = np.abs((e1 - e0) / e0)
-    # Plain path on a sample of systems, same steps per system scaled down.
+    # Plain path on a sample of systems, and the energy error of both paths on
+    # that sample after the same number of steps (the batched run repeated for
+    # the sample alone, so both start from the same state).
     sample = min(32, n_systems)
-    plain_steps = 200 if not quick else 50
-    plain_rate, _ = plain_path_rate(systems[:sample], dts[:sample], plain_steps)
-    return {"systems": n_systems, "steps": steps, "k_range": [2, 10], "block": block, "steps_per_launch": 500,
+    plain_steps = 500 if not quick else 50
+    plain_rate, e_plain = plain_path_rate(systems[:sample], dts[:sample], plain_steps)
+    e0s = e0[:sample]
+    small = Ensemble(systems[:sample], dts[:sample])
+    small.set_mapping(mapping)
+    small.set_launch(block, spl)
+    small.steps(plain_steps)
+    rel_plain = np.abs((e_plain - e0s) / e0s)
+    rel_batched = np.abs((small.energies() - e0s) / e0s)
+    return {"systems": n_systems, "steps": steps, "k_range": [2, 10], "mapping": mapping, "block": block,
+            "steps_per_launch": spl, "launch_chosen_by": "rgpu_ensemble_autotune",
             "system_steps_per_s": rate, "seconds": ms * 1e-3,
             "energy_rel_err_median": float(np.median(rel)), "energy_rel_err_p99": float(np.quantile(rel, 0.99)),
             "energy_sample": int(len(rel)),
             "plain_path_system_steps_per_s": plain_rate,
             "plain_path_sample": f"{sample} systems x {plain_steps} steps, one C-ABI call per step",
+            "matching_energy_error": {"systems": sample, "steps": plain_steps,
+                                      "plain_median": float(np.median(rel_plain)),
+                                      "plain_max": float(rel_plain.max()),
+                                      "batched_median": float(np.median(rel_batched)),
+                                      "batched_max": float(rel_batched.max())},
             "speedup_vs_plain": rate / plain_rate}

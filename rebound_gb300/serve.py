@@ -151,6 +151,42 @@ def run_stream(reqs, rate, seed=9, server=None, deadline_s=900.0):
     return lat, results, makespan, st
 
 
+def run_stream_bounded(reqs, rate, wall_s, seed=9):
+    """Submit `reqs` with Poisson arrivals at `rate` per second and stop waiting
+    `wall_s` seconds after the first submission.  Returns the server-side latency
+    of every request that finished by then (NaN for the others), the number still
+    in flight, the elapsed time and the server's counters."""
+    srv = Server()
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, size=len(reqs))
+    ids = []
+    t0 = time.perf_counter()
+    next_t = t0
+    for r, g in zip(reqs, gaps):
+        next_t += g
+        d = next_t - time.perf_counter()
+        if d > 0:
+            time.sleep(d)
+        ids.append(srv.submit(*r))
+    lat = np.full(len(reqs), np.nan)
+    pending = list(range(len(reqs)))
+    while pending and time.perf_counter() - t0 < wall_s:
+        still = []
+        for q in pending:
+            try:
+                _, lat[q] = srv.wait(ids[q], timeout=0.05)
+            except RGPUError as e:
+                if e.code != 11:
+                    srv.close()
+                    raise
+                still.append(q)
+        pending = still
+    elapsed = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    return lat, len(pending), elapsed, st
+
+
 def plain_rate(reqs, max_whfast=8, steps_cap=400, clusters=2, cluster_steps_cap=20):
     """System-steps/s and pair-int/s of the plain path (one rgpu_sim per request,
     one C-ABI call per step) on a sample of the stream with capped steps."""
@@ -183,29 +219,34 @@ def plain_rate(reqs, max_whfast=8, steps_cap=400, clusters=2, cluster_steps_cap=
             "cluster_pair_int_per_s": pairs / cl_time if cl_time else None}
 
 
-def bench_summary(quick=False, n_requests=400, rates=(100.0, 400.0), t_end_periods=(1e2, 1e3)):
-    """Served stream: 80 % WHFast systems, 20 % Plummer clusters, Poisson arrivals.
-    End times are drawn log-uniform in [1e2, 1e3] inner periods (the configured
-    range reaches 1e5 periods, i.e. 2e6 steps per request, minutes per request
-    on one GPU thread; the scaled range keeps the run to about a minute and
-    is reported in the output)."""
+def bench_summary(quick=False, n_requests=240, rates=(100.0,), t_end_periods=(1e2, 1e5), wall_s=120.0):
+    """Served stream of the configuration: 80 % WHFast systems with end times
+    log-uniform in [1e2, 1e5] inner periods (2e3 to 2e6 steps each), 20 % Plummer
+    clusters, Poisson arrivals.  The run is bounded by the request count and by
+    `wall_s` seconds of wall time: p50 / p99 are over the requests that finished,
+    and the number still in flight at the end is reported beside them."""
     if quick:
-        n_requests, rates, t_end_periods = 60, (200.0,), (1e2, 3e2)
+        n_requests, t_end_periods, wall_s = 60, (1e2, 1e3), 60.0
     reqs = make_stream(n_requests, t_end_periods=t_end_periods)
     wh_steps = sum(r[3] for r in reqs if r[0] == WHFAST)
     cl_pairs = sum(r[3] * len(r[1]) * (len(r[1]) - 1.0) for r in reqs if r[0] == CLUSTER)
     out = {"requests": n_requests, "whfast_requests": sum(r[0] == WHFAST for r in reqs),
            "t_end_inner_periods": list(t_end_periods), "whfast_system_steps": wh_steps,
            "cluster_pair_interactions": cl_pairs, "runs": []}
+    kinds = np.array([r[0] for r in reqs])
+    steps = np.array([r[3] for r in reqs], dtype=np.float64)
     for rate in rates:
-        lat, _, makespan, st = run_stream(reqs, rate)
-        kinds = np.array([r[0] for r in reqs])
-        out["runs"].append({"rate_per_s": rate, "p50_latency_s": float(np.quantile(lat, 0.5)),
-                            "p99_latency_s": float(np.quantile(lat, 0.99)),
-                            "p50_latency_whfast_s": float(np.quantile(lat[kinds == WHFAST], 0.5)),
-                            "p50_latency_cluster_s": float(np.quantile(lat[kinds == CLUSTER], 0.5)),
-                            "makespan_s": makespan,
-                            "system_steps_per_s": wh_steps / makespan, "pair_int_per_s": cl_pairs / makespan,
+        lat, in_flight, elapsed, st = run_stream_bounded(reqs, rate, wall_s)
+        ok = np.isfinite(lat)
+        q = lambda m, f: float(np.quantile(lat[ok & m], f)) if np.any(ok & m) else None
+        out["runs"].append({"rate_per_s": rate, "completed": int(ok.sum()), "in_flight_at_end": int(in_flight),
+                            "wall_s": elapsed, "p50_latency_s": q(ok, 0.5), "p99_latency_s": q(ok, 0.99),
+                            "p50_latency_whfast_s": q(kinds == WHFAST, 0.5),
+                            "p99_latency_whfast_s": q(kinds == WHFAST, 0.99),
+                            "p50_latency_cluster_s": q(kinds == CLUSTER, 0.5),
+                            "max_steps_completed": float(steps[ok].max()) if ok.any() else 0.0,
+                            "system_steps_per_s": st["system_steps"] / elapsed,
+                            "pair_int_per_s": st["pair_interactions"] / elapsed,
                             "ticks": st["ticks"]})
     plain = plain_rate(reqs)
     out["plain_path"] = plain

@@ -24,6 +24,9 @@ _CFG_INTS = ("testparticle_type", "N_root_x", "N_root_y", "N_root_z", "N_ghost_x
              "exact_finish_time")
 
 
+_RESTITUTION_FN = ctypes.CFUNCTYPE(ctypes.c_double, ctypes.c_void_p, ctypes.c_double)
+
+
 class Collision(Exception):
     """An integration stopped because two particles collided and collision_resolve
     is "halt" (rebound's Collision exception)."""
@@ -121,6 +124,16 @@ class Simulation:
         raise AttributeError(name)
 
     def __setattr__(self, name, value):
+        if name == "coefficient_of_restitution" and callable(value):
+            # velocity-dependent restitution, called as value(sim, v) for each resolved
+            # pair (rebound/simulation.py: sim.coefficient_of_restitution = f)
+            cb = _RESTITUTION_FN(lambda _user, v: float(value(self, v)))
+            object.__setattr__(self, "_eps_cb", cb)
+            check(self._L.rgpu_sim_set_restitution_fn(self._h, ctypes.cast(cb, ctypes.c_void_p), None), self._h)
+            return
+        if name == "coefficient_of_restitution" and self.__dict__.get("_eps_cb") is not None:
+            check(self._L.rgpu_sim_set_restitution_fn(self._h, None, None), self._h)
+            object.__setattr__(self, "_eps_cb", None)
         if name in _CFG_FLOATS:
             setattr(self._cfg, name, float(value))
         elif name in _CFG_INTS:
@@ -160,6 +173,17 @@ class Simulation:
     @property
     def collisions_log_n(self):
         return self._cfg.collisions_log_n
+
+    @property
+    def collisions_plog(self):
+        """Y-momentum transferred by hardsphere collisions (src/collision.c:655-662)."""
+        return self._cfg.collisions_plog
+
+    def resolve_time(self):
+        """(host milliseconds spent resolving collisions, number of resolves)."""
+        ms, n = ctypes.c_double(0.), ctypes.c_int64(0)
+        check(self._L.rgpu_sim_resolve_time(self._h, ctypes.byref(ms), ctypes.byref(n)), self._h)
+        return ms.value, n.value
 
     def configure_box(self, root_size, N_root_x=1, N_root_y=1, N_root_z=1):
         self._cfg.root_size = float(root_size)
@@ -308,6 +332,13 @@ class Simulation:
 
     def last_kernel_ms(self):
         return self._L.rgpu_sim_last_kernel_ms(self._h)
+
+    def guard_stats(self):
+        """(bodies off the fixed-point grid, particles recomputed in FP64) of the last
+        BASIC / COMPENSATED fixed-point force evaluation; (-1, -1) before one."""
+        a, b = ctypes.c_int64(0), ctypes.c_int64(0)
+        check(self._L.rgpu_sim_guard_stats(self._h, ctypes.byref(a), ctypes.byref(b)), self._h)
+        return a.value, b.value
 
     # ---- snapshots (Simulationarchive counterpart) --------------------------
     def save_to_file(self, filename, interval=None, step=None, delete_file=False):

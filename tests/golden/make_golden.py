@@ -19,7 +19,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("REBOUND_REF", "/root/reference")
+if len(sys.argv) < 2 and not os.environ.get("REBOUND_REF"):
+    sys.exit("usage: make_golden.py <reference checkout> [fixture ...]  (or set REBOUND_REF)")
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ["REBOUND_REF"]
 sys.dont_write_bytecode = True
 sys.path[:0] = [os.path.join(REPO, "oracle", "_ref"), REF, REPO]
 
@@ -146,6 +148,56 @@ def fixture_gravity_cases():
     np.savez_compressed(os.path.join(HERE, "gravity_cases.npz"), **out)
 
 
+def fixture_gravity_hierarchical():
+    """BASIC and COMPENSATED accelerations of hierarchical systems, whose small
+    coordinates lie far below the largest one: a tight binary near the origin in
+    a wide system, a cluster at the origin beside a distant body, and the
+    configuration-1 Plummer sphere with a tight binary at its centre."""
+    rng = np.random.default_rng(21)
+    cases = {}
+    # tight binary (separation ~3.7e-7) at ~4e-4 from the origin, 30 field bodies out to ~1e2, one body at 1e3
+    p = np.zeros(33, dtype=PARTICLE_DTYPE)
+    c = np.array([1e-4, -2e-4, 3e-4])
+    h = np.array([3e-7, 1e-7, -2e-7]) * 0.5
+    p[0]["x"], p[0]["y"], p[0]["z"] = c + h
+    p[1]["x"], p[1]["y"], p[1]["z"] = c - h
+    r = 10 ** rng.uniform(-2, 2, 30)
+    u = rng.normal(size=(30, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    for k, f in enumerate(("x", "y", "z")):
+        p[f][2:32] = r * u[:, k]
+    p[32]["x"] = 1e3
+    p["m"] = rng.uniform(0.5, 1.5, 33) * 1e-3
+    cases["binary_wide"] = (p, 0.0)
+    # cluster of 2048 at the origin (sigma 1e-2) beside one body at 1e3
+    n = 2048
+    q = np.zeros(n, dtype=PARTICLE_DTYPE)
+    q["x"], q["y"], q["z"] = rng.standard_normal((3, n)) * 1e-2
+    q["x"][0] = 1e3
+    q["m"] = 1.0 / n
+    cases["cluster_far"] = (q, 0.0)
+    # the N=4,096 Plummer sphere with a tight binary (separation 2e-6) near its centre
+    pl = plummer_truncated(4096, 11)
+    b = np.zeros(2, dtype=PARTICLE_DTYPE)
+    cb = np.array([2.5e-3, -1.5e-3, 1e-3])
+    hb = np.array([1e-6, -5e-7, 5e-7])
+    b[0]["x"], b[0]["y"], b[0]["z"] = cb + hb
+    b[1]["x"], b[1]["y"], b[1]["z"] = cb - hb
+    b["m"] = 1.0 / 4096
+    cases["plummer_binary"] = (np.concatenate([pl, b]), 0.0)
+    out = {}
+    for name, (arr, soft) in cases.items():
+        out[name + "_particles"] = arr
+        out[name + "_softening"] = np.float64(soft)
+        for mode in ("basic", "compensated"):
+            sim = rebound.Simulation()
+            sim.softening = soft
+            sim.gravity = mode
+            load(sim, arr)
+            out[f"{name}_acc_{mode}"] = accel(sim)
+    np.savez_compressed(os.path.join(HERE, "gravity_hierarchical.npz"), **out)
+
+
 def ring_patch(L, seed, omega=1.3143527e-4, surface_density=400., rho=400.):
     """Config-3 style shearing-sheet patch (examples/shearing_sheet/problem.c pattern)."""
     sim = rebound.Simulation()
@@ -253,6 +305,20 @@ def fixture_ring():
     out["after5_t"] = np.float64(sim2.t)
     out["after5_seed"] = np.int64(sim2.rand_seed)
     out["after5_collisions_log_n"] = np.int64(sim2.collisions_log_n)
+    out["after5_collisions_plog"] = np.float64(sim2.collisions_plog)
+    # The same five steps with the velocity-dependent restitution coefficient of the
+    # reference's own shearing-sheet test (rebound/tests/test_shearingsheet.py:26-32).
+    sim3 = ring_patch(200.0, seed=7)
+
+    def cor_bridges(r, v):
+        eps = 0.32 * pow(abs(v) * 100., -0.234)
+        return min(1., max(0., eps))
+    sim3.coefficient_of_restitution = cor_bridges
+    sim3.steps(5)
+    out["bridges_after5"] = state(sim3)
+    out["bridges_after5_seed"] = np.int64(sim3.rand_seed)
+    out["bridges_after5_collisions_log_n"] = np.int64(sim3.collisions_log_n)
+    out["bridges_after5_collisions_plog"] = np.float64(sim3.collisions_plog)
     np.savez_compressed(os.path.join(HERE, "ring_patch.npz"), **out)
 
 
@@ -842,7 +908,7 @@ if __name__ == "__main__":
     which = sys.argv[2:] or ["gravity_cases", "ring", "whfast", "sei", "gravity_plummer", "reference_cases",
                              "leapfrog_orders", "whfast_dh", "whfast_advanced", "whfast_coords",
                              "archive_cases", "collision_line", "tree_quadrupole",
-                             "whfast_gravity"]
+                             "whfast_gravity", "gravity_hierarchical"]
     for w in which:
         print("generating", w, flush=True)
         globals()["fixture_" + w]() if w != "sei" else fixture_sei_periodic()

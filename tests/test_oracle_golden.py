@@ -65,6 +65,15 @@ def ring_sim(g):
                  opening_angle2=oa2, t=t)
 
 
+@pytest.mark.parametrize("case", ["binary_wide", "cluster_far", "plummer_binary"])
+def test_oracle_gravity_hierarchical(case):
+    # small coordinates far below the largest one (the inputs of the fixed-point guard)
+    g = golden("gravity_hierarchical.npz")
+    s = O.Sim(g[case + "_particles"], softening=float(g[case + "_softening"]))
+    for mode in ("basic", "compensated"):
+        assert np.array_equal(s.gravity(mode), g[f"{case}_acc_{mode}"]), (case, mode)
+
+
 def test_oracle_tree_cells_and_gravity():
     g = golden("ring_patch.npz")
     s = ring_sim(g)
@@ -86,6 +95,14 @@ def test_oracle_collision_pairs(mode):
     pr = ring_sim(g).collisions(mode)
     assert len(pr) == len(g["pairs_" + mode]) > 0
     assert pair_key(pr) == pair_key(g["pairs_" + mode])
+
+
+def test_oracle_tree_search_threads_keep_the_serial_order():
+    # the OpenMP split of the tree search returns the serial list entry for entry
+    g = golden("ring_patch.npz")
+    s = ring_sim(g)
+    a, b = s.collisions("tree"), s.collisions("tree_omp")
+    assert len(a) == len(b) > 0 and a.tobytes() == b.tobytes()
 
 
 def test_oracle_kepler_solver():

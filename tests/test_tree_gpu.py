@@ -99,9 +99,38 @@ def test_sei_tree_collisions_hardsphere_trajectory(gpu):
     assert sim.t == g["after5_t"]
     assert sim.collisions_log_n == g["after5_collisions_log_n"]
     assert sim.rand_seed == g["after5_seed"]
+    # y-momentum transferred by the collisions (src/collision.c:655-662)
+    assert abs(sim.collisions_plog - g["after5_collisions_plog"]) <= 1e-10 * abs(g["after5_collisions_plog"])
     for f in XV:
         scale = np.abs(ref[f]).max()
         assert np.abs(p[f] - ref[f]).max() <= 1e-12 * scale, f
+
+
+def test_velocity_dependent_restitution(gpu):
+    # The reference's shearing-sheet restitution law (rebound/tests/test_shearingsheet.py:26-32),
+    # called on the host for each collision as REBOUND calls r->coefficient_of_restitution.
+    g = golden("ring_patch.npz")
+    sim = ring_gpu(gpu, g)
+    sim.collision = "tree"
+    sim.collision_resolve = "hardsphere"
+    calls = []
+
+    def cor_bridges(r, v):
+        calls.append(v)
+        eps = 0.32 * pow(abs(v) * 100., -0.234)
+        return min(1., max(0., eps))
+    sim.coefficient_of_restitution = cor_bridges
+    sim.rand_seed = int(g["after5_seed0"])
+    sim.steps(5)
+    p, ref = sim.particles, g["bridges_after5"]
+    assert sim.collisions_log_n == g["bridges_after5_collisions_log_n"] == len(calls)
+    assert sim.rand_seed == g["bridges_after5_seed"]
+    assert abs(sim.collisions_plog - g["bridges_after5_collisions_plog"]) <= 1e-10 * abs(g["bridges_after5_collisions_plog"])
+    for f in XV:
+        scale = np.abs(ref[f]).max()
+        assert np.abs(p[f] - ref[f]).max() <= 1e-12 * scale, f
+    ms, n = sim.resolve_time()
+    assert 1 <= n <= 5 and ms > 0
 
 
 def test_sei_basic_shear_trajectory(gpu):
@@ -196,6 +225,14 @@ def test_full_size_ring_patch(gpu):
     got = set(zip(inner["p1"].tolist(), inner["p2"].tolist()))
     exp = set(zip(i[ok].tolist(), j[ok].tolist()))
     assert got == exp
+    # the whole list, ghost-box pairs included, entry for entry in the reference's
+    # serial discovery order (the oracle's search, its particle loop split over
+    # OpenMP threads and joined in order)
+    ref_pairs = orc.collisions("tree_omp")
+    assert len(pairs) == len(ref_pairs)
+    assert np.any(np.any(ref_pairs["gb"] != 0, axis=1))
+    for f in ("p1", "p2", "gb"):
+        assert np.array_equal(pairs[f], ref_pairs[f]), f
 
 
 def test_tree_split_mode_matches_exact_walk(gpu):

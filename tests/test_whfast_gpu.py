@@ -121,3 +121,49 @@ def test_ensemble_many_systems_matches_plain(gpu):
         sim = plain(gpu, systems[s], dts[s])
         sim.steps(50)
         assert max_diff(sim.particles, out[s]) == 0.0, s
+
+
+def test_ensemble_warp_mapping_matches_thread_mapping(gpu):
+    # The warp-per-system mapping (lane i holds body i) runs the same WHFast step
+    # with its sums in tree order: it tracks the thread-per-system run of the same
+    # systems to rounding, and keeps the reference's energy error within 2x.
+    from rebound_gb300.ensemble import Ensemble
+    g = golden("whfast.npz")
+    systems = [g[f"sys{s}_p0"] for s in range(8)]
+    dts = [g[f"sys{s}_meta"][0] for s in range(8)]
+    a = Ensemble(systems, dts)
+    b = Ensemble(systems, dts)
+    b.set_mapping("warp")
+    assert b.launch()[0] == "warp"
+    b.set_launch(128, 37)                         # ragged chunking
+    a.steps(1000)
+    b.steps(1000)
+    eb = b.energies()
+    for s, (pa, pb) in enumerate(zip(a.particles(), b.particles())):
+        dt, e0, e1 = g[f"sys{s}_meta"]
+        assert abs((eb[s] - e0) / e0) <= 2 * abs((e1 - e0) / e0) + 1e-15, s
+        for f in ("x", "y", "z"):
+            assert np.abs(pa[f] - pb[f]).max() <= 1e-9 * np.abs(pa[f]).max(), (s, f)
+    assert np.allclose(b.times(), np.array(dts) * 1000)
+    with pytest.raises(Exception):
+        Ensemble(systems, dts, exact=True).set_mapping("warp")   # FMA flavour only
+
+
+def test_ensemble_autotune_chooses_mapping_and_steps_per_launch(gpu):
+    from rebound_gb300.ensemble import Ensemble
+    systems, periods = gpu.ics.planetary_systems(40, seed=23)
+    dts = periods / 20.0
+    ens = Ensemble(systems, dts)
+    block, ms = ens.autotune(probe_steps=4, max_steps_per_launch=64)
+    mapping, b, spl = ens.launch()
+    assert mapping in ("thread", "warp") and b == block and spl in (4, 16, 64) and ms > 0
+    # with 40 systems one thread each leaves the GPU nearly idle: the tuner takes warps
+    assert mapping == "warp", (mapping, b, spl)
+    ref = Ensemble(systems, dts)
+    ref.steps(64)
+    ens2 = Ensemble(systems, dts)
+    ens2.set_mapping(mapping)
+    ens2.set_launch(b, spl)
+    ens2.steps(64)
+    for pa, pb in zip(ref.particles(), ens2.particles()):
+        assert np.abs(pa["x"] - pb["x"]).max() <= 1e-9 * np.abs(pa["x"]).max()

@@ -19,6 +19,8 @@ from conftest import rel_err_vec
 pytestmark = pytest.mark.gpu
 FP64_TOL = 1e-14
 BASIC, COMPENSATED = 1, 2
+MIXED, MIXED_SPLIT = 64, 65
+NAMES = {BASIC: "basic", COMPENSATED: "compensated", MIXED: "mixed", MIXED_SPLIT: "mixed_split"}
 
 
 def noalloc_accel(R, torch, p, gravity, softening):
@@ -36,7 +38,7 @@ def noalloc_accel(R, torch, p, gravity, softening):
 
 def allocating_accel(R, p, gravity, softening):
     sim = R.Simulation()
-    sim.gravity = {BASIC: "basic", COMPENSATED: "compensated"}[gravity]
+    sim.gravity = NAMES[gravity]
     sim.softening = softening
     sim.add(p)
     sim.update_acceleration()
@@ -54,6 +56,20 @@ def test_noalloc_matches_allocating_entry_point_twice(gpu):
         assert np.all(np.isfinite(a))
         err = rel_err_vec(a, ref)
         assert err.max() <= FP64_TOL, (len(p), gravity, err.max())
+
+
+def test_noalloc_mixed_forms_twice(gpu):
+    # MIXED_SPLIT keeps its float split in its own region of the scratch array;
+    # both mixed forms against the allocating path at the mixed-precision budget
+    # of the other gravity tests (median <= 1e-6, max <= 1e-3), two calls in a row.
+    torch = pytest.importorskip("torch")
+    R = gpu
+    for p in (R.ics.plummer(4096, seed=23), R.ics.plummer(2999, seed=24)):
+        for gravity in (MIXED, MIXED_SPLIT):
+            a = noalloc_accel(R, torch, p, gravity, 0.01)
+            ref = allocating_accel(R, p, BASIC, 0.01)
+            err = rel_err_vec(a, ref)
+            assert np.median(err) <= 1e-6 and err.max() <= 1e-3, (len(p), gravity, np.median(err), err.max())
 
 
 def test_noalloc_rejects_sizes_beyond_its_maximum(gpu):
