@@ -170,9 +170,13 @@ def run_reference(args):
             times.append(el)
     rate = rows * (n - 1) * len(times) / sum(times) / 1e9
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    sample = f"{rows} of {n} i-rows x {n} j-bodies per step (oracle port of the OpenMP BASIC gather, src/gravity.c:215-233)"
+    sample = (f"{rows} of {n} i-rows x {n} j-bodies per step (oracle port of the OpenMP BASIC gather, "
+              f"src/gravity.c:215-233, timing build); the reference's own C is not on the GPU machine")
+    # ms_per_step is the time of one sampled step (what this run spent per step);
+    # a full N^2 evaluation at the same rate is given beside it.
     out = {"metric": METRIC, "value": rate, "unit": "Gpair-int/s", "impl": "reference", "n_gpus": world,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n * (n - 1) / (rate * 1e9),
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+           "ms_per_full_step_est": 1e3 * n * (n - 1) / (rate * 1e9), "sample_fraction": rows / n,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded Plummer sphere)", "config": config_block(n, 1),
            "cpu_baseline": {"value": rate, "unit": "Gpair-int/s", "cores": cores, "kind": "port", "sample": sample},
@@ -331,7 +335,7 @@ def run_gb300(args):
             extra["ensemble"] = {"error": repr(ex)}
     if args.tree and rank == 0 and not args.lite:
         try:
-            extra["tree"] = tree_summary(quick=args.quick)
+            extra["tree"] = tree_summary(quick=args.quick, sm_count=sm_count, sm_mhz=(clk or {}).get("sm_mhz"))
         except Exception as ex:
             extra["tree"] = {"error": repr(ex)}
     if args.serve and rank == 0 and not args.lite:
@@ -363,7 +367,10 @@ def run_gb300(args):
     return 0
 
 
-def tree_summary(quick=False, steps=2):
+TREE_COUNTS_FILE = os.path.join(REPO, "profiles", "tree_walk_counts.json")
+
+
+def tree_summary(quick=False, steps=2, sm_count=None, sm_mhz=None):
     """Configuration-3 ring patch: SEI, tree gravity (opening angle 0.5, 25 ghost
     boxes), shear boundary, tree collision search + hardsphere (epsilon 0.5).
     Device-timed full steps, a split of gravity / collision time, and the oracle
@@ -400,6 +407,9 @@ def tree_summary(quick=False, steps=2):
         R._lib.check(L.rgpu_sim_time_steps(h, 1, ctypes.byref(ms)), h)
         times.append(ms.value)
     step_s = sum(times) / len(times) / 1e3
+    rms, rcalls = sim.resolve_time()
+    resolve = {"host_ms_per_step": rms / max(1, steps + 1), "share_of_step": rms / max(1, steps + 1) / (1e3 * step_s),
+               "collisions_per_step": sim.collisions_log_n / (steps + 1)}
     g = make()
     g.collision = "none"
     t0 = time.perf_counter()
@@ -442,8 +452,28 @@ def tree_summary(quick=False, steps=2):
     cpu_rows_s = time.perf_counter() - t0
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     cpu_grav_step_s = cpu_rows_s / rows * len(p)
+    # Roofline of the exact walk: FP64-pipe lane instructions per (particle, ghost
+    # box, root) visit from the committed ncu count (valid while tree.cu and
+    # exactfp.cuh hash to the recorded digest) x the visits of one walk / the
+    # walk's time, against the nominal FP64 pipe rate at the sampled clock.
+    roof = {"bound": "fp64", "kernel": "walk_exact", "unit": "Tinst/s (FP64-pipe lane instructions)"}
+    try:
+        with open(TREE_COUNTS_FILE) as f:
+            rec = json.load(f)
+        if sources_digest(rec["sources"]) == rec["sha256"]:
+            visits = len(p) * 25 * n_root * n_root
+            ach = rec["fp64_lane_inst_per_root_visit"] * visits / grav_s / 1e12
+            peak = nominal_fp64_tflops(sm_count, sm_mhz) / 2 if sm_mhz else None
+            roof.update({"achieved": ach, "peak": peak, "frac": ach / peak if peak else None,
+                         "visits_per_walk": visits, "inst_per_visit": rec["fp64_lane_inst_per_root_visit"],
+                         "peak_source": "nominal FP64 pipe rate (0.5 lanes/clock/SMSP) at the sampled SM clock"})
+        else:
+            roof["counts"] = "tree sources changed since the ncu capture (sha256 mismatch)"
+    except (OSError, ValueError, KeyError) as ex:
+        roof["counts"] = repr(ex)
     return {"workload": f"ring patch {box:.0f} m box, N={len(p)}, 25 ghost boxes, {n_root * n_root} roots",
             "N": len(p), "gpu_step_s": step_s, "gpu_tree_gravity_s": grav_s, "gpu_collision_search_s": coll_s,
+            "roofline": roof, "resolve": resolve,
             "split_mode": {"gpu_step_s": split_step_s, "gpu_tree_gravity_s": split_s,
                            "steps_per_s": 1.0 / split_step_s,
                            "median_rel_diff_vs_exact_walk": float(np.median(split_err)),
@@ -532,6 +562,48 @@ def c5_cluster_drift(steps=1000):
         p = R.ics.plummer(n, seed=1000 + n)
         out[str(n)] = form_drift(p, 0.01, 1e-3, steps, forms=("basic", "mixed", "mixed_split"))
     return {"steps": steps, "clusters": out}
+
+
+def whfast_plain_summary(steps=200):
+    """The plain one-simulation-per-call WHFast path (what the REBOUND plugin
+    drives): a 5-body system of the configuration-4 generator, `steps` steps of
+    P_inner / 20, one C-ABI call (one program launch) per step."""
+    import rebound_gb300 as R
+    L = R.load()
+    systems, periods = R.ics.planetary_systems(64, seed=3)
+    k = next(q for q, s in enumerate(systems) if len(s) == 5)
+    sim = R.Simulation()
+    sim.dt, sim.integrator = float(periods[k]) / 20.0, "whfast"
+    sim.add(systems[k])
+    h = sim.handle
+    for _ in range(3):
+        R._lib.check(L.rgpu_steps(h, 1), h)
+    ms = ctypes.c_double(0.)
+    R._lib.check(L.rgpu_sim_time_steps(h, steps, ctypes.byref(ms)), h)
+    return {"bodies": 5, "steps": steps, "us_per_step": 1e3 * ms.value / steps}
+
+
+def tree_patch_summary(box=800.0):
+    """One tree-gravity evaluation and one tree collision search of a ring patch
+    (configuration-3 physics, `box` metres square): the small case of the tree
+    kernels' ncu summaries."""
+    import rebound_gb300 as R
+    L = R.load()
+    p = R.ics.ring_patch(box, seed=11)
+    n_root = int(box / 20.0)
+    sim = R.Simulation()
+    sim.G, sim.OMEGA, sim.softening = 6.674e-11, 1.3143527e-4, 0.1
+    sim.configure_box(20.0, n_root, n_root, 1)
+    sim.configure_ghostboxes(2, 2, 0)
+    sim.boundary, sim.gravity, sim.collision = "shear", "tree", "tree"
+    sim.add(p)
+    t0 = time.perf_counter()
+    sim.update_acceleration()
+    grav = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    pairs = sim.collision_search()
+    return {"N": len(p), "roots": n_root * n_root, "tree_gravity_s": grav,
+            "collision_search_s": time.perf_counter() - t0, "pairs": int(len(pairs))}
 
 
 def ensemble_only(args):
@@ -673,8 +745,10 @@ def main():
     ap.add_argument("--no-precision", dest="precision", action="store_false",
                     help="skip configuration 1 and the energy drift of every form (configurations 1, 2, 5)")
     ap.add_argument("--quick", action="store_true")
-    ap.add_argument("--only", choices=["tree", "ensemble", "serve"], default=None,
-                    help="run one secondary workload alone and print its summary")
+    ap.add_argument("--only", choices=["tree", "ensemble", "ensemble_full", "serve", "whfast_plain", "tree_patch"],
+                    default=None, help="run one secondary workload alone and print its summary (also the small "
+                                       "workloads the committed ncu summaries were captured on)")
+    ap.add_argument("--patch", type=float, default=800.0, help="ring-patch box size (m) for --only tree_patch")
     ap.add_argument("--ens-systems", type=int, default=8192)
     ap.add_argument("--ens-steps", type=int, default=20)
     ap.add_argument("--ens-block", type=int, default=128)
@@ -693,6 +767,13 @@ def main():
             print(json.dumps({"tree": tree_summary(quick=args.quick)}), flush=True)
         elif args.only == "ensemble":
             print(json.dumps({"ensemble": ensemble_only(args)}), flush=True)
+        elif args.only == "ensemble_full":
+            from rebound_gb300 import ensemble as E
+            print(json.dumps({"ensemble": E.bench_summary(quick=args.quick)}), flush=True)
+        elif args.only == "whfast_plain":
+            print(json.dumps({"whfast_plain": whfast_plain_summary(args.steps)}), flush=True)
+        elif args.only == "tree_patch":
+            print(json.dumps({"tree_patch": tree_patch_summary(args.patch)}), flush=True)
         else:
             from rebound_gb300 import serve as S
             print(json.dumps({"serving": S.bench_summary(quick=args.quick)}), flush=True)

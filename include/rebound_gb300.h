@@ -255,6 +255,11 @@ int rgpu_probe_rate(int which, double* ops_per_s);
  * for bit with the hardware a / b and sqrt(x); *mismatches counts differences.
  * No reference counterpart. */
 int rgpu_selftest_exactfp(long long n, unsigned long long seed, long long* mismatches);
+/* Self-check of the FMA-flavoured ensemble's FP64 division and square root
+ * (hardware approximations refined by Newton steps) against the IEEE operations
+ * on n pseudo-random operand sets: the largest differences in ulps.
+ * No reference counterpart. */
+int rgpu_selftest_fastmath(long long n, unsigned long long seed, double* worst_div_ulps, double* worst_sqrt_ulps);
 
 /* Kepler drift of n independent bodies with gravitational parameters mu[i]
  * over dt[i] (universal variables, Stumpff series, Newton / quartic solver
@@ -316,8 +321,8 @@ int  rgpu_ensemble_get_launch(const rgpu_ensemble* ens, int* mapping, int* block
 int  rgpu_ensemble_steps(rgpu_ensemble* ens, int64_t n);
 int  rgpu_ensemble_time_steps(rgpu_ensemble* ens, int64_t n, double* ms);
 /* Autotuner on the live ensemble (its probe steps advance the state): times
- * every mapping x CTA size over probe_steps, then max_steps_per_launch / 16, / 4
- * and itself as steps per launch, and keeps the fastest combination (read it
+ * every mapping x CTA size over probe_steps, then max_steps_per_launch / 256, / 64,
+ * / 16, / 4 and itself as steps per launch, and keeps the fastest combination (read it
  * back with rgpu_ensemble_get_launch). */
 int  rgpu_ensemble_autotune(rgpu_ensemble* ens, int64_t probe_steps, int64_t max_steps_per_launch,
                             int* best_block, double* best_ms_per_step);

@@ -112,6 +112,8 @@ SIGNATURES = {
     "rgpu_sim_guard_stats": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
     "rgpu_probe_rate": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "rgpu_selftest_exactfp": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_longlong)]),
+    "rgpu_selftest_fastmath": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_double),
+                                              ctypes.POINTER(ctypes.c_double)]),
     "rgpu_direct_accel_noalloc": (ctypes.c_int, [_P] * 7 + [ctypes.c_int64, ctypes.c_double, ctypes.c_double,
                                                             ctypes.c_int, _P]),
     "rgpu_kepler_solve": (ctypes.c_int, [_P, ctypes.c_size_t, _P, _P, _P, ctypes.c_size_t]),

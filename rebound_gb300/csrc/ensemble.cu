@@ -18,6 +18,7 @@
 // system) and a set of steps-per-launch values on the live ensemble and keeps
 // the fastest combination.
 #define ENSEMBLE_NS ens_fast
+#define WH_FAST_MATH 1          // approximate-then-refined FP64 division and sqrt (whfast_core.cuh)
 #include "ensemble_kernels.cuh"
 #include "whfast_warp.cuh"
 #include <algorithm>
@@ -88,7 +89,53 @@ __global__ void __launch_bounds__(128) persistent_warp_kernel(const WarpSys* __r
     }
 }
 
+// Self-check of the fast flavour's division and square root (wh::fast_div,
+// wh::fast_sqrt) against the IEEE operations: the largest difference in ulps of
+// the IEEE result over n operand sets from a counter-based generator.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ double ulps(double got, double ref) {
+    if (got == ref) return 0.;
+    const double u = fabs(ref) * 0x1p-52;     // one ulp of a normal result, within a factor 2
+    return fabs(got - ref) / (u > 0. ? u : 1e-300);
+}
+__global__ void fastmath_check(long long n, unsigned long long seed, unsigned long long* worst_div,
+                               unsigned long long* worst_sqrt) {
+    double wd = 0., ws = 0.;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long r1 = mix64(seed + 2 * (unsigned long long)k), r2 = mix64(seed + 2 * (unsigned long long)k + 1);
+        // mantissas uniform, exponents in [-60, 60], signs mixed
+        const double a = ldexp(1.0 + (double)(r1 >> 12) * 0x1p-52, (int)(r1 & 127) - 64) * ((r2 & 1) ? -1. : 1.);
+        const double b = ldexp(1.0 + (double)(r2 >> 12) * 0x1p-52, (int)((r2 >> 1) & 127) - 64);
+        wd = fmax(wd, ulps(wh::fast_div(a, b), a / b));
+        wd = fmax(wd, ulps(wh::fast_rcp(b), 1. / b));
+        ws = fmax(ws, ulps(wh::fast_sqrt(b), sqrt(b)));
+    }
+    atomicMax(worst_div, (unsigned long long)__double_as_longlong(wd));
+    atomicMax(worst_sqrt, (unsigned long long)__double_as_longlong(ws));
+}
+
 }  // namespace
+
+extern "C" int rgpu_selftest_fastmath(long long n, unsigned long long seed, double* worst_div_ulps,
+                                      double* worst_sqrt_ulps) {
+    if (n < 1 || !worst_div_ulps || !worst_sqrt_ulps) return RGPU_ERR_ARG;
+    unsigned long long* d = nullptr;
+    if (cudaMalloc(&d, 2 * sizeof(unsigned long long)) != cudaSuccess) { cudaGetLastError(); return RGPU_ERR_CUDA; }
+    cudaMemset(d, 0, 2 * sizeof(unsigned long long));
+    fastmath_check<<<152 * 8, 256>>>(n, seed, d, d + 1);
+    g_launches++;
+    unsigned long long h[2] = {0, 0};
+    const cudaError_t e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) { cudaGetLastError(); return RGPU_ERR_CUDA; }
+    *worst_div_ulps = __builtin_bit_cast(double, h[0]);
+    *worst_sqrt_ulps = __builtin_bit_cast(double, h[1]);
+    return RGPU_OK;
+}
 
 struct rgpu_ensemble {
     std::vector<EnsBucket> b;
@@ -375,9 +422,11 @@ int rgpu_ensemble_time_steps(rgpu_ensemble* e, int64_t n, double* ms) {
 // 1. mapping and CTA size: thread per system at 32 / 64 / 128 threads per CTA,
 //    and warp per system (FMA flavour only), each timed over `probe_steps` steps
 //    after one untimed run (graph build);
-// 2. steps per launch for the winner: `max_steps_per_launch` / 16, / 4 and itself
-//    (at least 1), each timed over max_steps_per_launch steps; the fastest wins,
-//    the smaller value on a tie within 2 % (it bounds time-to-first-result).
+// 2. steps per launch for the winner: `max_steps_per_launch` / 256, / 64, / 16, / 4
+//    and itself (at least 1), each timed over max_steps_per_launch steps; the fastest
+//    wins, the smaller value on a tie within 2 %.  Shorter chunks rebalance the
+//    persistent queue more often: a warp slowed by one hard system (many Kepler
+//    iterations near a close encounter) holds up the end of each launch.
 int rgpu_ensemble_autotune(rgpu_ensemble* e, int64_t probe_steps, int64_t max_steps_per_launch,
                            int* best_block, double* best_ms_per_step) {
     if (!e || probe_steps < 1 || max_steps_per_launch < 1) return RGPU_ERR_ARG;
@@ -397,11 +446,13 @@ int rgpu_ensemble_autotune(rgpu_ensemble* e, int64_t probe_steps, int64_t max_st
     }
     e->mapping = bc.mapping;
     e->block = bc.block;
-    const int64_t spls[3] = {std::max<int64_t>(1, max_steps_per_launch / 16),
+    const int64_t spls[5] = {std::max<int64_t>(1, max_steps_per_launch / 256),
+                             std::max<int64_t>(1, max_steps_per_launch / 64),
+                             std::max<int64_t>(1, max_steps_per_launch / 16),
                              std::max<int64_t>(1, max_steps_per_launch / 4), max_steps_per_launch};
     double best_spl_ms = 1e300;
     int64_t bspl = max_steps_per_launch;
-    for (int k = 0; k < 3; k++) {
+    for (int k = 0; k < 5; k++) {
         if (k > 0 && spls[k] == spls[k - 1]) continue;
         e->steps_per_launch = spls[k];
         double ms = 0.;

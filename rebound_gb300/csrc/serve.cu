@@ -6,14 +6,17 @@
 //
 // Two request kinds (the reference runs each as one reb_simulation):
 //  * WHFast planetary systems (src/integrator_whfast.c, Jacobi, safe_mode 1):
-//    slots in per-body-count buckets, thread per slot, each tick advances every
-//    live slot by min(chunk, remaining) steps;
+//    slots in per-body-count buckets, warp per slot (thread per slot on
+//    request), each tick advances every live slot by min(chunk, remaining)
+//    steps; FMA contraction and the fast flavour's division and square root
+//    (WH_FAST_MATH), as in the batched ensemble;
 //  * Plummer clusters with leapfrog (src/integrator_leapfrog.c) and the
 //    mixed-precision direct sum (FP64 displacement formed from two-float
 //    splits, FP32 force, compensated FP32 accumulation): particles in a pooled
 //    SoA, one CTA per (cluster, 256-particle tile), each thread summing its
 //    cluster's j-range in a fixed order.
 // Per-request results do not depend on which other requests share a tick.
+#define WH_FAST_MATH 1          // approximate-then-refined FP64 division and sqrt (whfast_core.cuh)
 #include "whfast_warp.cuh"
 #include <algorithm>
 #include <chrono>
@@ -192,36 +195,69 @@ __global__ void cl_split(Pool p, const ClusterItem* __restrict__ items, int k) {
 
 // Mixed-precision direct sum of one cluster tile: the FP64 displacement from the
 // two-float split (exact when it cancels), FP32 force, Kahan FP32 accumulation.
+// Mixed-precision force of one cluster tile (the MIXED_SPLIT form of the direct
+// sum): two-float displacements and FP32 G m / r^3 on the packed FP32x2 pipe, two
+// j-bodies per instruction, FP32 sums over 32 j-pairs folded into a compensated
+// FP32 pair per particle.  The tile is repacked in shared memory so one 64-bit
+// register holds the same field of two bodies.
+struct __align__(16) ClPair {
+    float4 a, b, c, d;     // (xh0, xh1, yh0, yh1), (zh0, zh1, m0, m1), (xl0, xl1, yl0, yl1), (zl0, zl1, -, -)
+};
+
 __global__ void __launch_bounds__(kT) cl_force(Pool p, const ClusterItem* __restrict__ items, int k) {
-    __shared__ float4 tile[2 * kT];
+    __shared__ ClPair tile[kT / 2];
     const ClusterItem it = items[blockIdx.y];
     if (k >= it.steps_now || blockIdx.x * kT >= it.n) return;
     const int i = blockIdx.x * kT + threadIdx.x;
     const bool live = i < it.n;
     float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi;
     if (live) { hi = p.split[2 * (it.off + i)]; lo = p.split[2 * (it.off + i) + 1]; }
-    const float eps2 = (float)it.eps2;
+    const float2 nxh = make_float2(-hi.x, -hi.x), nyh = make_float2(-hi.y, -hi.y), nzh = make_float2(-hi.z, -hi.z);
+    const float2 nxl = make_float2(-lo.x, -lo.x), nyl = make_float2(-lo.y, -lo.y), nzl = make_float2(-lo.z, -lo.z);
+    const float e = (float)it.eps2;
+    const float2 e2 = make_float2(e, e);
     float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
     for (int jt = 0; jt < it.n; jt += kT) {
         __syncthreads();
-        const int jl = jt + threadIdx.x;
-        tile[2 * threadIdx.x] = jl < it.n ? p.split[2 * (it.off + jl)] : make_float4(0.f, 0.f, 0.f, 0.f);
-        tile[2 * threadIdx.x + 1] = jl < it.n ? p.split[2 * (it.off + jl) + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
+        {
+            const int jl = jt + threadIdx.x;
+            float4 h = make_float4(0.f, 0.f, 0.f, 0.f), l = h;   // missing partner: massless, far from i below
+            if (jl < it.n) { h = p.split[2 * (it.off + jl)]; l = p.split[2 * (it.off + jl) + 1]; }
+            float* t = reinterpret_cast<float*>(&tile[threadIdx.x >> 1]);
+            const int q = threadIdx.x & 1;
+            t[0 + q] = h.x; t[2 + q] = h.y; t[4 + q] = h.z; t[6 + q] = h.w;
+            t[8 + q] = l.x; t[10 + q] = l.y; t[12 + q] = l.z;
+        }
         __syncthreads();
-        const int nt = min(kT, it.n - jt);
-        for (int q = 0; q < nt; q++) {
-            const float4 h = tile[2 * q], l = tile[2 * q + 1];
-            const float dx = (h.x - hi.x) + (l.x - lo.x);
-            const float dy = (h.y - hi.y) + (l.y - lo.y);
-            const float dz = (h.z - hi.z) + (l.z - lo.z);
-            const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-            const float ri = rsqrtf(r2);
-            float s = h.w * ri * ri * ri;
-            s = (jt + q == i) ? 0.f : s;
+        const int nj = min(kT, it.n - jt);
+        const int nq = (nj + 1) >> 1;
+        for (int qs = 0; qs < nq; qs += 32) {
+            const int qe = min(nq, qs + 32);
+            float2 ax = make_float2(0.f, 0.f), ay = ax, az = ax;
+#pragma unroll 4
+            for (int q = qs; q < qe; q++) {
+                const ClPair J = tile[q];
+                const float2 dx = __fadd2_rn(__fadd2_rn(make_float2(J.a.x, J.a.y), nxh),
+                                             __fadd2_rn(make_float2(J.c.x, J.c.y), nxl));
+                const float2 dy = __fadd2_rn(__fadd2_rn(make_float2(J.a.z, J.a.w), nyh),
+                                             __fadd2_rn(make_float2(J.c.z, J.c.w), nyl));
+                const float2 dz = __fadd2_rn(__fadd2_rn(make_float2(J.b.x, J.b.y), nzh),
+                                             __fadd2_rn(make_float2(J.d.x, J.d.y), nzl));
+                const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
+                const float2 ri = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+                float2 sv = __fmul2_rn(__fmul2_rn(ri, ri), __fmul2_rn(make_float2(J.b.z, J.b.w), ri));
+                const int j = jt + 2 * q;
+                sv.x = (j == i) ? 0.f : sv.x;                           // self pair (and eps = 0)
+                sv.y = (j + 1 == i || j + 1 >= jt + nj) ? 0.f : sv.y;   // and the missing partner
+                ax = __ffma2_rn(sv, dx, ax);
+                ay = __ffma2_rn(sv, dy, ay);
+                az = __ffma2_rn(sv, dz, az);
+            }
+            const float tx = ax.x + ax.y, ty = ay.x + ay.y, tz = az.x + az.y;
             float t, y;
-            y = fmaf(s, dx, -cx); t = sx + y; cx = (t - sx) - y; sx = t;
-            y = fmaf(s, dy, -cy); t = sy + y; cy = (t - sy) - y; sy = t;
-            y = fmaf(s, dz, -cz); t = sz + y; cz = (t - sz) - y; sz = t;
+            y = tx - cx; t = sx + y; cx = (t - sx) - y; sx = t;
+            y = ty - cy; t = sy + y; cy = (t - sy) - y; sy = t;
+            y = tz - cz; t = sz + y; cz = (t - sz) - y; sz = t;
         }
     }
     if (!live) return;

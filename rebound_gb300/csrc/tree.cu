@@ -345,11 +345,16 @@ constexpr int kStack = 192;
 
 // QUAD: the far-cell term of a QUADRUPOLE build (src/tree.c:293-306).
 template <bool QUAD>
-__global__ void __launch_bounds__(128) walk_exact(ParticlesSoA p, int N, CellArrays c, int n_root,
-                                                  const GhostArr* __restrict__ gh, double G, double eps2,
+// Threads take particles in key order (`order`, the sorted index array of the
+// build), so a warp's 32 particles are neighbours in space: they see the same
+// roots far or near and descend the same cells, which keeps the warp converged.
+// Each particle's own sum keeps the reference's order, so results do not change.
+__global__ void __launch_bounds__(128) walk_exact(ParticlesSoA p, int N, const int* __restrict__ order, CellArrays c,
+                                                  int n_root, const GhostArr* __restrict__ gh, double G, double eps2,
                                                   double oa2, uint32_t* status) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N) return;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    const int i = order[k];
     int stack[kStack];
     double ax = 0., ay = 0., az = 0.;
     const double px = p.x[i], py = p.y[i], pz = p.z[i];
@@ -435,11 +440,12 @@ __device__ __forceinline__ void virtual_root(const BoxGeom& g, double sx, double
     iz = (int)floor((sz + g.bz / 2.) / g.root_size);
 }
 
-__global__ void __launch_bounds__(128) walk_near(ParticlesSoA p, int N, CellArrays c, BoxGeom geo,
-                                                 const GhostArr* __restrict__ gh, double G, double eps2, double oa2,
-                                                 int K, uint32_t* status) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N) return;
+__global__ void __launch_bounds__(128) walk_near(ParticlesSoA p, int N, const int* __restrict__ order, CellArrays c,
+                                                 BoxGeom geo, const GhostArr* __restrict__ gh, double G, double eps2,
+                                                 double oa2, int K, uint32_t* status) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;      // particles in key order, as walk_exact
+    if (k >= N) return;
+    const int i = order[k];
     int stack[kStack];
     double ax = 0., ay = 0., az = 0.;
     const double px = p.x[i], py = p.y[i], pz = p.z[i];
@@ -909,11 +915,11 @@ int tree_accel(rgpu_sim* s) {
     if (cf.gravity != RGPU_GRAVITY_TREE_SPLIT) {
         ktimer_begin(s);
         if (cf.tree_quadrupole)
-            walk_exact<true><<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, arrays(t), t->n_root, g_ghosts, cf.G,
-                                                                      eps2, cf.opening_angle2, s->d_status);
+            walk_exact<true><<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, t->idx, arrays(t), t->n_root, g_ghosts,
+                                                                      cf.G, eps2, cf.opening_angle2, s->d_status);
         else
-            walk_exact<false><<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, arrays(t), t->n_root, g_ghosts, cf.G,
-                                                                       eps2, cf.opening_angle2, s->d_status);
+            walk_exact<false><<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, t->idx, arrays(t), t->n_root, g_ghosts,
+                                                                       cf.G, eps2, cf.opening_angle2, s->d_status);
         ktimer_end(s);
         g_launches++;
         RGPU_CUDA(s, cudaGetLastError());
@@ -936,7 +942,7 @@ int tree_accel(rgpu_sim* s) {
     }
     RootSweep* sw = (RootSweep*)t->sweep;
     build_root_sweep<<<grid_for(n_root, kB), kB, 0, s->stream>>>(arrays(t), n_root, geo, cf.G, sw);
-    walk_near<<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, arrays(t), geo, g_ghosts, cf.G, eps2,
+    walk_near<<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, t->idx, arrays(t), geo, g_ghosts, cf.G, eps2,
                                                         cf.opening_angle2, K, s->d_status);
     ktimer_begin(s);
     sweep_far<<<grid_for(N, kSweepTile), kSweepTile, 0, s->stream>>>(s->p, N, sw, n_root, geo, g_ghosts, eps2, K);

@@ -21,6 +21,45 @@ namespace wh {
 
 constexpr int kMaxBodies = 16;
 
+// Division and square root.  By default the IEEE operations, as the reference
+// computes them.  A unit that defines WH_FAST_MATH before including this header
+// (the FMA-contracted ensemble, which already trades bit-identity for speed)
+// gets them from the hardware's approximate reciprocal and reciprocal square
+// root refined by Newton steps in FP64 (within an ulp or two of IEEE, checked by
+// rgpu_selftest_fastmath): fewer instructions on GB300's narrow FP64 pipe.
+#ifdef WH_FAST_MATH
+__device__ __forceinline__ double fast_rcp(double b) {
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(b));
+    double e = fma(-b, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-b, y, 1.0);
+    return fma(y, e, y);
+}
+__device__ __forceinline__ double fast_div(double a, double b) {
+    const double y = fast_rcp(b);
+    const double q = a * y;
+    return fma(fma(-b, q, a), y, q);
+}
+__device__ __forceinline__ double fast_sqrt(double x) {
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    y = y * fma(-0.5 * x * y, y, 1.5);
+    const double s = x * y;
+    const double r = fma(fma(-s, s, x), 0.5 * y, s);
+    // positive finite: r; 0 and +inf give themselves, negative and NaN give NaN (as IEEE)
+    const bool pos = x > 0. && x < __longlong_as_double(0x7ff0000000000000LL);
+    return pos ? r : (x == 0. || x > 0. ? x : __longlong_as_double(0x7ff8000000000000LL));
+}
+#define WH_DIV(a, b) (::wh::fast_div((a), (b)))
+#define WH_RCP(b) (::wh::fast_rcp(b))
+#define WH_SQRT(x) (::wh::fast_sqrt(x))
+#else
+#define WH_DIV(a, b) ((a) / (b))
+#define WH_RCP(b) (1. / (b))
+#define WH_SQRT(x) (sqrt(x))
+#endif
+
 template <int NB>
 struct System {
     double x[NB], y[NB], z[NB], vx[NB], vy[NB], vz[NB], m[NB];
@@ -75,17 +114,17 @@ __device__ __forceinline__ void stiefel_g3(double Gs[4], double beta, double X, 
 __device__ inline void kepler_solver(double& px, double& py, double& pz, double& pvx, double& pvy, double& pvz,
                                      double mu, double dt, uint32_t* status) {
     const double x = px, y = py, z = pz, vx = pvx, vy = pvy, vz = pvz;
-    const double r0 = sqrt(x * x + y * y + z * z);
-    const double r0i = 1. / r0;
+    const double r0 = WH_SQRT(x * x + y * y + z * z);
+    const double r0i = WH_RCP(r0);
     const double v2 = vx * vx + vy * vy + vz * vz;
     const double beta = 2. * mu * r0i - v2;
     const double eta0 = x * vx + y * vy + z * vz;
     const double zeta0 = mu - beta * r0;
     double X, Gs[4], invperiod = 0, X_per_period = __longlong_as_double(0x7ff8000000000000LL);
     if (beta > 0.) {
-        const double sb = sqrt(beta);
-        invperiod = sb * beta / (2. * M_PI * mu);
-        X_per_period = 2. * M_PI / sb;
+        const double sb = WH_SQRT(beta);
+        invperiod = WH_DIV(sb * beta, 2. * M_PI * mu);
+        X_per_period = WH_DIV(2. * M_PI, sb);
         const double dtr0i = dt * r0i;
         X = dtr0i * (1. - dtr0i * eta0 * 0.5 * r0i);
     } else {
@@ -95,26 +134,35 @@ __device__ inline void kepler_solver(double& px, double& py, double& pz, double&
     double oldX = X;
     stiefel_g3(Gs, beta, X, status);
     const double e1 = eta0 * Gs[1] + zeta0 * Gs[2];
-    double ri = 1. / (r0 + e1);
+    double ri = WH_RCP(r0 + e1);
     X = ri * (X * e1 - eta0 * Gs[2] - zeta0 * Gs[3] + dt);
     if (fabs(X - oldX) > 0.01 * X_per_period) {
         // Quartic (Laguerre-type) solver, up to 64 iterations, converged when X repeats.
-        X = beta * dt / mu;
-        double prevX[64];
+        X = WH_DIV(beta * dt, mu);
+        // Converged when X repeats an earlier iterate (a cycle).  The bit-exact
+        // flavours compare with every earlier iterate, as the reference; the
+        // fast flavour keeps the last 8 in a ring (less local memory per thread).
+#ifdef WH_FAST_MATH
+        constexpr int kHist = 8;
+#else
+        constexpr int kHist = 64;
+#endif
+        double prevX[kHist];
         for (int nl = 1; nl < 64; nl++) {
             stiefel_g3(Gs, beta, X, status);
             const double f = r0 * X + eta0 * Gs[2] + zeta0 * Gs[3] - dt;
             const double fp = r0 + eta0 * Gs[1] + zeta0 * Gs[2];
             const double fpp = eta0 * Gs[0] + zeta0 * Gs[1];
-            const double den = fp + sqrt(fabs(16. * fp * fp - 20. * f * fpp));
-            X = (X * den - 5. * f) / den;
-            for (int i = 1; i < nl; i++) {
+            const double den = fp + WH_SQRT(fabs(16. * fp * fp - 20. * f * fpp));
+            X = WH_DIV(X * den - 5. * f, den);
+            const int stored = nl - 1 < kHist ? nl - 1 : kHist;
+            for (int i = 0; i < stored; i++) {
                 if (X == prevX[i]) { nl = 64; converged = 1; break; }
             }
-            if (nl < 64) prevX[nl] = X;
+            if (nl < 64) prevX[(nl - 1) % kHist] = X;
         }
         const double e2 = eta0 * Gs[1] + zeta0 * Gs[2];
-        ri = 1. / (r0 + e2);
+        ri = WH_RCP(r0 + e2);
     } else {
         double oldX2;
         for (int nh = 1; nh < 32; nh++) {
@@ -122,7 +170,7 @@ __device__ inline void kepler_solver(double& px, double& py, double& pz, double&
             oldX = X;
             stiefel_g3(Gs, beta, X, status);
             const double e2 = eta0 * Gs[1] + zeta0 * Gs[2];
-            ri = 1. / (r0 + e2);
+            ri = WH_RCP(r0 + e2);
             X = ri * (X * e2 - eta0 * Gs[2] - zeta0 * Gs[3] + dt);
             if (X == oldX || X == oldX2) { converged = 1; break; }
         }
@@ -151,7 +199,7 @@ __device__ inline void kepler_solver(double& px, double& py, double& pz, double&
             if (++it > 4096) { atomicOr(status, DEV_ERR_KEPLER); break; }
         } while (fabs(Xmax - Xmin) > fabs((Xmax + Xmin) * 1e-15));
         const double e2 = eta0 * Gs[1] + zeta0 * Gs[2];
-        ri = 1. / (r0 + e2);
+        ri = WH_RCP(r0 + e2);
     }
     if (isnan(ri)) { ri = 0.; Gs[1] = 0.; Gs[2] = 0.; Gs[3] = 0.; }
     const double f = -mu * Gs[2] * r0i;
@@ -269,8 +317,8 @@ __device__ __forceinline__ void gravity_01(const System<NB>& s, double ax[NB], d
             const double dx = (0. + s.x[i]) - s.x[jj];
             const double dy = (0. + s.y[i]) - s.y[jj];
             const double dz = (0. + s.z[i]) - s.z[jj];
-            const double r = sqrt(dx * dx + dy * dy + dz * dz + eps2);
-            const double pf = G / (r * r * r);
+            const double r = WH_SQRT(dx * dx + dy * dy + dz * dz + eps2);
+            const double pf = WH_DIV(G, r * r * r);
             const double pfj = -pf * s.m[jj];
             const double pfi = pf * s.m[i];
             ax[i] += pfj * dx; ay[i] += pfj * dy; az[i] += pfj * dz;
@@ -287,8 +335,8 @@ __device__ __forceinline__ void gravity_01(const System<NB>& s, double ax[NB], d
             const double dx = (0. + s.x[i]) - s.x[jj];
             const double dy = (0. + s.y[i]) - s.y[jj];
             const double dz = (0. + s.z[i]) - s.z[jj];
-            const double r = sqrt(dx * dx + dy * dy + dz * dz + eps2);
-            const double pf = G / (r * r * r);
+            const double r = WH_SQRT(dx * dx + dy * dy + dz * dz + eps2);
+            const double pf = WH_DIV(G, r * r * r);
             const double pfj = -pf * s.m[jj];
             ax[i] += pfj * dx; ay[i] += pfj * dy; az[i] += pfj * dz;
             if (tp) {
@@ -335,8 +383,8 @@ __device__ __forceinline__ void interaction_step(Jacobi<NB>& j, const System<NB>
         j.vy[i] += dt * jay[i];
         j.vz[i] += dt * jaz[i];
         if (i > 1 && jacobi_term) {   // with gravity = JACOBI the term is in the accelerations
-            const double rj2i = 1. / (qx * qx + qy * qy + qz * qz);
-            const double rji = sqrt(rj2i);
+            const double rj2i = WH_RCP(qx * qx + qy * qy + qz * qz);
+            const double rji = WH_SQRT(rj2i);
             const double rj3iM = rji * rj2i * G * eta;
             const double pf = dt * rj3iM;
             j.vx[i] += pf * qx;

@@ -35,6 +35,12 @@
  * configuration) are reported with reb_simulation_error and set r->status to
  * REB_STATUS_GENERIC_ERROR, so integrate returns with that status.
  *
+ * Speed: the GPU pays off for direct sums and trees of thousands of particles
+ * and more.  The plain WHFast path runs one small system per call on one warp,
+ * about 67 µs per step for 5 bodies against about 2.5 µs for REBOUND's WHFast
+ * on one CPU core; many systems belong in the batched ensemble
+ * (rgpu_ensemble_*) or the request loop (rgpu_server_*).
+ *
  * REBOUND 5.0.0's registry compares a new name against the entry after each
  * registered one (src/rebound.c:100-104), which reads its terminator once one
  * custom integrator exists: register at most one custom integrator per process.

@@ -219,7 +219,7 @@ def plain_rate(reqs, max_whfast=8, steps_cap=400, clusters=2, cluster_steps_cap=
             "cluster_pair_int_per_s": pairs / cl_time if cl_time else None}
 
 
-def bench_summary(quick=False, n_requests=240, rates=(100.0,), t_end_periods=(1e2, 1e5), wall_s=120.0):
+def bench_summary(quick=False, n_requests=240, rates=(100.0,), t_end_periods=(1e2, 1e5), wall_s=90.0):
     """Served stream of the configuration: 80 % WHFast systems with end times
     log-uniform in [1e2, 1e5] inner periods (2e3 to 2e6 steps each), 20 % Plummer
     clusters, Poisson arrivals.  The run is bounded by the request count and by
