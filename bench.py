@@ -407,6 +407,7 @@ def tree_summary(quick=False, steps=2, sm_count=None, sm_mhz=None):
         R._lib.check(L.rgpu_sim_time_steps(h, 1, ctypes.byref(ms)), h)
         times.append(ms.value)
     step_s = sum(times) / len(times) / 1e3
+    R._lib.check(L.rgpu_sim_get_config(h, ctypes.byref(sim._cfg)), h)     # counters advanced by the steps
     rms, rcalls = sim.resolve_time()
     resolve = {"host_ms_per_step": rms / max(1, steps + 1), "share_of_step": rms / max(1, steps + 1) / (1e3 * step_s),
                "collisions_per_step": sim.collisions_log_n / (steps + 1)}
@@ -583,10 +584,10 @@ def whfast_plain_summary(steps=200):
     return {"bodies": 5, "steps": steps, "us_per_step": 1e3 * ms.value / steps}
 
 
-def tree_patch_summary(box=800.0):
+def tree_patch_summary(box=800.0, gravity="tree"):
     """One tree-gravity evaluation and one tree collision search of a ring patch
     (configuration-3 physics, `box` metres square): the small case of the tree
-    kernels' ncu summaries."""
+    kernels' ncu summaries.  gravity "tree_split" runs the split mode."""
     import rebound_gb300 as R
     L = R.load()
     p = R.ics.ring_patch(box, seed=11)
@@ -595,14 +596,14 @@ def tree_patch_summary(box=800.0):
     sim.G, sim.OMEGA, sim.softening = 6.674e-11, 1.3143527e-4, 0.1
     sim.configure_box(20.0, n_root, n_root, 1)
     sim.configure_ghostboxes(2, 2, 0)
-    sim.boundary, sim.gravity, sim.collision = "shear", "tree", "tree"
+    sim.boundary, sim.gravity, sim.collision = "shear", gravity, "tree"
     sim.add(p)
     t0 = time.perf_counter()
     sim.update_acceleration()
     grav = time.perf_counter() - t0
     t0 = time.perf_counter()
     pairs = sim.collision_search()
-    return {"N": len(p), "roots": n_root * n_root, "tree_gravity_s": grav,
+    return {"N": len(p), "roots": n_root * n_root, "gravity": gravity, "tree_gravity_s": grav,
             "collision_search_s": time.perf_counter() - t0, "pairs": int(len(pairs))}
 
 
@@ -749,6 +750,8 @@ def main():
                     default=None, help="run one secondary workload alone and print its summary (also the small "
                                        "workloads the committed ncu summaries were captured on)")
     ap.add_argument("--patch", type=float, default=800.0, help="ring-patch box size (m) for --only tree_patch")
+    ap.add_argument("--tree-gravity", default="tree", choices=["tree", "tree_split"],
+                    help="gravity mode for --only tree_patch")
     ap.add_argument("--ens-systems", type=int, default=8192)
     ap.add_argument("--ens-steps", type=int, default=20)
     ap.add_argument("--ens-block", type=int, default=128)
@@ -773,7 +776,7 @@ def main():
         elif args.only == "whfast_plain":
             print(json.dumps({"whfast_plain": whfast_plain_summary(args.steps)}), flush=True)
         elif args.only == "tree_patch":
-            print(json.dumps({"tree_patch": tree_patch_summary(args.patch)}), flush=True)
+            print(json.dumps({"tree_patch": tree_patch_summary(args.patch, args.tree_gravity)}), flush=True)
         else:
             from rebound_gb300 import serve as S
             print(json.dumps({"serving": S.bench_summary(quick=args.quick)}), flush=True)

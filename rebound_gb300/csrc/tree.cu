@@ -33,6 +33,7 @@ struct TreeBuffers {
     // cells (structure of arrays)
     size_t ccap = 0;
     double *cx = nullptr, *cy = nullptr, *cz = nullptr, *cw = nullptr;
+    double* cw2 = nullptr;          // w * w, rounded as the walk's opening test computes it
     double *cm = nullptr, *cmx = nullptr, *cmy = nullptr, *cmz = nullptr;
     double *cqxx = nullptr, *cqxy = nullptr, *cqxz = nullptr, *cqyy = nullptr, *cqyz = nullptr;  // quadrupole
     int* cstart = nullptr;          // range in sorted order
@@ -199,6 +200,7 @@ __global__ void radix_scatter(const unsigned long long* __restrict__ keys, const
 // --- 3. cells ------------------------------------------------------------------
 struct CellArrays {
     double *x, *y, *z, *w, *m, *mx, *my, *mz;
+    double* w2;                               // w * w (the opening test's left side, same rounding)
     double *qxx, *qxy, *qxz, *qyy, *qyz;     // mass quadrupole (q_zz = -q_xx - q_yy)
     int *start, *end, *first, *nchild, *pt, *depth;
     unsigned long long* path;
@@ -212,6 +214,7 @@ __global__ void init_roots(CellArrays c, int n_root, BoxGeom g) {
     c.y[r] = -g.by / 2. + g.root_size * (0.5 + (double)rj);
     c.z[r] = -g.bz / 2. + g.root_size * (0.5 + (double)rk);
     c.w[r] = g.root_size;
+    c.w2[r] = g.root_size * g.root_size;
     c.start[r] = 0; c.end[r] = 0;
     c.first[r] = -1; c.nchild[r] = 0;
     c.pt[r] = INT_MIN;
@@ -284,6 +287,7 @@ __global__ void split_level(const unsigned long long* __restrict__ keys, const i
         if (ce <= cs) continue;
         const double wc = w / 2.;
         c.w[q] = wc;
+        c.w2[q] = wc * wc;
         c.x[q] = c.x[cell] + wc / 2. * ((o & 1) == 0 ? 1. : -1);
         c.y[q] = c.y[cell] + wc / 2. * ((o & 2) == 0 ? 1. : -1);
         c.z[q] = c.z[cell] + wc / 2. * ((o & 4) == 0 ? 1. : -1);
@@ -370,8 +374,7 @@ __global__ void __launch_bounds__(128) walk_exact(ParticlesSoA p, int N, const i
                 const double r2 = dx * dx + dy * dy + dz * dz;
                 const int pt = c.pt[q];
                 if (pt < 0) {
-                    const double w = c.w[q];
-                    if (w * w > oa2 * r2) {
+                    if (c.w2[q] > oa2 * r2) {
                         const int f = c.first[q], n = c.nchild[q];
                         if (sp + n > kStack) { atomicOr(status, DEV_ERR_STACK); sp = 0; break; }
                         for (int k = n - 1; k >= 0; k--) stack[sp++] = f + k;
@@ -469,8 +472,7 @@ __global__ void __launch_bounds__(128) walk_near(ParticlesSoA p, int N, const in
                 const double r2 = dx * dx + dy * dy + dz * dz;
                 const int pt = c.pt[q];
                 if (pt < 0) {
-                    const double w = c.w[q];
-                    if (w * w > oa2 * r2) {
+                    if (c.w2[q] > oa2 * r2) {
                         const int f = c.first[q], n = c.nchild[q];
                         if (sp + n > kStack) { atomicOr(status, DEV_ERR_STACK); sp = 0; break; }
                         for (int k = n - 1; k >= 0; k--) stack[sp++] = f + k;
@@ -655,24 +657,31 @@ __global__ void max_speed2(ParticlesSoA p, int N, unsigned long long* out) {
 }
 
 template <bool LINE>
-__global__ void __launch_bounds__(128) tree_pairs_count(ParticlesSoA p, int N, CellArrays c, BoxGeom g,
+// Both pair kernels take particles in key order (`order`), like the walks; counts
+// and output offsets stay indexed by particle, so the list keeps the reference's
+// particle-major discovery order.
+__global__ void __launch_bounds__(128) tree_pairs_count(ParticlesSoA p, int N, const int* __restrict__ order,
+                                                        CellArrays c, BoxGeom g,
                                                         const GhostArr* __restrict__ gh, int nring, const double* r2nd,
                                                         double dtl, const unsigned long long* vmax2, int* count,
                                                         uint32_t* status) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N) return;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    const int i = order[k];
     int stack[kStack];
     count[i] = tree_pairs_one<LINE>(i, p, c, g, gh, nring, r2nd[0], r2nd[1], dtl,
                                     LINE ? __longlong_as_double((long long)*vmax2) : 0., nullptr, 0, stack, status);
 }
 
 template <bool LINE>
-__global__ void __launch_bounds__(128) tree_pairs_write(ParticlesSoA p, int N, CellArrays c, BoxGeom g,
+__global__ void __launch_bounds__(128) tree_pairs_write(ParticlesSoA p, int N, const int* __restrict__ order,
+                                                        CellArrays c, BoxGeom g,
                                                         const GhostArr* __restrict__ gh, int nring, const double* r2nd,
                                                         double dtl, const unsigned long long* vmax2,
                                                         const long long* off, rgpu_collision* out, uint32_t* status) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N) return;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    const int i = order[k];
     int stack[kStack];
     tree_pairs_one<LINE>(i, p, c, g, gh, nring, r2nd[0], r2nd[1], dtl,
                          LINE ? __longlong_as_double((long long)*vmax2) : 0., out, off[i], stack, status);
@@ -736,19 +745,19 @@ __global__ void exclusive_scan_counts(const int* __restrict__ cnt, int N, long l
 
 // --- host side -------------------------------------------------------------------------
 CellArrays arrays(TreeBuffers* t) {
-    return CellArrays{t->cx, t->cy, t->cz, t->cw, t->cm, t->cmx, t->cmy, t->cmz,
+    return CellArrays{t->cx, t->cy, t->cz, t->cw, t->cm, t->cmx, t->cmy, t->cmz, t->cw2,
                       t->cqxx, t->cqxy, t->cqxz, t->cqyy, t->cqyz, t->cstart, t->cend, t->cfirst, t->cnchild, t->cpt, t->cdepth, t->cpath};
 }
 
 void free_cells(TreeBuffers* t) {
-    double* d[] = {t->cx, t->cy, t->cz, t->cw, t->cm, t->cmx, t->cmy, t->cmz,
+    double* d[] = {t->cx, t->cy, t->cz, t->cw, t->cm, t->cmx, t->cmy, t->cmz, t->cw2,
                    t->cqxx, t->cqxy, t->cqxz, t->cqyy, t->cqyz};
     for (double* q : d) cudaFree(q);
     t->cqxx = t->cqxy = t->cqxz = t->cqyy = t->cqyz = nullptr;
     int* n[] = {t->cstart, t->cend, t->cfirst, t->cnchild, t->cpt, t->cdepth};
     for (int* q : n) cudaFree(q);
     cudaFree(t->cpath);
-    t->cx = t->cy = t->cz = t->cw = t->cm = t->cmx = t->cmy = t->cmz = nullptr;
+    t->cx = t->cy = t->cz = t->cw = t->cm = t->cmx = t->cmy = t->cmz = t->cw2 = nullptr;
     t->cstart = t->cend = t->cfirst = t->cnchild = t->cpt = t->cdepth = nullptr;
     t->cpath = nullptr;
     t->ccap = 0;
@@ -756,7 +765,7 @@ void free_cells(TreeBuffers* t) {
 
 int alloc_cells(rgpu_sim* s, TreeBuffers* t, size_t ccap) {
     free_cells(t);
-    double** d[] = {&t->cx, &t->cy, &t->cz, &t->cw, &t->cm, &t->cmx, &t->cmy, &t->cmz,
+    double** d[] = {&t->cx, &t->cy, &t->cz, &t->cw, &t->cm, &t->cmx, &t->cmy, &t->cmz, &t->cw2,
                     &t->cqxx, &t->cqxy, &t->cqxz, &t->cqyy, &t->cqyz};
     for (double** q : d) RGPU_CUDA(s, cudaMalloc(q, sizeof(double) * ccap));
     int** n[] = {&t->cstart, &t->cend, &t->cfirst, &t->cnchild, &t->cpt, &t->cdepth};
@@ -979,10 +988,10 @@ int tree_collisions(rgpu_sim* s, rgpu_collision* out, size_t cap, size_t* n_foun
     }
     const double dtl = s->dt_last_done;
     if (line)
-        tree_pairs_count<true><<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, c, g, g_ghosts, nring, t->r_top,
+        tree_pairs_count<true><<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, t->idx, c, g, g_ghosts, nring, t->r_top,
                                                                         dtl, vmax2, t->pair_count, s->d_status);
     else
-        tree_pairs_count<false><<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, c, g, g_ghosts, nring, t->r_top,
+        tree_pairs_count<false><<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, t->idx, c, g, g_ghosts, nring, t->r_top,
                                                                          dtl, vmax2, t->pair_count, s->d_status);
     exclusive_scan_counts<<<1, kB, 0, s->stream>>>(t->pair_count, N, t->pair_off);
     g_launches += 4;
@@ -1000,11 +1009,11 @@ int tree_collisions(rgpu_sim* s, rgpu_collision* out, size_t cap, size_t* n_foun
     }
     if (total) {
         if (line)
-            tree_pairs_write<true><<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, c, g, g_ghosts, nring, t->r_top,
+            tree_pairs_write<true><<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, t->idx, c, g, g_ghosts, nring, t->r_top,
                                                                             dtl, vmax2, t->pair_off, t->pairs,
                                                                             s->d_status);
         else
-            tree_pairs_write<false><<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, c, g, g_ghosts, nring,
+            tree_pairs_write<false><<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, t->idx, c, g, g_ghosts, nring,
                                                                              t->r_top, dtl, vmax2, t->pair_off,
                                                                              t->pairs, s->d_status);
         g_launches++;

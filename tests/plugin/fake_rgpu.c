@@ -86,6 +86,17 @@ int rgpu_sim_configure(rgpu_sim* s, const rgpu_config* c) {
                                                                           : reb_collision_resolve_halt;
     r->extras = s;
     r->coefficient_of_restitution = s->eps_fn ? eps_trampoline : NULL;
+    if (c->integrator == RGPU_INTEGRATOR_WHFAST) {
+        struct reb_integrator_whfast_state* w = (struct reb_integrator_whfast_state*)r->integrator.state;
+        w->safe_mode = (unsigned)c->whfast_safe_mode;
+        w->corrector = (unsigned)c->whfast_corrector;
+        w->corrector2 = (unsigned)c->whfast_corrector2;
+        w->kernel = c->whfast_kernel;
+        w->coordinates = c->whfast_coordinates;
+        w->keep_unsynchronized = (unsigned)c->whfast_keep_unsynchronized;
+    } else if (c->integrator == RGPU_INTEGRATOR_LEAPFROG) {
+        ((struct reb_integrator_leapfrog_state*)r->integrator.state)->order = c->leapfrog_order ? (unsigned)c->leapfrog_order : 2u;
+    }
     r->root_size = c->root_size;
     r->N_root_x = (size_t)c->N_root_x; r->N_root_y = (size_t)c->N_root_y; r->N_root_z = (size_t)c->N_root_z;
     r->N_ghost_x = c->N_ghost_x; r->N_ghost_y = c->N_ghost_y; r->N_ghost_z = c->N_ghost_z;

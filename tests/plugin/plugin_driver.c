@@ -8,11 +8,17 @@
  * Phases: integrate with a shortened last step, a modified particle, an added
  * particle, a removed particle, plain steps, a periodic boundary held by the
  * plugin, and the boundary handed back when the built-in integrator is
- * selected again.  A failing GPU library ends the run with
+ * selected again.  With the argument "whfast" it runs the outer solar system
+ * through REBOUND's WHFast and the plugin's "gpu_whfast" instead (one custom
+ * integrator per process: see rgpu_rebound.h).  A failing GPU library ends the
+ * run with
  *   ERROR <message REBOUND stored>
  * (the no-GPU path of the real library). */
 #include <math.h>
 #include <stdio.h>
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
 #include <stdlib.h>
 #include <string.h>
 
@@ -53,7 +59,36 @@ static int report(const char* phase, struct reb_simulation* a, struct reb_simula
     return 0;
 }
 
-int main(void) {
+/* WHFast (safe_mode 1, Jacobi) on the outer solar system: built-in against the plugin. */
+static int run_whfast(void) {
+    rgpu_rebound_register(RGPU_INTEGRATOR_WHFAST, "gpu_whfast");
+    struct reb_simulation* a = reb_simulation_create();
+    struct reb_simulation* b = reb_simulation_create();
+    reb_simulation_add_fmt(a, "outer solar system");
+    reb_simulation_add_fmt(b, "outer solar system");
+    a->dt = b->dt = 0.005 * 12. * 2. * M_PI;
+    a->save_messages = b->save_messages = 1;
+    reb_simulation_set_integrator(a, "whfast");
+    struct rgpu_rebound_state* st = reb_simulation_set_integrator(b, "gpu_whfast");
+    if (!st || st->scheme != RGPU_INTEGRATOR_WHFAST || st->safe_mode != 1) {
+        printf("ERROR set_integrator did not return the plugin state\n");
+        return 0;
+    }
+    int sa = reb_simulation_integrate(a, 100.), sb = reb_simulation_integrate(b, 100.);
+    if (report("whfast_integrate", a, b, sa, sb)) return 0;
+    a->particles[2].vx *= 1.0001; a->did_modify_particles = 1;
+    b->particles[2].vx *= 1.0001; b->did_modify_particles = 1;
+    sa = reb_simulation_integrate(a, 250.); sb = reb_simulation_integrate(b, 250.);
+    if (report("whfast_modified", a, b, sa, sb)) return 0;
+    printf("ENERGY %.17g %.17g\n", reb_simulation_energy(a), reb_simulation_energy(b));
+    reb_simulation_free(a);
+    reb_simulation_free(b);
+    printf("DONE\n");
+    return 0;
+}
+
+int main(int argc, char** argv) {
+    if (argc > 1 && strcmp(argv[1], "whfast") == 0) return run_whfast();
     rgpu_rebound_register(RGPU_INTEGRATOR_LEAPFROG, "gpu_leapfrog");
     struct reb_simulation* a = make(64);
     struct reb_simulation* b = make(64);

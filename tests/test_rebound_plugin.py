@@ -6,10 +6,12 @@ sources named by the REBOUND_REFERENCE environment variable or recorded in
 oracle/_ref/reference_path by the build step; without them these tests skip.
 
 * With a test double of the C ABI (tests/plugin/fake_rgpu.c) whose "device" is a
-  private REBOUND simulation running REBOUND's built-in leapfrog, the plugin must
-  reproduce the built-in integrator bit for bit through REBOUND's own integrate
-  and steps loops: shortened last step, modified / added / removed particles,
-  and a periodic boundary the plugin holds for the device and hands back.
+  private REBOUND simulation running REBOUND's built-in integrators, the plugin
+  must reproduce the built-in integrator bit for bit through REBOUND's own
+  integrate and steps loops: leapfrog with a shortened last step, modified /
+  added / removed particles and a periodic boundary the plugin holds for the
+  device and hands back; WHFast on the outer solar system (its synchronize on
+  exit and before the shortened last step).
 * Linked with the real librebound_gb300: on a machine without a GPU,
   reb_simulation_integrate must end with REB_STATUS_GENERIC_ERROR and the
   library's error in REBOUND's message list (no crash); with a GPU it must track
@@ -58,11 +60,11 @@ def build_driver(tmp_path, backend):
     return exe
 
 
-def run(exe):
+def run(exe, *args):
     env = dict(os.environ)
     cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
     env["LD_LIBRARY_PATH"] = os.path.join(cuda, "lib64") + ":" + env.get("LD_LIBRARY_PATH", "")
-    out = subprocess.run([exe], capture_output=True, text=True, timeout=300, env=env)
+    out = subprocess.run([exe, *args], capture_output=True, text=True, timeout=300, env=env)
     assert out.returncode == 0, out.stdout + out.stderr
     return out.stdout.splitlines()
 
@@ -90,6 +92,19 @@ def test_plugin_reproduces_builtin_leapfrog_through_rebound_loops(tmp_path):
     # the plugin held the periodic boundary for the device and gave it back
     assert extra["HELD"] == ["0", "2"]
     assert extra["RETURNED"] == ["2"]
+
+
+def test_plugin_reproduces_builtin_whfast(tmp_path):
+    # the WHFast plugin (safe_mode 1, Jacobi) through REBOUND's integrate loop, its
+    # synchronize called on exit and before the shortened last step
+    exe = build_driver(tmp_path, [os.path.join(REPO, "tests", "plugin", "fake_rgpu.c")])
+    status, diff, extra = parse(run(exe, "whfast"))
+    assert "DONE" in extra, (status, diff, extra)
+    for phase in ("whfast_integrate", "whfast_modified"):
+        assert status[phase] == (REB_STATUS_SUCCESS, REB_STATUS_SUCCESS), (phase, status[phase])
+        assert diff[phase] == (0.0, 0.0), (phase, diff[phase])
+    ea, eb = map(float, extra["ENERGY"])
+    assert ea == eb
 
 
 def test_plugin_with_gpu_library(tmp_path):
