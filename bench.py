@@ -453,21 +453,36 @@ def tree_summary(quick=False, steps=2, sm_count=None, sm_mhz=None):
     cpu_rows_s = time.perf_counter() - t0
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     cpu_grav_step_s = cpu_rows_s / rows * len(p)
-    # Roofline of the exact walk: FP64-pipe lane instructions per (particle, ghost
-    # box, root) visit from the committed ncu count (valid while tree.cu and
-    # exactfp.cuh hash to the recorded digest) x the visits of one walk / the
-    # walk's time, against the nominal FP64 pipe rate at the sampled clock.
-    roof = {"bound": "fp64", "kernel": "walk_exact", "unit": "Tinst/s (FP64-pipe lane instructions)"}
+    # Roofline of the exact walk.  The committed ncu counts (valid while tree.cu and
+    # exactfp.cuh hash to the recorded digest) give, per (particle, ghost box, root)
+    # visit, the FP64-pipe lane instructions and the warp instructions issued on all
+    # pipes; times the visits of one walk / the walk's time, against the nominal FP64
+    # pipe rate (0.5 lanes/clock/SMSP) and the issue rate (one warp instruction per
+    # clock per SMSP) at the sampled clock.  The bound is the larger fraction.
+    roof = {"kernel": "walk_exact"}
     try:
         with open(TREE_COUNTS_FILE) as f:
             rec = json.load(f)
         if sources_digest(rec["sources"]) == rec["sha256"]:
             visits = len(p) * 25 * n_root * n_root
-            ach = rec["fp64_lane_inst_per_root_visit"] * visits / grav_s / 1e12
-            peak = nominal_fp64_tflops(sm_count, sm_mhz) / 2 if sm_mhz else None
-            roof.update({"achieved": ach, "peak": peak, "frac": ach / peak if peak else None,
-                         "visits_per_walk": visits, "inst_per_visit": rec["fp64_lane_inst_per_root_visit"],
-                         "peak_source": "nominal FP64 pipe rate (0.5 lanes/clock/SMSP) at the sampled SM clock"})
+            clk = sm_mhz * 1e6 if sm_mhz else None
+            fp64_ach = rec["fp64_lane_inst_per_root_visit"] * visits / grav_s
+            fp64_peak = FP64_LANES_PER_CLK_PER_SMSP * 4 * sm_count * clk if clk and sm_count else None
+            iss_ach = rec["warp_inst_per_root_visit"] * visits / grav_s if "warp_inst_per_root_visit" in rec else None
+            iss_peak = 4 * sm_count * clk if clk and sm_count else None
+            fr64 = fp64_ach / fp64_peak if fp64_peak else None
+            friss = iss_ach / iss_peak if (iss_ach and iss_peak) else None
+            bound = "issue" if (friss or 0) > (fr64 or 0) else "fp64"
+            roof.update({"bound": bound, "frac": friss if bound == "issue" else fr64,
+                         "fp64": {"achieved": fp64_ach / 1e12, "peak": fp64_peak / 1e12 if fp64_peak else None,
+                                  "unit": "T lane-inst/s", "frac": fr64,
+                                  "inst_per_visit": rec["fp64_lane_inst_per_root_visit"]},
+                         "issue": {"achieved": iss_ach / 1e12 if iss_ach else None,
+                                   "peak": iss_peak / 1e12 if iss_peak else None,
+                                   "unit": "T warp-inst/s", "frac": friss,
+                                   "inst_per_visit": rec.get("warp_inst_per_root_visit")},
+                         "visits_per_walk": visits,
+                         "peak_source": "nominal rates at the sampled SM clock"})
         else:
             roof["counts"] = "tree sources changed since the ncu capture (sha256 mismatch)"
     except (OSError, ValueError, KeyError) as ex:

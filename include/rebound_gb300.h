@@ -250,10 +250,11 @@ int64_t rgpu_launch_count(void);
  * the current device: 0 = FP64 FMA, 1 = FP32 FMA, 2 = FP64<->FP32 conversion,
  * 3 = FP32 rsqrt (MUFU), 4 = integer ALU (3-input logic op). */
 int rgpu_probe_rate(int which, double* ops_per_s);
-/* Self-check of the integer-pipe IEEE FP64 division and square root used by the
- * exact tree walk: n pseudo-random operand sets from `seed`, each compared bit
- * for bit with the hardware a / b and sqrt(x); *mismatches counts differences.
- * No reference counterpart. */
+/* Self-check of the integer-pipe IEEE FP64 arithmetic used by the exact tree
+ * walk (division, square root, non-negative addition, multiplication, square):
+ * n pseudo-random operand sets from `seed`, each compared bit for bit with the
+ * hardware operation; *mismatches counts differences.  No reference
+ * counterpart. */
 int rgpu_selftest_exactfp(long long n, unsigned long long seed, long long* mismatches);
 /* Self-check of the FMA-flavoured ensemble's FP64 division and square root
  * (hardware approximations refined by Newton steps) against the IEEE operations

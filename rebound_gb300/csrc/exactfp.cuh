@@ -147,4 +147,126 @@ FIX_HD double sqrt_rn(double x) {
     return fixpair::bits_double(((u64)(be - 1) << 52) + mant);
 }
 
+// ---------------------------------------------------------------------------
+// Squares, products and sums of non-negative numbers.  Each FP64 instruction on
+// GB300 holds the FP64 pipe for 64 clocks per warp (0.5 lanes per clock per SM
+// sub-partition), while the ALU and IMAD pipes issue a warp instruction every
+// clock or two; the same IEEE round-to-nearest-even results built from 30-45
+// 32-bit integer instructions leave the FP64 pipe free for the rest of the
+// work.  (A general signed addition needs about twice as many instructions and
+// stays on the FP64 pipe.)
+//
+// The *_try forms return the exact result when the operands and the result are
+// normal numbers and otherwise set `special` (the value is then meaningless):
+// the caller recomputes such rare cases with hardware FP64 in a branch of its
+// own, so that no FP64 instruction is issued on the common path.
+//
+// Rounding: a significand s with its leading bit at bit 62 keeps bits 62..10;
+// bits 9..0 decide, with every bit shifted out below bit 0 jammed into bit 0
+// (sticky).  Jamming keeps floor(s / 2) and whether anything is left below,
+// which is all a rounding position two or more bits up reads.
+
+// s = sh:sl (leading bit at 62, sticky in bit 0) rounded to 53 bits, ties to
+// even, added to the biased exponent minus one (be1) in the high word: a
+// round-up to 2^53 carries into the exponent.  Returns the double's bits.
+FIX_HD u64 round_assemble(u32 sh, u32 sl, u32 be1) {
+    const u32 add = 0x1FFu + ((sl >> 10) & 1u);
+    const u32 lo = sl + add;
+    const u32 hi = sh + (lo < sl ? 1u : 0u);
+    const u32 mlo = fixpair::shf_r(lo, hi, 10), mhi = hi >> 10;
+    return ((u64)((be1 << 20) + mhi) << 32) | mlo;
+}
+
+// P = p3:p2:p1:p0 in [2^104, 2^106) (a product of two 53-bit significands) to the
+// rounded double; e: the biased exponent of the product if P < 2^105.
+FIX_HD double finish_product(u32 p0, u32 p1, u32 p2, u32 p3, int e, u32 sign, u32& special) {
+    const u32 top = p3 >> 9;                                         // P >= 2^105
+    const int sh = 10 + (int)top;                                    // s = P >> (32 + sh)
+    const u32 sl = fixpair::shf_r(p1, p2, sh), shi = fixpair::shf_r(p2, p3, sh);
+    const u32 sticky = (p0 | (p1 & ((1u << sh) - 1u))) != 0u ? 1u : 0u;
+    e += (int)top;
+    special |= (unsigned)(e - 1) >= 2045u ? 1u : 0u;                 // subnormal or overflowing result
+    return fixpair::bits_double(round_assemble(shi, sl | sticky, (u32)(e - 1)) | ((u64)sign << 32));
+}
+
+// a * a.
+FIX_HD double sqr_try(double a, u32& special) {
+    const u64 A = dbits(a);
+    const u32 ah = (u32)(A >> 32), al = (u32)A;
+    const int ea = (int)((ah >> 20) & 0x7FFu);
+    special |= (unsigned)(ea - 1) >= 2046u ? 1u : 0u;                // zero, subnormal, inf, NaN
+    const u32 h = (ah & 0xFFFFFu) | 0x100000u;                       // significand = h 2^32 + al, h < 2^21
+    // P = h^2 2^64 + 2 h al 2^32 + al^2
+    const u64 ll = fixpair::wide(al, al);
+    const u64 t = fixpair::mad_wide(h << 1, al, ll >> 32);           // < 2^55
+    const u64 u = fixpair::mad_wide(h, h, t >> 32);                  // < 2^43
+    return finish_product((u32)ll, (u32)t, (u32)u, (u32)(u >> 32), 2 * ea - 1023, 0u, special);
+}
+
+// a * b.
+FIX_HD double mul_try(double a, double b, u32& special) {
+    const u64 A = dbits(a), B = dbits(b);
+    const u32 ah = (u32)(A >> 32), al = (u32)A, bh = (u32)(B >> 32), bl = (u32)B;
+    const int ea = (int)((ah >> 20) & 0x7FFu), eb = (int)((bh >> 20) & 0x7FFu);
+    special |= ((unsigned)(ea - 1) >= 2046u || (unsigned)(eb - 1) >= 2046u) ? 1u : 0u;
+    const u32 ha = (ah & 0xFFFFFu) | 0x100000u, hb = (bh & 0xFFFFFu) | 0x100000u;
+    // P = ha hb 2^64 + (ha bl + al hb) 2^32 + al bl
+    const u64 ll = fixpair::wide(al, bl);
+    const u64 t1 = fixpair::mad_wide(ha, bl, ll >> 32);              // < 2^54
+    const u64 t2 = fixpair::mad_wide(al, hb, (u32)t1);               // < 2^54
+    const u64 u = fixpair::mad_wide(ha, hb, t1 >> 32) + (t2 >> 32);  // < 2^43
+    return finish_product((u32)ll, (u32)t2, (u32)u, (u32)(u >> 32), ea + eb - 1023, (ah ^ bh) & 0x80000000u,
+                          special);
+}
+
+// a + b for a, b >= +0 (no cancellation, no sign).
+FIX_HD double add_pos_try(double a, double b, u32& special) {
+    const u64 A = dbits(a), B = dbits(b);
+    const bool sw = B > A;
+    const u64 X = sw ? B : A, Y = sw ? A : B;
+    const u32 xh = (u32)(X >> 32), yh = (u32)(Y >> 32);
+    const int ex = (int)(xh >> 20), ey = (int)(yh >> 20);            // sign bits included: negatives are special
+    special |= (ey == 0 || ex >= 2047) ? 1u : 0u;
+    const u64 mx = ((X & kFrac) | kHidden) << 10;                    // leading bit at 62
+    const u64 my = ((Y & kFrac) | kHidden) << 10;
+    const int d = ex - ey < 63 ? ex - ey : 63;
+    const u64 t = my >> d;
+    const u64 s0 = mx + (t | ((t << d) != my ? 1ull : 0ull));        // sticky; < 2^64
+    const u32 c = (u32)(s0 >> 63);                                   // renormalise by one bit, keeping the sticky
+    const u32 sl = fixpair::shf_r((u32)s0, (u32)(s0 >> 32), (int)c) | ((u32)s0 & c);
+    const u32 shi = (u32)(s0 >> 32) >> c;
+    const int e = ex + (int)c;
+    special |= e >= 2046 ? 1u : 0u;
+    return fixpair::bits_double(round_assemble(shi, sl, (u32)(e - 1)));
+}
+
+// The same with the hardware operation for the special cases (used by tests).
+FIX_HD double sqr_rn(double a) {
+    u32 sp = 0;
+    const double r = sqr_try(a, sp);
+    return sp ? a * a : r;
+}
+FIX_HD double mul_rn(double a, double b) {
+    u32 sp = 0;
+    const double r = mul_try(a, b, sp);
+    return sp ? a * b : r;
+}
+FIX_HD double add_pos_rn(double a, double b) {
+    u32 sp = 0;
+    const double r = add_pos_try(a, b, sp);
+    return sp ? a + b : r;
+}
+
+// w2 > c * r2 for w2 >= +0 (not NaN) and c = 2^k: the product is r2 with k
+// added to its exponent, exact while it stays normal, and non-negative doubles
+// order as their bit patterns.  Returns -1 when r2 is not a positive normal
+// number or the product leaves the normal range (the caller then compares in
+// FP64).
+FIX_HD int gt_scaled_pow2(double w2, double r2, int k) {
+    const u64 R = dbits(r2);
+    const int er = (int)(R >> 52);                                   // the sign bit included: negatives fail
+    if ((unsigned)(er - 1) >= 2046u || (unsigned)(er + k - 1) >= 2046u) return -1;
+    return dbits(w2) > R + ((u64)(long long)k << 52) ? 1 : 0;
+}
+
 }  // namespace exactfp

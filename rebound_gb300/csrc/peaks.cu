@@ -111,6 +111,13 @@ __global__ void exactfp_check(long long n, unsigned long long seed, unsigned lon
         const double x = fabs(random_double(s, -1000, 2001));
         if (__double_as_longlong(exactfp::div_rn(a, b)) != __double_as_longlong(a / b)) local++;
         if (__double_as_longlong(exactfp::sqrt_rn(x)) != __double_as_longlong(sqrt(x))) local++;
+        // non-negative sums (wide and close exponents), products and squares
+        const double c = __longlong_as_double(__double_as_longlong(a) ^ (long long)(splitmix(s) & 0x3FFFFFull));
+        const double ya = fabs(a), yb = fabs(b), yc = fabs(c);
+        if (__double_as_longlong(exactfp::add_pos_rn(ya, yb)) != __double_as_longlong(ya + yb)) local++;
+        if (__double_as_longlong(exactfp::add_pos_rn(ya, yc)) != __double_as_longlong(ya + yc)) local++;
+        if (__double_as_longlong(exactfp::mul_rn(a, b)) != __double_as_longlong(a * b)) local++;
+        if (__double_as_longlong(exactfp::sqr_rn(c)) != __double_as_longlong(c * c)) local++;
     }
     if (local) atomicAdd(bad, local);
 }

@@ -347,15 +347,114 @@ struct GhostArr {
 
 constexpr int kStack = 192;
 
-// QUAD: the far-cell term of a QUADRUPOLE build (src/tree.c:293-306).
+// Walk constants.  oa2_k: opening_angle2 = 2^oa2_k exactly (kNoPow2 otherwise),
+// which turns the opening test into an integer comparison.
+constexpr int kNoPow2 = 1 << 20;
+
+struct WalkConst {
+    double G, eps2, oa2;
+    int oa2_k;
+    int soft;      // eps2 != 0: r^2 + eps^2 is formed (r^2 + 0 is r^2 itself)
+};
+
+static int pow2_exponent(double v) {
+    int e = 0;
+    const double m = frexp(v, &e);
+    return (v > 0. && m == 0.5 && e > -1000 && e < 1000) ? e - 1 : kNoPow2;
+}
+
+static WalkConst walk_const(const rgpu_config& cf, double eps2) {
+    WalkConst w;
+    w.G = cf.G;
+    w.eps2 = eps2;
+    w.oa2 = cf.opening_angle2;
+    w.oa2_k = pow2_exponent(cf.opening_angle2);
+    w.soft = eps2 != 0.;
+    return w;
+}
+
+// Rare cases of the visit below in hardware FP64: operands or results outside
+// the normal range (a zero displacement, a zero radius, subnormal or
+// overflowing squares).  Kept out of line so that the common path issues no
+// FP64 instruction for them.
+__device__ __noinline__ double r2_fp64(double dx, double dy, double dz) { return dx * dx + dy * dy + dz * dz; }
+
+__device__ __noinline__ double r3_fp64(double r2, double eps2) {
+    const double rr = sqrt(r2 + eps2);
+    return rr * rr * rr;
+}
+
+__device__ __noinline__ int open_fp64(double w2, double oa2, double r2) { return w2 > oa2 * r2; }
+
+// One root's subtree for particle i, shifted to (sx, sy, sz): the reference's
+// depth-first descent and force sum (src/tree.c:275-328; QUAD adds the far-cell
+// quadrupole term of src/tree.c:293-306).  Every FP64 operation of the visit is
+// rounded exactly as the reference rounds it.  The squares, the sums of r^2 and
+// r^2 + eps^2, the opening test, the square root, r^3 and the division run on
+// the integer pipes (exactfp); the displacement, G m / r^3 and the three
+// accumulations (signed sums) stay on the FP64 pipe, which then carries 10 of the
+// visit's 20 FP64 operations.
 template <bool QUAD>
+__device__ __forceinline__ void walk_root(int r, int i, double sx, double sy, double sz, const CellArrays& c,
+                                          const WalkConst& w, int* stack, double& ax, double& ay, double& az,
+                                          uint32_t* status) {
+    int sp = 0;
+    stack[sp++] = r;
+    while (sp > 0) {
+        const int q = stack[--sp];
+        const double dx = sx - c.mx[q], dy = sy - c.my[q], dz = sz - c.mz[q];
+        exactfp::u32 special = 0;
+        double r2 = exactfp::add_pos_try(
+            exactfp::add_pos_try(exactfp::sqr_try(dx, special), exactfp::sqr_try(dy, special), special),
+            exactfp::sqr_try(dz, special), special);
+        if (special) r2 = r2_fp64(dx, dy, dz);
+        const int pt = c.pt[q];
+        if (pt < 0) {
+            const double w2 = c.w2[q];
+            int open = w.oa2_k != kNoPow2 ? exactfp::gt_scaled_pow2(w2, r2, w.oa2_k) : -1;
+            if (open < 0) open = open_fp64(w2, w.oa2, r2);
+            if (open) {
+                const int f = c.first[q], n = c.nchild[q];
+                if (sp + n > kStack) { atomicOr(status, DEV_ERR_STACK); return; }
+                for (int k = n - 1; k >= 0; k--) stack[sp++] = f + k;
+                continue;
+            }
+            if (QUAD) {
+                const double rr = exactfp::sqrt_rn(r2 + w.eps2);
+                const double pf = exactfp::div_rn(-w.G, rr * rr * rr) * c.m[q];
+                const double qxx = c.qxx[q], qxy = c.qxy[q], qxz = c.qxz[q], qyy = c.qyy[q], qyz = c.qyz[q];
+                const double qzz = -qxx - qyy;
+                double qpf = exactfp::div_rn(w.G, rr * rr * rr * rr * rr);
+                ax += qpf * (dx * qxx + dy * qxy + dz * qxz);
+                ay += qpf * (dx * qxy + dy * qyy + dz * qyz);
+                az += qpf * (dx * qxz + dy * qyz + dz * qzz);
+                const double mrr = dx * dx * qxx + dy * dy * qyy + dz * dz * qzz + 2. * dx * dy * qxy +
+                                   2. * dx * dz * qxz + 2. * dy * dz * qyz;
+                qpf *= exactfp::div_rn(-5.0, 2.0 * rr * rr) * mrr;
+                ax += (qpf + pf) * dx; ay += (qpf + pf) * dy; az += (qpf + pf) * dz;
+                continue;
+            }
+        } else if (pt == i) {
+            continue;
+        }
+        exactfp::u32 special2 = 0;
+        const double s2 = w.soft ? exactfp::add_pos_try(r2, w.eps2, special2) : r2;
+        const double rr = exactfp::sqrt_rn(s2);
+        double rr3 = exactfp::mul_try(exactfp::sqr_try(rr, special2), rr, special2);
+        if (special2) rr3 = r3_fp64(r2, w.eps2);
+        const double pf = exactfp::div_rn(-w.G, rr3) * c.m[q];
+        ax += pf * dx; ay += pf * dy; az += pf * dz;
+    }
+}
+
 // Threads take particles in key order (`order`, the sorted index array of the
 // build), so a warp's 32 particles are neighbours in space: they see the same
 // roots far or near and descend the same cells, which keeps the warp converged.
 // Each particle's own sum keeps the reference's order, so results do not change.
+template <bool QUAD>
 __global__ void __launch_bounds__(128) walk_exact(ParticlesSoA p, int N, const int* __restrict__ order, CellArrays c,
-                                                  int n_root, const GhostArr* __restrict__ gh, double G, double eps2,
-                                                  double oa2, uint32_t* status) {
+                                                  int n_root, const GhostArr* __restrict__ gh, WalkConst w,
+                                                  uint32_t* status) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= N) return;
     const int i = order[k];
@@ -366,43 +465,7 @@ __global__ void __launch_bounds__(128) walk_exact(ParticlesSoA p, int N, const i
         const double sx = gh->off[g][0] + px, sy = gh->off[g][1] + py, sz = gh->off[g][2] + pz;
         for (int r = 0; r < n_root; r++) {
             if (c.pt[r] == INT_MIN) continue;
-            int sp = 0;
-            stack[sp++] = r;
-            while (sp > 0) {
-                const int q = stack[--sp];
-                const double dx = sx - c.mx[q], dy = sy - c.my[q], dz = sz - c.mz[q];
-                const double r2 = dx * dx + dy * dy + dz * dz;
-                const int pt = c.pt[q];
-                if (pt < 0) {
-                    if (c.w2[q] > oa2 * r2) {
-                        const int f = c.first[q], n = c.nchild[q];
-                        if (sp + n > kStack) { atomicOr(status, DEV_ERR_STACK); sp = 0; break; }
-                        for (int k = n - 1; k >= 0; k--) stack[sp++] = f + k;
-                        continue;
-                    }
-                    if (QUAD) {
-                        const double rr = exactfp::sqrt_rn(r2 + eps2);
-                        const double pf = exactfp::div_rn(-G, rr * rr * rr) * c.m[q];
-                        const double qxx = c.qxx[q], qxy = c.qxy[q], qxz = c.qxz[q], qyy = c.qyy[q], qyz = c.qyz[q];
-                        const double qzz = -qxx - qyy;
-                        double qpf = exactfp::div_rn(G, rr * rr * rr * rr * rr);
-                        ax += qpf * (dx * qxx + dy * qxy + dz * qxz);
-                        ay += qpf * (dx * qxy + dy * qyy + dz * qyz);
-                        az += qpf * (dx * qxz + dy * qyz + dz * qzz);
-                        const double mrr = dx * dx * qxx + dy * dy * qyy + dz * dz * qzz + 2. * dx * dy * qxy +
-                                           2. * dx * dz * qxz + 2. * dy * dz * qyz;
-                        qpf *= exactfp::div_rn(-5.0, 2.0 * rr * rr) * mrr;
-                        ax += (qpf + pf) * dx; ay += (qpf + pf) * dy; az += (qpf + pf) * dz;
-                        continue;
-                    }
-                } else if (pt == i) {
-                    continue;
-                }
-                // IEEE sqrt and division, bit-identical, on the integer pipes (exactfp)
-                const double rr = exactfp::sqrt_rn(r2 + eps2);
-                const double pf = exactfp::div_rn(-G, rr * rr * rr) * c.m[q];
-                ax += pf * dx; ay += pf * dy; az += pf * dz;
-            }
+            walk_root<QUAD>(r, i, sx, sy, sz, c, w, stack, ax, ay, az, status);
         }
     }
     p.ax[i] = ax; p.ay[i] = ay; p.az[i] = az;
@@ -444,8 +507,8 @@ __device__ __forceinline__ void virtual_root(const BoxGeom& g, double sx, double
 }
 
 __global__ void __launch_bounds__(128) walk_near(ParticlesSoA p, int N, const int* __restrict__ order, CellArrays c,
-                                                 BoxGeom geo, const GhostArr* __restrict__ gh, double G, double eps2,
-                                                 double oa2, int K, uint32_t* status) {
+                                                 BoxGeom geo, const GhostArr* __restrict__ gh, WalkConst w, int K,
+                                                 uint32_t* status) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;      // particles in key order, as walk_exact
     if (k >= N) return;
     const int i = order[k];
@@ -464,28 +527,7 @@ __global__ void __launch_bounds__(128) walk_near(ParticlesSoA p, int N, const in
         for (int ri = x0; ri <= x1; ri++) {
             const int r = (rk * geo.ny + rj) * geo.nx + ri;
             if (c.pt[r] == INT_MIN) continue;
-            int sp = 0;
-            stack[sp++] = r;
-            while (sp > 0) {
-                const int q = stack[--sp];
-                const double dx = sx - c.mx[q], dy = sy - c.my[q], dz = sz - c.mz[q];
-                const double r2 = dx * dx + dy * dy + dz * dz;
-                const int pt = c.pt[q];
-                if (pt < 0) {
-                    if (c.w2[q] > oa2 * r2) {
-                        const int f = c.first[q], n = c.nchild[q];
-                        if (sp + n > kStack) { atomicOr(status, DEV_ERR_STACK); sp = 0; break; }
-                        for (int k = n - 1; k >= 0; k--) stack[sp++] = f + k;
-                        continue;
-                    }
-                } else if (pt == i) {
-                    continue;
-                }
-                // IEEE sqrt and division, bit-identical, on the integer pipes (exactfp)
-                const double rr = exactfp::sqrt_rn(r2 + eps2);
-                const double pf = exactfp::div_rn(-G, rr * rr * rr) * c.m[q];
-                ax += pf * dx; ay += pf * dy; az += pf * dz;
-            }
+            walk_root<false>(r, i, sx, sy, sz, c, w, stack, ax, ay, az, status);
         }
     }
     p.ax[i] = ax; p.ay[i] = ay; p.az[i] = az;
@@ -925,10 +967,10 @@ int tree_accel(rgpu_sim* s) {
         ktimer_begin(s);
         if (cf.tree_quadrupole)
             walk_exact<true><<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, t->idx, arrays(t), t->n_root, g_ghosts,
-                                                                      cf.G, eps2, cf.opening_angle2, s->d_status);
+                                                                      walk_const(cf, eps2), s->d_status);
         else
             walk_exact<false><<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, t->idx, arrays(t), t->n_root, g_ghosts,
-                                                                       cf.G, eps2, cf.opening_angle2, s->d_status);
+                                                                       walk_const(cf, eps2), s->d_status);
         ktimer_end(s);
         g_launches++;
         RGPU_CUDA(s, cudaGetLastError());
@@ -951,8 +993,8 @@ int tree_accel(rgpu_sim* s) {
     }
     RootSweep* sw = (RootSweep*)t->sweep;
     build_root_sweep<<<grid_for(n_root, kB), kB, 0, s->stream>>>(arrays(t), n_root, geo, cf.G, sw);
-    walk_near<<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, t->idx, arrays(t), geo, g_ghosts, cf.G, eps2,
-                                                        cf.opening_angle2, K, s->d_status);
+    walk_near<<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, t->idx, arrays(t), geo, g_ghosts,
+                                                        walk_const(cf, eps2), K, s->d_status);
     ktimer_begin(s);
     sweep_far<<<grid_for(N, kSweepTile), kSweepTile, 0, s->stream>>>(s->p, N, sw, n_root, geo, g_ghosts, eps2, K);
     ktimer_end(s);

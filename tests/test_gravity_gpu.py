@@ -340,9 +340,10 @@ def test_energy_matches_oracle(gpu):
     assert abs(e - g["energy0"]) <= 1e-13 * abs(g["energy0"])
 
 
-def test_integer_pipe_ieee_division_and_sqrt_match_hardware(gpu):
-    # the exact tree walk's division and square root, bit for bit against the GPU's
-    # own IEEE operations on 2e7 operand sets (normal range, edge mantissas, signs)
+def test_integer_pipe_ieee_arithmetic_matches_hardware(gpu):
+    # the exact tree walk's division, square root, non-negative addition,
+    # multiplication and square, bit for bit against the GPU's own IEEE
+    # operations on 2e7 operand sets (normal range, edge mantissas, signs)
     L = gpu.load()
     bad = ctypes.c_longlong(-1)
     assert L.rgpu_selftest_exactfp(20_000_000, 12345, ctypes.byref(bad)) == 0
