@@ -487,6 +487,17 @@ def tree_summary(quick=False, steps=2, sm_count=None, sm_mhz=None):
             roof["counts"] = "tree sources changed since the ncu capture (sha256 mismatch)"
     except (OSError, ValueError, KeyError) as ex:
         roof["counts"] = repr(ex)
+    # Throughput of each FP64 routine of a visit alone (rgpu_probe_rate 5-12), as
+    # SM-sub-partition clocks per warp operation at the sampled clock.
+    if sm_mhz and sm_count:
+        names = {5: "int_div", 6: "int_sqrt", 7: "int_square", 8: "int_product", 9: "int_nonneg_sum",
+                 10: "hw_div", 11: "hw_sqrt", 12: "hw_add"}
+        clocks = {}
+        for which, name in names.items():
+            r = ctypes.c_double(0.)
+            if L.rgpu_probe_rate(which, ctypes.byref(r)) == 0 and r.value > 0:
+                clocks[name] = round(4 * sm_count * sm_mhz * 1e6 * 32 / r.value, 1)
+        roof["routine_clocks_per_warp_op"] = clocks
     return {"workload": f"ring patch {box:.0f} m box, N={len(p)}, 25 ghost boxes, {n_root * n_root} roots",
             "N": len(p), "gpu_step_s": step_s, "gpu_tree_gravity_s": grav_s, "gpu_collision_search_s": coll_s,
             "roofline": roof, "resolve": resolve,

@@ -246,9 +246,13 @@ int rgpu_set_displacement_mode(int mode);
 int rgpu_sim_guard_stats(rgpu_sim* sim, int64_t* n_inexact, int64_t* n_redo);
 /* Count of this library's kernel launches since load. */
 int64_t rgpu_launch_count(void);
-/* Measured sustained lane-operation rate (ops/s) of one instruction class on
- * the current device: 0 = FP64 FMA, 1 = FP32 FMA, 2 = FP64<->FP32 conversion,
- * 3 = FP32 rsqrt (MUFU), 4 = integer ALU (3-input logic op). */
+/* Measured sustained lane-operation rate (ops/s) of one instruction class or
+ * FP64 routine on the current device: 0 = FP64 FMA, 1 = FP32 FMA,
+ * 2 = FP64<->FP32 conversion, 3 = FP32 rsqrt (MUFU), 4 = integer ALU (3-input
+ * logic op); the exact tree walk's IEEE routines on the integer pipes:
+ * 5 = division, 6 = square root, 7 = square, 8 = product, 9 = sum of two
+ * non-negative numbers; and the hardware FP64 forms: 10 = division,
+ * 11 = square root, 12 = addition. */
 int rgpu_probe_rate(int which, double* ops_per_s);
 /* Self-check of the integer-pipe IEEE FP64 arithmetic used by the exact tree
  * walk (division, square root, non-negative addition, multiplication, square):
@@ -256,7 +260,7 @@ int rgpu_probe_rate(int which, double* ops_per_s);
  * hardware operation; *mismatches counts differences.  No reference
  * counterpart. */
 int rgpu_selftest_exactfp(long long n, unsigned long long seed, long long* mismatches);
-/* Self-check of the FMA-flavoured ensemble's FP64 division and square root
+/* Self-check of the serving kernel's FP64 division and square root
  * (hardware approximations refined by Newton steps) against the IEEE operations
  * on n pseudo-random operand sets: the largest differences in ulps.
  * No reference counterpart. */

@@ -18,7 +18,8 @@
 // system) and a set of steps-per-launch values on the live ensemble and keeps
 // the fastest combination.
 #define ENSEMBLE_NS ens_fast
-#define WH_FAST_MATH 1          // approximate-then-refined FP64 division and sqrt (whfast_core.cuh)
+#define WH_FAST_MATH 1          // FMA-contracted flavour (whfast_core.cuh)
+#define WH_INT_DIVSQRT 1        // IEEE division and sqrt on the integer pipes (whfast_core.cuh)
 #include "ensemble_kernels.cuh"
 #include "whfast_warp.cuh"
 #include <algorithm>
@@ -89,8 +90,9 @@ __global__ void __launch_bounds__(128) persistent_warp_kernel(const WarpSys* __r
     }
 }
 
-// Self-check of the fast flavour's division and square root (wh::fast_div,
-// wh::fast_sqrt) against the IEEE operations: the largest difference in ulps of
+// Self-check of the FP64-refined division and square root (wh::fast_div,
+// wh::fast_sqrt; the serving kernel's forms) against the IEEE operations: the
+// largest difference in ulps of
 // the IEEE result over n operand sets from a counter-based generator.
 __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
     z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;

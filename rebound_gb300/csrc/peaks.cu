@@ -81,6 +81,34 @@ __global__ void probe_alu(unsigned* out, unsigned m) {
     if (t == 12345u) out[0] = t;
 }
 
+// Throughput of one FP64 routine: each thread applies it to a stream of
+// independent operands (consecutive bit patterns near 1.0), so the pipes that
+// carry the routine, not latency, set the rate.  OP: 5 integer-pipe division,
+// 6 integer-pipe square root, 7 integer-pipe square, 8 integer-pipe product,
+// 9 integer-pipe non-negative sum, 10 hardware division, 11 hardware square
+// root, 12 hardware addition.
+template <int OP>
+__global__ void probe_routine(unsigned long long* out, unsigned long long base, double c) {
+    unsigned long long acc = 0;
+    exactfp::u32 special = 0;
+    const unsigned long long b0 = base + threadIdx.x * 977ull + blockIdx.x * 131ull;
+#pragma unroll 4
+    for (int it = 0; it < kIters; it++) {
+        const double x = __longlong_as_double((long long)(b0 + (unsigned long long)it * 0x10001ull));
+        double r;
+        if (OP == 5) r = exactfp::div_rn(c, x);
+        if (OP == 6) r = exactfp::sqrt_rn(x);
+        if (OP == 7) r = exactfp::sqr_try(x, special);
+        if (OP == 8) r = exactfp::mul_try(x, c, special);
+        if (OP == 9) r = exactfp::add_pos_try(x, c, special);
+        if (OP == 10) r = c / x;
+        if (OP == 11) r = sqrt(x);
+        if (OP == 12) r = x + c;
+        acc ^= (unsigned long long)__double_as_longlong(r);
+    }
+    if (acc == 0x123456789ull || special == 77u) out[0] = acc + special;
+}
+
 // Self-check of the integer-pipe IEEE division and square root against the
 // hardware operations on pseudo-random normal operands (splitmix64 stream).
 __device__ __forceinline__ unsigned long long splitmix(unsigned long long& s) {
@@ -143,7 +171,7 @@ extern "C" int rgpu_selftest_exactfp(long long n, unsigned long long seed, long 
 }
 
 extern "C" int rgpu_probe_rate(int which, double* ops_per_s) {
-    if (!ops_per_s || which < 0 || which > 4) return RGPU_ERR_ARG;
+    if (!ops_per_s || which < 0 || which > 12) return RGPU_ERR_ARG;
     int dev = 0, nsm = 1;
     if (cudaGetDevice(&dev) != cudaSuccess) return RGPU_ERR_CUDA;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -153,7 +181,8 @@ extern "C" int rgpu_probe_rate(int which, double* ops_per_s) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     const int threads = 256, blocks = nsm * 8;
-    double ops = (double)threads * blocks * kChains * kIters;
+    double ops = (double)threads * blocks * (which >= 5 ? 1 : kChains) * kIters;
+    const unsigned long long one = 0x3FF0000000000000ull;
     float best = 1e30f;
     for (int rep = 0; rep < 4; rep++) {
         cudaEventRecord(e0);
@@ -162,6 +191,14 @@ extern "C" int rgpu_probe_rate(int which, double* ops_per_s) {
             case 1: probe_ffma<<<blocks, threads>>>((float*)buf, 0.999999f, 1e-7f); break;
             case 2: probe_cvt<<<blocks, threads>>>((double*)buf, 0.5); break;
             case 4: probe_alu<<<blocks, threads>>>((unsigned*)buf, 3u); break;
+            case 5: probe_routine<5><<<blocks, threads>>>((unsigned long long*)buf, one, 1.0000001); break;
+            case 6: probe_routine<6><<<blocks, threads>>>((unsigned long long*)buf, one, 1.0000001); break;
+            case 7: probe_routine<7><<<blocks, threads>>>((unsigned long long*)buf, one, 1.0000001); break;
+            case 8: probe_routine<8><<<blocks, threads>>>((unsigned long long*)buf, one, 1.0000001); break;
+            case 9: probe_routine<9><<<blocks, threads>>>((unsigned long long*)buf, one, 1.0000001); break;
+            case 10: probe_routine<10><<<blocks, threads>>>((unsigned long long*)buf, one, 1.0000001); break;
+            case 11: probe_routine<11><<<blocks, threads>>>((unsigned long long*)buf, one, 1.0000001); break;
+            case 12: probe_routine<12><<<blocks, threads>>>((unsigned long long*)buf, one, 1.0000001); break;
             default: probe_rsqrt<<<blocks, threads>>>((float*)buf, 0.5f); break;
         }
         g_launches++;

@@ -398,52 +398,57 @@ template <bool QUAD>
 __device__ __forceinline__ void walk_root(int r, int i, double sx, double sy, double sz, const CellArrays& c,
                                           const WalkConst& w, int* stack, double& ax, double& ay, double& az,
                                           uint32_t* status) {
-    int sp = 0;
-    stack[sp++] = r;
-    while (sp > 0) {
-        const int q = stack[--sp];
-        const double dx = sx - c.mx[q], dy = sy - c.my[q], dz = sz - c.mz[q];
-        exactfp::u32 special = 0;
-        double r2 = exactfp::add_pos_try(
-            exactfp::add_pos_try(exactfp::sqr_try(dx, special), exactfp::sqr_try(dy, special), special),
-            exactfp::sqr_try(dz, special), special);
-        if (special) r2 = r2_fp64(dx, dy, dz);
-        const int pt = c.pt[q];
-        if (pt < 0) {
-            const double w2 = c.w2[q];
-            int open = w.oa2_k != kNoPow2 ? exactfp::gt_scaled_pow2(w2, r2, w.oa2_k) : -1;
-            if (open < 0) open = open_fp64(w2, w.oa2, r2);
-            if (open) {
-                const int f = c.first[q], n = c.nchild[q];
-                if (sp + n > kStack) { atomicOr(status, DEV_ERR_STACK); return; }
-                for (int k = n - 1; k >= 0; k--) stack[sp++] = f + k;
-                continue;
+    // The root itself is visited without a stack round trip; only opened cells
+    // push their children.
+    int sp = 0, q = r;
+    for (;;) {
+        {
+            const double dx = sx - c.mx[q], dy = sy - c.my[q], dz = sz - c.mz[q];
+            exactfp::u32 special = 0;
+            double r2 = exactfp::add_pos_try(
+                exactfp::add_pos_try(exactfp::sqr_try(dx, special), exactfp::sqr_try(dy, special), special),
+                exactfp::sqr_try(dz, special), special);
+            if (special) r2 = r2_fp64(dx, dy, dz);
+            const int pt = c.pt[q];
+            if (pt < 0) {
+                const double w2 = c.w2[q];
+                int open = w.oa2_k != kNoPow2 ? exactfp::gt_scaled_pow2(w2, r2, w.oa2_k) : -1;
+                if (open < 0) open = open_fp64(w2, w.oa2, r2);
+                if (open) {
+                    const int f = c.first[q], n = c.nchild[q];
+                    if (sp + n > kStack) { atomicOr(status, DEV_ERR_STACK); return; }
+                    for (int k = n - 1; k >= 0; k--) stack[sp++] = f + k;
+                    goto next;
+                }
+                if (QUAD) {
+                    const double rr = exactfp::sqrt_rn(r2 + w.eps2);
+                    const double pf = exactfp::div_rn(-w.G, rr * rr * rr) * c.m[q];
+                    const double qxx = c.qxx[q], qxy = c.qxy[q], qxz = c.qxz[q], qyy = c.qyy[q], qyz = c.qyz[q];
+                    const double qzz = -qxx - qyy;
+                    double qpf = exactfp::div_rn(w.G, rr * rr * rr * rr * rr);
+                    ax += qpf * (dx * qxx + dy * qxy + dz * qxz);
+                    ay += qpf * (dx * qxy + dy * qyy + dz * qyz);
+                    az += qpf * (dx * qxz + dy * qyz + dz * qzz);
+                    const double mrr = dx * dx * qxx + dy * dy * qyy + dz * dz * qzz + 2. * dx * dy * qxy +
+                                       2. * dx * dz * qxz + 2. * dy * dz * qyz;
+                    qpf *= exactfp::div_rn(-5.0, 2.0 * rr * rr) * mrr;
+                    ax += (qpf + pf) * dx; ay += (qpf + pf) * dy; az += (qpf + pf) * dz;
+                    goto next;
+                }
+            } else if (pt == i) {
+                goto next;
             }
-            if (QUAD) {
-                const double rr = exactfp::sqrt_rn(r2 + w.eps2);
-                const double pf = exactfp::div_rn(-w.G, rr * rr * rr) * c.m[q];
-                const double qxx = c.qxx[q], qxy = c.qxy[q], qxz = c.qxz[q], qyy = c.qyy[q], qyz = c.qyz[q];
-                const double qzz = -qxx - qyy;
-                double qpf = exactfp::div_rn(w.G, rr * rr * rr * rr * rr);
-                ax += qpf * (dx * qxx + dy * qxy + dz * qxz);
-                ay += qpf * (dx * qxy + dy * qyy + dz * qyz);
-                az += qpf * (dx * qxz + dy * qyz + dz * qzz);
-                const double mrr = dx * dx * qxx + dy * dy * qyy + dz * dz * qzz + 2. * dx * dy * qxy +
-                                   2. * dx * dz * qxz + 2. * dy * dz * qyz;
-                qpf *= exactfp::div_rn(-5.0, 2.0 * rr * rr) * mrr;
-                ax += (qpf + pf) * dx; ay += (qpf + pf) * dy; az += (qpf + pf) * dz;
-                continue;
-            }
-        } else if (pt == i) {
-            continue;
+            exactfp::u32 special2 = 0;
+            const double s2 = w.soft ? exactfp::add_pos_try(r2, w.eps2, special2) : r2;
+            const double rr = exactfp::sqrt_rn(s2);
+            double rr3 = exactfp::mul_try(exactfp::sqr_try(rr, special2), rr, special2);
+            if (special2) rr3 = r3_fp64(r2, w.eps2);
+            const double pf = exactfp::div_rn(-w.G, rr3) * c.m[q];
+            ax += pf * dx; ay += pf * dy; az += pf * dz;
         }
-        exactfp::u32 special2 = 0;
-        const double s2 = w.soft ? exactfp::add_pos_try(r2, w.eps2, special2) : r2;
-        const double rr = exactfp::sqrt_rn(s2);
-        double rr3 = exactfp::mul_try(exactfp::sqr_try(rr, special2), rr, special2);
-        if (special2) rr3 = r3_fp64(r2, w.eps2);
-        const double pf = exactfp::div_rn(-w.G, rr3) * c.m[q];
-        ax += pf * dx; ay += pf * dy; az += pf * dz;
+    next:
+        if (sp == 0) return;
+        q = stack[--sp];
     }
 }
 

@@ -340,6 +340,22 @@ def test_energy_matches_oracle(gpu):
     assert abs(e - g["energy0"]) <= 1e-13 * abs(g["energy0"])
 
 
+def test_fp64_routine_probes(gpu):
+    # throughput probes of the walk's integer-pipe routines and the hardware FP64
+    # forms (rgpu_probe_rate 5-12): every class runs and reports a finite rate;
+    # the integer-pipe division and square root beat the hardware sequences
+    L = gpu.load()
+    rates = {}
+    for which in range(5, 13):
+        r = ctypes.c_double(0.)
+        assert L.rgpu_probe_rate(which, ctypes.byref(r)) == 0
+        assert 0 < r.value < 1e15
+        rates[which] = r.value
+    assert rates[5] > rates[10] and rates[6] > rates[11]
+    bad = ctypes.c_double(0.)
+    assert L.rgpu_probe_rate(13, ctypes.byref(bad)) != 0
+
+
 def test_integer_pipe_ieee_arithmetic_matches_hardware(gpu):
     # the exact tree walk's division, square root, non-negative addition,
     # multiplication and square, bit for bit against the GPU's own IEEE
