@@ -85,10 +85,15 @@ FIX_HD double div_rn(double a, double b) {
     //    ma 2^K / mb = ma 2^(K - 52) / B = ma R 2^(K + ey - 114) = (ma 2^11 R / 2^64) 2^(lt + ey - 8)
     const u64 hi = fixpair::mulhi64(ma << 11, R);
     u64 Q = hi >> (8 - lt - ey);
-    //    exact remainder modulo 2^64 (its true value is small) and correction
+    //    exact remainder modulo 2^64 (its true value is small) and correction.
+    //    Error of Q against floor(ma 2^K / mb) = floor(T), T < 2^54: R is low by
+    //    less than 2^-53 relative (the 9 bits cleared by << 9 of a value >= 2^62),
+    //    which costs less than 2.0000005 units; the series and E / Q2 roundings
+    //    move Q by less than 2^-61 relative (0.007 units) either way.  So Q is in
+    //    [floor(T) - 3, floor(T) + 1]: one downward step, up to three upward.
     const u64 num_lo = ma << (53 + lt);                              // low 64 bits of ma 2^K
     long long rem = (long long)(num_lo - Q * mb);
-    for (int k = 0; k < 3 && rem < 0; k++) { Q -= 1; rem += (long long)mb; }
+    if (rem < 0) { Q -= 1; rem += (long long)mb; }
     for (int k = 0; k < 3 && rem >= (long long)mb; k++) { Q += 1; rem -= (long long)mb; }
     // 4. round (no ties) and assemble; the hidden bit of Q >> 1 adds the last exponent unit
     const u64 mant = (Q >> 1) + (Q & 1);
