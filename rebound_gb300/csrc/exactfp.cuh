@@ -55,13 +55,14 @@ FIX_HD float seed_rcp(float x) {
 constexpr u64 kFrac = 0xFFFFFFFFFFFFFull;
 constexpr u64 kHidden = 1ull << 52;
 
-// a / b rounded to nearest even.
-FIX_HD double div_rn(double a, double b) {
+// a / b rounded to nearest even; `special` is set (and the value is meaningless)
+// for a zero, subnormal, infinite or NaN operand or a quotient near the ends of
+// the range.  No branch: every input runs the same instructions.
+FIX_HD double div_try(double a, double b, u32& special) {
     const u64 ab = dbits(a), bb = dbits(b);
     const int ea = (int)((ab >> 52) & 0x7FF), eb = (int)((bb >> 52) & 0x7FF);
     const int be = ea - eb + 1023;                                  // biased exponent if ma >= mb
-    if ((unsigned)(ea - 1) >= 2046u || (unsigned)(eb - 1) >= 2046u || (unsigned)(be - 2) >= 2043u)
-        return a / b;                                                // zero, subnormal, inf/nan, or near the range ends
+    special |= ((unsigned)(ea - 1) >= 2046u || (unsigned)(eb - 1) >= 2046u || (unsigned)(be - 2) >= 2043u) ? 1u : 0u;
     const u64 ma = (ab & kFrac) | kHidden, mb = (bb & kFrac) | kHidden;
     const int lt = ma < mb ? 1 : 0;
     // 1. seed y0 ~ 1/B, B = mb / 2^52 in [1, 2); y0 = Y 2^(ey - 23)
@@ -101,17 +102,34 @@ FIX_HD double div_rn(double a, double b) {
     return fixpair::bits_double(bits | ((ab ^ bb) & 0x8000000000000000ull));
 }
 
-// sqrt(x) rounded to nearest even.
-FIX_HD double sqrt_rn(double x) {
-    const u64 xb_ = dbits(x);
-    const int ex = (int)(xb_ >> 52);                                 // sign bit included: negatives fail below
-    if ((unsigned)(ex - 1) >= 2046u) {
+// The hardware operations for the special cases, out of line on the device: a
+// call is never evaluated speculatively, whereas an inline `sp ? a / b : q`
+// would have the compiler issue the whole FP64 division sequence every time.
 #ifdef __CUDA_ARCH__
-        return sqrt(x);
+static __device__ __noinline__ double hw_div(double a, double b) { return a / b; }
+static __device__ __noinline__ double hw_sqrt(double x) { return sqrt(x); }
+static __device__ __noinline__ double hw_mul(double a, double b) { return a * b; }
+static __device__ __noinline__ double hw_add(double a, double b) { return a + b; }
 #else
-        return __builtin_sqrt(x);
+inline double hw_div(double a, double b) { return a / b; }
+inline double hw_sqrt(double x) { return __builtin_sqrt(x); }
+inline double hw_mul(double a, double b) { return a * b; }
+inline double hw_add(double a, double b) { return a + b; }
 #endif
-    }
+
+// a / b rounded to nearest even (the hardware division for the special cases).
+FIX_HD double div_rn(double a, double b) {
+    u32 sp = 0;
+    const double q = div_try(a, b, sp);
+    return sp ? hw_div(a, b) : q;
+}
+
+// sqrt(x) rounded to nearest even; `special` is set for x not a positive normal
+// number.  No branch.
+FIX_HD double sqrt_try(double x, u32& special) {
+    const u64 xb_ = dbits(x);
+    const int ex = (int)(xb_ >> 52);                                 // sign bit included: negatives are special
+    special |= (unsigned)(ex - 1) >= 2046u ? 1u : 0u;
     const u64 mx = (xb_ & kFrac) | kHidden;
     const int t = ex - 1075;                                         // x = mx 2^t
     const int odd = t & 1;
@@ -150,6 +168,13 @@ FIX_HD double sqrt_rn(double x) {
     const u64 mant = (Q >> 1) + (Q & 1);
     const int be = 1049 + ((t - odd) >> 1);                          // 1023 + 53 + (t - odd - 54) / 2
     return fixpair::bits_double(((u64)(be - 1) << 52) + mant);
+}
+
+// sqrt(x) rounded to nearest even (the hardware square root for the special cases).
+FIX_HD double sqrt_rn(double x) {
+    u32 sp = 0;
+    const double r = sqrt_try(x, sp);
+    return sp ? hw_sqrt(x) : r;
 }
 
 // ---------------------------------------------------------------------------
@@ -245,21 +270,21 @@ FIX_HD double add_pos_try(double a, double b, u32& special) {
     return fixpair::bits_double(round_assemble(shi, sl, (u32)(e - 1)));
 }
 
-// The same with the hardware operation for the special cases (used by tests).
+// The same with the hardware operation for the special cases.
 FIX_HD double sqr_rn(double a) {
     u32 sp = 0;
     const double r = sqr_try(a, sp);
-    return sp ? a * a : r;
+    return sp ? hw_mul(a, a) : r;
 }
 FIX_HD double mul_rn(double a, double b) {
     u32 sp = 0;
     const double r = mul_try(a, b, sp);
-    return sp ? a * b : r;
+    return sp ? hw_mul(a, b) : r;
 }
 FIX_HD double add_pos_rn(double a, double b) {
     u32 sp = 0;
     const double r = add_pos_try(a, b, sp);
-    return sp ? a + b : r;
+    return sp ? hw_add(a, b) : r;
 }
 
 // w2 > c * r2 for w2 >= +0 (not NaN) and c = 2^k: the product is r2 with k
