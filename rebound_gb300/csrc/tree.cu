@@ -379,9 +379,9 @@ static WalkConst walk_const(const rgpu_config& cf, double eps2) {
 // FP64 instruction for them.
 __device__ __noinline__ double r2_fp64(double dx, double dy, double dz) { return dx * dx + dy * dy + dz * dz; }
 
-__device__ __noinline__ double r3_fp64(double r2, double eps2) {
+__device__ __noinline__ double pf_fp64(double r2, double eps2, double G, double m) {
     const double rr = sqrt(r2 + eps2);
-    return rr * rr * rr;
+    return -G / (rr * rr * rr) * m;
 }
 
 __device__ __noinline__ int open_fp64(double w2, double oa2, double r2) { return w2 > oa2 * r2; }
@@ -440,10 +440,10 @@ __device__ __forceinline__ void walk_root(int r, int i, double sx, double sy, do
             }
             exactfp::u32 special2 = 0;
             const double s2 = w.soft ? exactfp::add_pos_try(r2, w.eps2, special2) : r2;
-            const double rr = exactfp::sqrt_rn(s2);
-            double rr3 = exactfp::mul_try(exactfp::sqr_try(rr, special2), rr, special2);
-            if (special2) rr3 = r3_fp64(r2, w.eps2);
-            const double pf = exactfp::div_rn(-w.G, rr3) * c.m[q];
+            const double rr = exactfp::sqrt_try(s2, special2);
+            const double rr3 = exactfp::mul_try(exactfp::sqr_try(rr, special2), rr, special2);
+            double pf = exactfp::div_try(-w.G, rr3, special2) * c.m[q];
+            if (special2) pf = pf_fp64(r2, w.eps2, w.G, c.m[q]);
             ax += pf * dx; ay += pf * dy; az += pf * dz;
         }
     next:
