@@ -345,18 +345,24 @@ int  rgpu_ensemble_times(rgpu_ensemble* ens, double* t);
  *   mixed-precision direct sum (RGPU_GRAVITY_MIXED_SPLIT), softening given.
  * A worker thread admits queued requests FIFO while the device bytes of the
  * resident ones stay within hbm_budget_bytes, and advances every resident
- * request in batched kernels each tick (WHFast: steps_per_launch steps per
- * slot; clusters: cluster_steps_per_tick leapfrog steps).  A request's result
- * does not depend on which other requests share its ticks. */
+ * request in batched kernels each tick (WHFast: tick_ns of device time or
+ * steps_per_launch steps per slot; clusters: cluster_steps_per_tick leapfrog
+ * steps).  A request's result does not depend on which other requests share
+ * its ticks, nor on how its steps fall into ticks. */
 enum { RGPU_SERVE_WHFAST = 1, RGPU_SERVE_CLUSTER = 2 };
 typedef struct rgpu_server_config {
     size_t hbm_budget_bytes;         /* default 120 GiB */
-    int64_t steps_per_launch;        /* WHFast steps per slot per tick (default 256) */
+    int64_t steps_per_launch;        /* WHFast steps per slot per tick when tick_ns is 0 or
+                                        thread_per_system is 1 (default 64) */
     int32_t slots_per_bucket;        /* WHFast slots per body count (default 16,384) */
     int32_t pool_particles;          /* cluster particle pool (default 4,194,304) */
     int32_t cluster_steps_per_tick;  /* default 8 */
     int32_t thread_per_system;       /* 0 (default): one warp per WHFast system, lanes = bodies
                                         (lowest latency); 1: one thread per system */
+    int64_t tick_ns;                 /* warp per system: > 0 (default 2,000,000), each slot steps
+                                        for about this much device time per tick, so light systems
+                                        are not held back by the heaviest one of the tick; 0: each
+                                        slot takes exactly steps_per_launch steps per tick */
 } rgpu_server_config;
 typedef struct rgpu_server_stats {
     int64_t completed, waiting, resident, ticks;

@@ -55,7 +55,8 @@ class Config(ctypes.Structure):
 class ServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_size_t), ("steps_per_launch", ctypes.c_int64),
                 ("slots_per_bucket", ctypes.c_int32), ("pool_particles", ctypes.c_int32),
-                ("cluster_steps_per_tick", ctypes.c_int32), ("thread_per_system", ctypes.c_int32)]
+                ("cluster_steps_per_tick", ctypes.c_int32), ("thread_per_system", ctypes.c_int32),
+                ("tick_ns", ctypes.c_int64)]
 
 
 class ServerStats(ctypes.Structure):

@@ -7,18 +7,22 @@
 // Two request kinds (the reference runs each as one reb_simulation):
 //  * WHFast planetary systems (src/integrator_whfast.c, Jacobi, safe_mode 1):
 //    slots in per-body-count buckets, warp per slot (thread per slot on
-//    request), each tick advances every live slot by min(chunk, remaining)
-//    steps; FMA contraction and the fast flavour's division and square root
-//    (WH_FAST_MATH), as in the batched ensemble;
+//    request); each tick, every live warp steps its slot until a device-time
+//    budget (tick_ns) has passed, so a tick lasts about the budget and no light
+//    system waits for the heaviest one (or, with tick_ns = 0 and on the thread
+//    path, min(chunk, remaining) steps); FMA contraction and the FP64-refined
+//    division and square root (WH_FAST_MATH);
 //  * Plummer clusters with leapfrog (src/integrator_leapfrog.c) and the
 //    mixed-precision direct sum (FP64 displacement formed from two-float
 //    splits, FP32 force, compensated FP32 accumulation): particles in a pooled
 //    SoA, one CTA per (cluster, 256-particle tile), each thread summing its
 //    cluster's j-range in a fixed order.
-// Per-request results do not depend on which other requests share a tick.
+// Per-request results do not depend on which other requests share a tick, nor on
+// how a request's steps fall into ticks.
 #define WH_FAST_MATH 1          // approximate-then-refined FP64 division and sqrt (whfast_core.cuh)
 #include "whfast_warp.cuh"
 #include <algorithm>
+#include <cstdint>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -66,17 +70,18 @@ __global__ void __launch_bounds__(128) wh_slots_kernel(double* __restrict__ st, 
 }
 
 // --- warp per system (whfast_warp.cuh) -------------------------------------------
-// Advance WHFast slot `sid` of one bucket by up to `chunk` steps; called by a whole warp.
+// Advance WHFast slot `sid` of one bucket by up to `chunk` steps, and with
+// budget_ns > 0 only for about that much device time; called by a whole warp.
 template <int NB>
 __device__ __noinline__ void warp_advance(double* __restrict__ st, const double* __restrict__ dt,
                                           int64_t* __restrict__ remaining, int cap, int sid, int chunk, double G,
-                                          uint32_t* status) {
+                                          long long budget_ns, uint32_t* status) {
     const int lane = (int)(threadIdx.x & 31);
     const int64_t rem = remaining[sid];
     if (rem <= 0) return;
     const int nsteps = (int)(rem < chunk ? rem : chunk);
-    whw::warp_steps<NB>(st, cap, sid, nsteps, dt[sid], G, status);
-    if (lane == 0) remaining[sid] = rem - nsteps;
+    const int done = whw::warp_steps<NB>(st, cap, sid, nsteps, dt[sid], G, status, budget_ns);
+    if (lane == 0) remaining[sid] = rem - done;
 }
 
 // One launch per tick over the live slots of every bucket: a unit is up to four
@@ -90,27 +95,27 @@ struct WarpUnit {
 };
 
 __global__ void __launch_bounds__(128) wh_warp_units(const WarpUnit* __restrict__ units, int chunk, double G,
-                                                     uint32_t* status) {
+                                                     long long budget_ns, uint32_t* status) {
     const WarpUnit U = units[blockIdx.x];
     const int w = (int)(threadIdx.x >> 5);
     if (w >= U.nslots) return;                       // whole warps exit together
     const int sid = U.slot0 + w;
     switch (U.nb) {
-        case 2: warp_advance<2>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
-        case 3: warp_advance<3>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
-        case 4: warp_advance<4>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
-        case 5: warp_advance<5>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
-        case 6: warp_advance<6>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
-        case 7: warp_advance<7>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
-        case 8: warp_advance<8>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
-        case 9: warp_advance<9>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
-        case 10: warp_advance<10>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
-        case 11: warp_advance<11>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
-        case 12: warp_advance<12>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
-        case 13: warp_advance<13>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
-        case 14: warp_advance<14>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
-        case 15: warp_advance<15>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
-        default: warp_advance<16>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, status); break;
+        case 2: warp_advance<2>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, budget_ns, status); break;
+        case 3: warp_advance<3>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, budget_ns, status); break;
+        case 4: warp_advance<4>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, budget_ns, status); break;
+        case 5: warp_advance<5>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, budget_ns, status); break;
+        case 6: warp_advance<6>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, budget_ns, status); break;
+        case 7: warp_advance<7>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, budget_ns, status); break;
+        case 8: warp_advance<8>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, budget_ns, status); break;
+        case 9: warp_advance<9>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, budget_ns, status); break;
+        case 10: warp_advance<10>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, budget_ns, status); break;
+        case 11: warp_advance<11>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, budget_ns, status); break;
+        case 12: warp_advance<12>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, budget_ns, status); break;
+        case 13: warp_advance<13>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, budget_ns, status); break;
+        case 14: warp_advance<14>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, budget_ns, status); break;
+        case 15: warp_advance<15>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, budget_ns, status); break;
+        default: warp_advance<16>(U.st, U.dt, U.remaining, U.cap, sid, chunk, G, budget_ns, status); break;
     }
 }
 
@@ -475,7 +480,9 @@ void whfast_worker(rgpu_server* s) {
             s->cv_work.wait_for(lk, std::chrono::milliseconds(20));
             continue;
         }
-        const int chunk = (int)s->cfg.steps_per_launch;
+        // fixed chunk, or (warp per system, tick_ns > 0) a device-time budget per slot
+        const bool sliced = !s->cfg.thread_per_system && s->cfg.tick_ns > 0;
+        const int chunk = sliced ? INT32_MAX : (int)s->cfg.steps_per_launch;
         std::vector<WhBucket*> live;
         for (auto& kv : s->buckets) if (kv.second.cap && kv.second.live) live.push_back(&kv.second);
         lk.unlock();
@@ -504,7 +511,7 @@ void whfast_worker(rgpu_server* s) {
             }
             if (nu && nu <= s->units_cap) {
                 cudaMemcpyAsync(s->d_units, s->units.data(), sizeof(WarpUnit) * nu, cudaMemcpyHostToDevice, st);
-                wh_warp_units<<<nu, 128, 0, st>>>(s->d_units, chunk, 1.0, s->d_status);
+                wh_warp_units<<<nu, 128, 0, st>>>(s->d_units, chunk, 1.0, (long long)s->cfg.tick_ns, s->d_status);
                 g_launches++;
             }
             for (WhBucket* B : live) {
@@ -703,6 +710,7 @@ void rgpu_server_config_default(rgpu_server_config* c) {
     c->pool_particles = 1 << 22;
     c->steps_per_launch = 64;
     c->cluster_steps_per_tick = 8;
+    c->tick_ns = 2000000;
 }
 
 int rgpu_server_create(rgpu_server** out, const rgpu_server_config* cfg) {
@@ -714,7 +722,10 @@ int rgpu_server_create(rgpu_server** out, const rgpu_server_config* cfg) {
     if (!s) return RGPU_ERR_NOMEM;
     if (cfg) s->cfg = *cfg; else rgpu_server_config_default(&s->cfg);
     if (s->cfg.slots_per_bucket < 32 || s->cfg.pool_particles < 256 || s->cfg.steps_per_launch < 1 ||
-        s->cfg.cluster_steps_per_tick < 1) { delete s; return RGPU_ERR_ARG; }
+        s->cfg.steps_per_launch > INT32_MAX || s->cfg.cluster_steps_per_tick < 1 || s->cfg.tick_ns < 0) {
+        delete s;
+        return RGPU_ERR_ARG;
+    }
     const int P = (int)s->cfg.pool_particles;
     s->pool_cap = P;
     double** f[10] = {&s->pool.x, &s->pool.y, &s->pool.z, &s->pool.vx, &s->pool.vy, &s->pool.vz,

@@ -40,11 +40,20 @@ __device__ __forceinline__ double lane_exclusive(double v, int lane) {  // sum o
     return lane == 0 ? 0. : e;
 }
 
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // Advance one system of a [field][body][system] table (`cap` systems per field
-// row) by `nsteps` steps of length h; called by a whole warp.
+// row) by up to `nsteps` steps of length h; called by a whole warp.  With
+// budget_ns > 0 the warp also stops after the first step that ends budget_ns
+// or more after it started (lane 0's clock decides for the whole warp).
+// Returns the steps taken.
 template <int NB>
-__device__ __forceinline__ void warp_steps(double* __restrict__ st, int cap, int sid, int nsteps, double h, double G,
-                                           uint32_t* status) {
+__device__ __forceinline__ int warp_steps(double* __restrict__ st, int cap, int sid, int nsteps, double h, double G,
+                                          uint32_t* status, long long budget_ns = 0) {
     const int lane = (int)(threadIdx.x & 31);
     const size_t f = (size_t)NB * cap;
     const bool on = lane < NB;
@@ -67,6 +76,23 @@ __device__ __forceinline__ void warp_steps(double* __restrict__ st, int cap, int
     double mj[NB];
 #pragma unroll
     for (int j = 0; j < NB; j++) mj[j] = __shfl_sync(kFull, m, j);
+    // Pair forces are spread over the lanes: lane l of round r holds the pair
+    // p = 32 r + l (bodies pi < pj, in row order).  A lone warp is bound by FP64
+    // warp instructions (each holds the pipe for 64 clocks whatever the active
+    // lanes), so one square root and division per pair across 32 lanes beats one
+    // row per lane.
+    constexpr int kPairs = NB * (NB - 1) / 2;
+    constexpr int kRounds = (kPairs + 31) / 32;
+    int pi[kRounds], pj[kRounds];
+#pragma unroll
+    for (int r = 0; r < kRounds; r++) {
+        int q = 32 * r + lane, a = 0;
+        while (a < NB - 1 && q >= NB - 1 - a) { q -= NB - 1 - a; a++; }
+        pi[r] = a;
+        pj[r] = a + 1 + q;                        // >= NB for lanes past the last pair
+    }
+    const unsigned long long t_start = budget_ns > 0 ? global_ns() : 0ull;
+    int done = 0;
     for (int k = 0; k < nsteps; k++) {
         // inertial -> Jacobi (lane 0: centre of mass)
         double qx, qy, qz, ux, uy, uz;
@@ -100,17 +126,40 @@ __device__ __forceinline__ void warp_steps(double* __restrict__ st, int cap, int
                          Wz = lane_suffix<NB>(wf * qz, lane);
             x = (jac ? qx : 0.) + Xc - Wx; y = (jac ? qy : 0.) + Yc - Wy; z = (jac ? qz : 0.) + Zc - Wz;
         }
-        // inertial accelerations, all pairs except (0, 1), no softening (src/gravity.c:195-257)
+        // inertial accelerations, all pairs except (0, 1), no softening (src/gravity.c:195-257):
+        // G (x_i - x_j) / r^3 once per pair, then each body sums its partners' terms in order
+        double gx[kRounds], gy[kRounds], gz[kRounds];
+#pragma unroll
+        for (int r = 0; r < kRounds; r++) {
+            const int a = pi[r], b = pj[r] < NB ? pj[r] : a;
+            const double dx = __shfl_sync(kFull, x, a) - __shfl_sync(kFull, x, b);
+            const double dy = __shfl_sync(kFull, y, a) - __shfl_sync(kFull, y, b);
+            const double dz = __shfl_sync(kFull, z, a) - __shfl_sync(kFull, z, b);
+            double g = 0.;
+            if (pj[r] < NB) {
+                const double rr = sqrt(dx * dx + dy * dy + dz * dz);
+                g = G / (rr * rr * rr);
+            }
+            gx[r] = g * dx; gy[r] = g * dy; gz[r] = g * dz;
+        }
         double ax = 0., ay = 0., az = 0.;
 #pragma unroll
-        for (int j = 0; j < NB; j++) {
-            const double xj = __shfl_sync(kFull, x, j), yj = __shfl_sync(kFull, y, j), zj = __shfl_sync(kFull, z, j);
-            if (on && j != lane && lane + j != 1) {
-                const double dx = x - xj, dy = y - yj, dz = z - zj;
-                const double r = sqrt(dx * dx + dy * dy + dz * dz);
-                const double pfj = -(G / (r * r * r)) * mj[j];
-                ax += pfj * dx; ay += pfj * dy; az += pfj * dz;
+        for (int q = 0; q < NB; q++) {
+            // partner q: its pair's term sits at row-order index p (round p / 32,
+            // lane p % 32) and enters with -m_q for the pair's first body, +m_q
+            // for the second
+            const int a = lane < q ? lane : q, b = lane < q ? q : lane;
+            const int p = a * (NB - 1) - a * (a - 1) / 2 + (b - a - 1);
+            const double sgm = (lane == q || !on || (a == 0 && b == 1)) ? 0. : (lane < q ? -mj[q] : mj[q]);
+            double tx = 0., ty = 0., tz = 0.;
+#pragma unroll
+            for (int r = 0; r < kRounds; r++) {
+                const int sl = p - 32 * r;
+                const double vx_ = __shfl_sync(kFull, gx[r], sl & 31), vy_ = __shfl_sync(kFull, gy[r], sl & 31),
+                             vz_ = __shfl_sync(kFull, gz[r], sl & 31);
+                if (sl >= 0 && sl < 32) { tx = vx_; ty = vy_; tz = vz_; }
             }
+            ax += sgm * tx; ay += sgm * ty; az += sgm * tz;
         }
         // kick in Jacobi coordinates (src/transformations.c:147-176, src/integrator_whfast.c:447-472)
         {
@@ -140,11 +189,17 @@ __device__ __forceinline__ void warp_steps(double* __restrict__ st, int cap, int
             vx = (jac ? ux : 0.) + Vx - Wvx; vy = (jac ? uy : 0.) + Vy - Wvy; vz = (jac ? uz : 0.) + Vz - Wvz;
         }
         if (!on) { x = y = z = vx = vy = vz = 0.; }
+        done = k + 1;
+        if (budget_ns > 0) {
+            const long long el = (long long)(global_ns() - t_start);
+            if (__shfl_sync(kFull, el, 0) >= budget_ns) break;
+        }
     }
     if (on) {
         st[o] = x; st[f + o] = y; st[2 * f + o] = z;
         st[3 * f + o] = vx; st[4 * f + o] = vy; st[5 * f + o] = vz;
     }
+    return done;
 }
 
 }  // namespace whw

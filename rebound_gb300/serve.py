@@ -21,13 +21,14 @@ WHFAST, CLUSTER = 1, 2
 
 class Server:
     def __init__(self, hbm_budget_bytes=None, steps_per_launch=None, slots_per_bucket=None, pool_particles=None,
-                 cluster_steps_per_tick=None, thread_per_system=None):
+                 cluster_steps_per_tick=None, thread_per_system=None, tick_ns=None):
         self._L = _lib.load()
         cfg = ServerConfig()
         self._L.rgpu_server_config_default(ctypes.byref(cfg))
         for k, v in dict(hbm_budget_bytes=hbm_budget_bytes, steps_per_launch=steps_per_launch,
                          slots_per_bucket=slots_per_bucket, pool_particles=pool_particles,
-                         cluster_steps_per_tick=cluster_steps_per_tick, thread_per_system=thread_per_system).items():
+                         cluster_steps_per_tick=cluster_steps_per_tick, thread_per_system=thread_per_system,
+                         tick_ns=tick_ns).items():
             if v is not None:
                 setattr(cfg, k, v)
         h = ctypes.c_void_p()
@@ -151,12 +152,13 @@ def run_stream(reqs, rate, seed=9, server=None, deadline_s=900.0):
     return lat, results, makespan, st
 
 
-def run_stream_bounded(reqs, rate, wall_s, seed=9):
+def run_stream_bounded(reqs, rate, wall_s, seed=9, **server_kw):
     """Submit `reqs` with Poisson arrivals at `rate` per second and stop waiting
     `wall_s` seconds after the first submission.  Returns the server-side latency
     of every request that finished by then (NaN for the others), the number still
-    in flight, the elapsed time and the server's counters."""
-    srv = Server()
+    in flight, the elapsed time and the server's counters.  `server_kw` configure
+    the Server."""
+    srv = Server(**server_kw)
     rng = np.random.default_rng(seed)
     gaps = rng.exponential(1.0 / rate, size=len(reqs))
     ids = []
@@ -219,7 +221,8 @@ def plain_rate(reqs, max_whfast=8, steps_cap=400, clusters=2, cluster_steps_cap=
             "cluster_pair_int_per_s": pairs / cl_time if cl_time else None}
 
 
-def bench_summary(quick=False, n_requests=240, rates=(100.0,), t_end_periods=(1e2, 1e5), wall_s=90.0):
+def bench_summary(quick=False, n_requests=240, rates=(100.0,), t_end_periods=(1e2, 1e5), wall_s=90.0,
+                  **server_kw):
     """Served stream of the configuration: 80 % WHFast systems with end times
     log-uniform in [1e2, 1e5] inner periods (2e3 to 2e6 steps each), 20 % Plummer
     clusters, Poisson arrivals.  The run is bounded by the request count and by
@@ -236,7 +239,7 @@ def bench_summary(quick=False, n_requests=240, rates=(100.0,), t_end_periods=(1e
     kinds = np.array([r[0] for r in reqs])
     steps = np.array([r[3] for r in reqs], dtype=np.float64)
     for rate in rates:
-        lat, in_flight, elapsed, st = run_stream_bounded(reqs, rate, wall_s)
+        lat, in_flight, elapsed, st = run_stream_bounded(reqs, rate, wall_s, **server_kw)
         ok = np.isfinite(lat)
         q = lambda m, f: float(np.quantile(lat[ok & m], f)) if np.any(ok & m) else None
         out["runs"].append({"rate_per_s": rate, "completed": int(ok.sum()), "in_flight_at_end": int(in_flight),

@@ -36,6 +36,32 @@ def test_results_identical_alone_and_in_the_mix(gpu):
         assert same(out, mixed[q]), q
 
 
+def test_time_sliced_ticks_give_the_same_results(gpu):
+    # tick_ns > 0: each warp steps its system for a device-time budget per tick
+    # instead of a fixed chunk; results are the same step sequence, so bit for
+    # bit the fixed-chunk results
+    from rebound_gb300.serve import Server, run_stream
+    reqs = small_stream(gpu, 16)
+    fixed = Server(tick_ns=0)
+    _, res_fixed, _, st_fixed = run_stream(reqs, rate=1000.0, server=fixed)
+    fixed.close()
+    sliced = Server(tick_ns=200_000)
+    _, res_sliced, _, st_sliced = run_stream(reqs, rate=1000.0, server=sliced)
+    sliced.close()
+    assert st_sliced["completed"] == st_fixed["completed"] == len(reqs)
+    for q in range(len(reqs)):
+        assert same(res_fixed[q], res_sliced[q]), q
+
+
+def test_time_sliced_config_is_checked(gpu):
+    from rebound_gb300 import _lib
+    from rebound_gb300.serve import Server
+    with pytest.raises(_lib.RGPUError):
+        Server(tick_ns=-1)
+    with pytest.raises(_lib.RGPUError):
+        Server(steps_per_launch=1 << 40)
+
+
 @pytest.mark.parametrize("thread_per_system", [0, 1])
 def test_results_track_plain_path(gpu, thread_per_system):
     # 0: warp per WHFast system (lanes = bodies, prefix-sum Jacobi transforms);
