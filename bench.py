@@ -331,6 +331,8 @@ def run_gb300(args):
             from rebound_gb300 import ensemble as E
             extra["ensemble"] = E.bench_summary(quick=args.quick)
             extra["ensemble"]["cpu_baseline"] = ensemble_cpu_baseline(seconds=2.0 if args.quick else 8.0)
+            extra["ensemble"]["roofline"] = ensemble_roofline(extra["ensemble"]["system_steps_per_s"], sm_count,
+                                                              (clk or {}).get("sm_mhz"))
         except Exception as ex:  # reported, not hidden
             extra["ensemble"] = {"error": repr(ex)}
     if args.tree and rank == 0 and not args.lite:
@@ -677,6 +679,30 @@ def ensemble_cpu_baseline(seconds=8.0, seed=3, steps=10000):
 
 
 COUNTS_FILE = os.path.join(REPO, "profiles", "direct_kernel_counts.json")
+ENSEMBLE_COUNTS_FILE = os.path.join(REPO, "profiles", "ensemble_kernel_counts.json")
+
+
+def ensemble_roofline(rate, sm_count, sm_mhz):
+    """FP64-pipe roofline of the thread-per-system ensemble kernel: FP64-pipe lane
+    instructions per system-step from the committed ncu count (valid while the
+    kernel's sources hash to the recorded digest) x the measured system-steps/s,
+    against the nominal FP64 pipe rate (0.5 lanes/clock/SMSP) at the sampled clock."""
+    roof = {"kernel": "ens_fast::persistent_kernel", "bound": "fp64"}
+    try:
+        with open(ENSEMBLE_COUNTS_FILE) as f:
+            rec = json.load(f)
+        if sources_digest(rec["sources"]) != rec["sha256"]:
+            roof["counts"] = "ensemble sources changed since the ncu capture (sha256 mismatch)"
+            return roof
+        ach = rec["fp64_lane_inst_per_system_step"] * rate
+        peak = FP64_LANES_PER_CLK_PER_SMSP * 4 * sm_count * sm_mhz * 1e6 if (sm_count and sm_mhz) else None
+        roof.update({"achieved": ach / 1e12, "peak": peak / 1e12 if peak else None, "unit": "T lane-inst/s",
+                     "frac": ach / peak if peak else None,
+                     "inst_per_system_step": rec["fp64_lane_inst_per_system_step"],
+                     "peak_source": "nominal FP64 pipe rate at the sampled SM clock"})
+    except (OSError, ValueError, KeyError) as ex:
+        roof["counts"] = repr(ex)
+    return roof
 
 
 def sources_digest(paths):
