@@ -146,8 +146,14 @@ WH_SOLVER void kepler_solver(double& px, double& py, double& pz, double& pvx, do
     const double eta0 = x * vx + y * vy + z * vz;
     const double zeta0 = mu - beta * r0;
     double X, Gs[4], X_per_period = __longlong_as_double(0x7ff8000000000000LL);
+#ifndef WH_INT_DIVSQRT
+    double invperiod = 0.;
+#endif
     if (beta > 0.) {
         const double sb = WH_SQRT(beta);
+#ifndef WH_INT_DIVSQRT
+        invperiod = WH_DIV(sb * beta, 2. * M_PI * mu);
+#endif
         X_per_period = WH_DIV(2. * M_PI, sb);
         const double dtr0i = dt * r0i;
         X = dtr0i * (1. - dtr0i * eta0 * 0.5 * r0i);
@@ -203,9 +209,12 @@ WH_SOLVER void kepler_solver(double& px, double& py, double& pz, double& pvx, do
         // Bisection fallback (src/integrator_whfast.c:333-370), capped.
         double Xmin, Xmax;
         if (beta > 0.) {
-            // the orbital frequency, needed only here (src/integrator_whfast.c:262)
+#ifdef WH_INT_DIVSQRT
+            // the ensemble forms the orbital frequency only here, where it is
+            // used (the reference forms it up front for a warning, :258)
             const double sb = WH_SQRT(beta);
             const double invperiod = WH_DIV(sb * beta, 2. * M_PI * mu);
+#endif
             Xmin = X_per_period * floor(dt * invperiod);
             Xmax = Xmin + X_per_period;
         } else {
