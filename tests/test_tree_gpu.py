@@ -264,6 +264,20 @@ def test_tree_split_mode_matches_exact_walk(gpu):
         assert abs(qs - qe) <= 1e-2 * qe, (q, qe, qs)
 
 
+@pytest.mark.parametrize("theta2", [0.3, 0.7, 0.125])
+def test_tree_gravity_bit_exact_any_opening_angle(gpu, theta2):
+    # opening_angle2 = 2^k turns the walk's opening test into an integer
+    # comparison; any other value takes the FP64 comparison.  Both must give the
+    # oracle's tree accelerations bit for bit (0.125 = 2^-3 is the integer path).
+    g = golden("ring_patch.npz")
+    sim = ring_gpu(gpu, g)
+    sim.opening_angle2 = theta2
+    sim.update_acceleration()
+    orc = ring_oracle(g)
+    orc.s.opening_angle2 = theta2
+    assert np.array_equal(gpu.accelerations(sim), orc.gravity("tree"))
+
+
 @pytest.mark.parametrize("theta2", [0.25, 0.5])
 def test_tree_quadrupole_bit_exact(gpu, theta2):
     # mass quadrupoles in the cells and the quadrupole far-cell term, against the
