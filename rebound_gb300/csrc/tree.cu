@@ -354,7 +354,6 @@ constexpr int kNoPow2 = 1 << 20;
 struct WalkConst {
     double G, eps2, oa2;
     int oa2_k;
-    int soft;      // eps2 != 0: r^2 + eps^2 is formed (r^2 + 0 is r^2 itself)
 };
 
 static int pow2_exponent(double v) {
@@ -369,7 +368,6 @@ static WalkConst walk_const(const rgpu_config& cf, double eps2) {
     w.eps2 = eps2;
     w.oa2 = cf.opening_angle2;
     w.oa2_k = pow2_exponent(cf.opening_angle2);
-    w.soft = eps2 != 0.;
     return w;
 }
 
@@ -389,11 +387,12 @@ __device__ __noinline__ int open_fp64(double w2, double oa2, double r2) { return
 // One root's subtree for particle i, shifted to (sx, sy, sz): the reference's
 // depth-first descent and force sum (src/tree.c:275-328; QUAD adds the far-cell
 // quadrupole term of src/tree.c:293-306).  Every FP64 operation of the visit is
-// rounded exactly as the reference rounds it.  The squares, the sums of r^2 and
-// r^2 + eps^2, the opening test, the square root, r^3 and the division run on
-// the integer pipes (exactfp); the displacement, G m / r^3 and the three
-// accumulations (signed sums) stay on the FP64 pipe, which then carries 10 of the
-// visit's 20 FP64 operations.
+// rounded exactly as the reference rounds it.  The squares, the two sums of r^2,
+// the opening test, the square root, r^3 and the division run on the integer
+// pipes (exactfp); the displacement, r^2 + eps^2, G m / r^3 and the three
+// accumulations stay on the FP64 pipe, which then carries 11 of the visit's 20
+// FP64 operations (the split that measured fastest: moving r^2 + eps^2 to the
+// integer pipes, or r^3 or the sums of r^2 to the FP64 pipe, was slower).
 template <bool QUAD>
 __device__ __forceinline__ void walk_root(int r, int i, double sx, double sy, double sz, const CellArrays& c,
                                           const WalkConst& w, int* stack, double& ax, double& ay, double& az,
@@ -439,7 +438,7 @@ __device__ __forceinline__ void walk_root(int r, int i, double sx, double sy, do
                 goto next;
             }
             exactfp::u32 special2 = 0;
-            const double s2 = w.soft ? exactfp::add_pos_try(r2, w.eps2, special2) : r2;
+            const double s2 = r2 + w.eps2;
             const double rr = exactfp::sqrt_try(s2, special2);
             const double rr3 = exactfp::mul_try(exactfp::sqr_try(rr, special2), rr, special2);
             double pf = exactfp::div_try(-w.G, rr3, special2) * c.m[q];
