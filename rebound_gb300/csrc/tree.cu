@@ -390,7 +390,7 @@ __device__ __noinline__ int open_fp64(double w2, double oa2, double r2) { return
 // rounded exactly as the reference rounds it.  The squares, the two sums of r^2,
 // the opening test, the square root, r^3 and the division run on the integer
 // pipes (exactfp); the displacement, r^2 + eps^2, G m / r^3 and the three
-// accumulations stay on the FP64 pipe, which then carries 11 of the visit's 20
+// accumulations stay on the FP64 pipe, which then carries 11 of the visit's 22
 // FP64 operations (the split that measured fastest: moving r^2 + eps^2 to the
 // integer pipes, or r^3 or the sums of r^2 to the FP64 pipe, was slower).
 template <bool QUAD>
