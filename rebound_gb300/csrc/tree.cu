@@ -483,24 +483,38 @@ __global__ void __launch_bounds__(128) walk_exact(ParticlesSoA p, int N, const i
 // window |offset| <= K with the reference's FP64 descent and sweeps all other
 // roots as monopoles in a tiled kernel: FP64 displacement formed from two-float
 // splits, FP32 force, compensated FP32 accumulation.
-struct RootSweep {
-    float4 hi;      // COM (hi split) and G m (float)
-    float4 lo;      // COM (lo split)
-    int4 meta;      // root ix, iy, iz, leaf particle index (or -1)
+// Roots in pairs for the packed FP32x2 sweep (80 B): COM hi / lo two-float splits
+// and G m of both roots, and for each root its index position (ix | iy << 11 |
+// iz << 22) and its leaf particle (-1 for a cell or an empty root).  Empty roots
+// and the partner of the last root of an odd count are massless.
+struct __align__(16) RootPair {
+    float4 a, b, c, d;   // (xh0, xh1, yh0, yh1), (zh0, zh1, Gm0, Gm1), (xl0, xl1, yl0, yl1), (zl0, zl1, 0, 0)
+    int4 meta;           // pos0, pos1, leaf0, leaf1
 };
 
-__global__ void build_root_sweep(CellArrays c, int n_root, BoxGeom g, double G, RootSweep* __restrict__ out) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= n_root) return;
-    const bool empty = c.pt[r] == INT_MIN;
-    const double mx = empty ? 0. : c.mx[r], my = empty ? 0. : c.my[r], mz = empty ? 0. : c.mz[r];
-    const double gm = empty ? 0. : G * c.m[r];
-    const float hx = (float)mx, hy = (float)my, hz = (float)mz;
-    RootSweep s;
-    s.hi = make_float4(hx, hy, hz, (float)gm);
-    s.lo = make_float4((float)(mx - (double)hx), (float)(my - (double)hy), (float)(mz - (double)hz), 0.f);
-    s.meta = make_int4(r % g.nx, (r / g.nx) % g.ny, r / (g.nx * g.ny), (!empty && c.pt[r] >= 0) ? c.pt[r] : -1);
-    out[r] = s;
+__global__ void build_root_pairs(CellArrays c, int n_root, BoxGeom g, double G, RootPair* __restrict__ out) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (n_root + 1) / 2) return;
+    float xh[2], yh[2], zh[2], gm[2], xl[2], yl[2], zl[2];
+    int pos[2], leaf[2];
+    for (int k = 0; k < 2; k++) {
+        const int r = 2 * q + k;
+        const bool full = r < n_root && c.pt[r] != INT_MIN;
+        const double mx = full ? c.mx[r] : 0., my = full ? c.my[r] : 0., mz = full ? c.mz[r] : 0.;
+        xh[k] = (float)mx; yh[k] = (float)my; zh[k] = (float)mz;
+        xl[k] = (float)(mx - (double)xh[k]); yl[k] = (float)(my - (double)yh[k]); zl[k] = (float)(mz - (double)zh[k]);
+        gm[k] = full ? (float)(G * c.m[r]) : 0.f;
+        const int rr = r < n_root ? r : 0;
+        pos[k] = (rr % g.nx) | (((rr / g.nx) % g.ny) << 11) | ((rr / (g.nx * g.ny)) << 22);
+        leaf[k] = (full && c.pt[r] >= 0) ? c.pt[r] : -1;
+    }
+    RootPair P;
+    P.a = make_float4(xh[0], xh[1], yh[0], yh[1]);
+    P.b = make_float4(zh[0], zh[1], gm[0], gm[1]);
+    P.c = make_float4(xl[0], xl[1], yl[0], yl[1]);
+    P.d = make_float4(zl[0], zl[1], 0.f, 0.f);
+    P.meta = make_int4(pos[0], pos[1], leaf[0], leaf[1]);
+    out[q] = P;
 }
 
 __device__ __forceinline__ void virtual_root(const BoxGeom& g, double sx, double sy, double sz, int& ix, int& iy,
@@ -537,45 +551,82 @@ __global__ void __launch_bounds__(128) walk_near(ParticlesSoA p, int N, const in
     p.ax[i] = ax; p.ay[i] = ay; p.az[i] = az;
 }
 
-constexpr int kSweepTile = 256;
+constexpr int kSweepTile = 256;              // particles per CTA
+constexpr int kSweepPairs = kSweepTile / 2;   // root pairs per shared-memory tile
+constexpr int kSweepSub = 32;                 // root pairs summed in FP32 before a fold
 
-__global__ void __launch_bounds__(kSweepTile) sweep_far(ParticlesSoA p, int N, const RootSweep* __restrict__ roots,
-                                                        int n_root, BoxGeom geo, const GhostArr* __restrict__ gh,
+// Far roots of every particle and ghost box: the packed FP32x2 pipe evaluates two
+// roots per instruction (displacement from the two-float splits, r^2, G m / r^3,
+// the accumulation); the roots of the particle's near window (walked exactly by
+// walk_near) and its own leaf root contribute zero.  Terms are summed in FP32 over
+// 32 root pairs and each sum is folded into a compensated FP32 pair.
+__global__ void __launch_bounds__(kSweepTile) sweep_far(ParticlesSoA p, int N, const RootPair* __restrict__ roots,
+                                                        int n_pair, BoxGeom geo, const GhostArr* __restrict__ gh,
                                                         double eps2, int K) {
-    __shared__ RootSweep tile[kSweepTile];
+    __shared__ RootPair tile[kSweepPairs];
     const int i = blockIdx.x * kSweepTile + threadIdx.x;
     const bool live = i < N;
     const double px = live ? p.x[i] : 0., py = live ? p.y[i] : 0., pz = live ? p.z[i] : 0.;
-    const float e2 = (float)eps2;
+    const float ef = (float)eps2;
+    const float2 e2 = make_float2(ef, ef);
+    const unsigned span = 2u * (unsigned)K;
     float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
-    for (int rt = 0; rt < n_root; rt += kSweepTile) {
+    for (int qt = 0; qt < n_pair; qt += kSweepPairs) {
         __syncthreads();
-        const int rl = rt + threadIdx.x;
-        if (rl < n_root) tile[threadIdx.x] = roots[rl];
+        if (threadIdx.x < kSweepPairs) {
+            const int ql = qt + threadIdx.x;
+            if (ql < n_pair) {
+                tile[threadIdx.x] = roots[ql];
+            } else {
+                RootPair Z;
+                Z.a = Z.b = Z.c = Z.d = make_float4(0.f, 0.f, 0.f, 0.f);
+                Z.meta = make_int4(0, 0, -1, -1);
+                tile[threadIdx.x] = Z;
+            }
+        }
         __syncthreads();
-        const int nt = min(kSweepTile, n_root - rt);
+        const int nq = min(kSweepPairs, n_pair - qt);
         for (int g = 0; g < gh->n; g++) {
             const double gx = gh->off[g][0] + px, gy = gh->off[g][1] + py, gz = gh->off[g][2] + pz;
             int ixv, iyv, izv;
             virtual_root(geo, gx, gy, gz, ixv, iyv, izv);
+            const int bx = ixv - K, by = iyv - K, bz = izv - K;    // near window corner
             const float hx = (float)gx, hy = (float)gy, hz = (float)gz;
             const float lx = (float)(gx - (double)hx), ly = (float)(gy - (double)hy), lz = (float)(gz - (double)hz);
-            for (int k = 0; k < nt; k++) {
-                const RootSweep R = tile[k];
-                const bool near = abs(R.meta.x - ixv) <= K && abs(R.meta.y - iyv) <= K && abs(R.meta.z - izv) <= K;
-                const bool self = R.meta.w == i;          // a single-particle root holding i itself
-                // displacement root - particle (the force on i points along it)
-                const float dx = (R.hi.x - hx) + (R.lo.x - lx);
-                const float dy = (R.hi.y - hy) + (R.lo.y - ly);
-                const float dz = (R.hi.z - hz) + (R.lo.z - lz);
-                const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, e2)));
-                const float ri = rsqrtf(r2);
-                float s = R.hi.w * ri * ri * ri;
-                s = (near || self) ? 0.f : s;
+            const float2 nxh = make_float2(-hx, -hx), nyh = make_float2(-hy, -hy), nzh = make_float2(-hz, -hz);
+            const float2 nxl = make_float2(-lx, -lx), nyl = make_float2(-ly, -ly), nzl = make_float2(-lz, -lz);
+            for (int qs = 0; qs < nq; qs += kSweepSub) {
+                const int qe = min(nq, qs + kSweepSub);
+                float2 ax = make_float2(0.f, 0.f), ay = ax, az = ax;
+#pragma unroll 4
+                for (int q = qs; q < qe; q++) {
+                    const RootPair J = tile[q];
+                    const float2 dx = __fadd2_rn(__fadd2_rn(make_float2(J.a.x, J.a.y), nxh),
+                                                 __fadd2_rn(make_float2(J.c.x, J.c.y), nxl));
+                    const float2 dy = __fadd2_rn(__fadd2_rn(make_float2(J.a.z, J.a.w), nyh),
+                                                 __fadd2_rn(make_float2(J.c.z, J.c.w), nyl));
+                    const float2 dz = __fadd2_rn(__fadd2_rn(make_float2(J.b.x, J.b.y), nzh),
+                                                 __fadd2_rn(make_float2(J.d.x, J.d.y), nzl));
+                    const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
+                    const float2 ri = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+                    float2 s = __fmul2_rn(__fmul2_rn(ri, ri), __fmul2_rn(make_float2(J.b.z, J.b.w), ri));
+                    // near window: every index within K of the virtual root's
+                    const int p0 = J.meta.x, p1 = J.meta.y;
+                    const bool near0 = (unsigned)((p0 & 2047) - bx) <= span && (unsigned)(((p0 >> 11) & 2047) - by) <= span &&
+                                       (unsigned)((p0 >> 22) - bz) <= span;
+                    const bool near1 = (unsigned)((p1 & 2047) - bx) <= span && (unsigned)(((p1 >> 11) & 2047) - by) <= span &&
+                                       (unsigned)((p1 >> 22) - bz) <= span;
+                    s.x = (near0 || J.meta.z == i || J.b.z == 0.f) ? 0.f : s.x;
+                    s.y = (near1 || J.meta.w == i || J.b.w == 0.f) ? 0.f : s.y;
+                    ax = __ffma2_rn(s, dx, ax);
+                    ay = __ffma2_rn(s, dy, ay);
+                    az = __ffma2_rn(s, dz, az);
+                }
+                const float tx = ax.x + ax.y, ty = ay.x + ay.y, tz = az.x + az.y;
                 float t, y;
-                y = fmaf(s, dx, -cx); t = sx + y; cx = (t - sx) - y; sx = t;
-                y = fmaf(s, dy, -cy); t = sy + y; cy = (t - sy) - y; sy = t;
-                y = fmaf(s, dz, -cz); t = sz + y; cz = (t - sz) - y; sz = t;
+                y = tx - cx; t = sx + y; cx = (t - sx) - y; sx = t;
+                y = ty - cy; t = sy + y; cy = (t - sy) - y; sy = t;
+                y = tz - cz; t = sz + y; cz = (t - sz) - y; sz = t;
             }
         }
     }
@@ -988,19 +1039,20 @@ int tree_accel(rgpu_sim* s) {
     const int K = (int)ceil(1.0 / sqrt(cf.opening_angle2)) + 1;
     int n_root = 0;
     const BoxGeom geo = geometry(cf, &n_root);
-    if ((size_t)n_root > t->sweep_cap) {
+    const int n_pair = (n_root + 1) / 2;
+    if ((size_t)n_pair > t->sweep_cap) {
         cudaFree(t->sweep);
         t->sweep = nullptr;
         t->sweep_cap = 0;
-        RGPU_CUDA(s, cudaMalloc(&t->sweep, sizeof(RootSweep) * n_root));
-        t->sweep_cap = (size_t)n_root;
+        RGPU_CUDA(s, cudaMalloc(&t->sweep, sizeof(RootPair) * n_pair));
+        t->sweep_cap = (size_t)n_pair;
     }
-    RootSweep* sw = (RootSweep*)t->sweep;
-    build_root_sweep<<<grid_for(n_root, kB), kB, 0, s->stream>>>(arrays(t), n_root, geo, cf.G, sw);
+    RootPair* sw = (RootPair*)t->sweep;
+    build_root_pairs<<<grid_for(n_pair, kB), kB, 0, s->stream>>>(arrays(t), n_root, geo, cf.G, sw);
     walk_near<<<grid_for(N, 128), 128, 0, s->stream>>>(s->p, N, t->idx, arrays(t), geo, g_ghosts,
                                                         walk_const(cf, eps2), K, s->d_status);
     ktimer_begin(s);
-    sweep_far<<<grid_for(N, kSweepTile), kSweepTile, 0, s->stream>>>(s->p, N, sw, n_root, geo, g_ghosts, eps2, K);
+    sweep_far<<<grid_for(N, kSweepTile), kSweepTile, 0, s->stream>>>(s->p, N, sw, n_pair, geo, g_ghosts, eps2, K);
     ktimer_end(s);
     g_launches += 3;
     RGPU_CUDA(s, cudaGetLastError());
