@@ -722,7 +722,8 @@ int rgpu_server_create(rgpu_server** out, const rgpu_server_config* cfg) {
     if (!s) return RGPU_ERR_NOMEM;
     if (cfg) s->cfg = *cfg; else rgpu_server_config_default(&s->cfg);
     if (s->cfg.slots_per_bucket < 32 || s->cfg.pool_particles < 256 || s->cfg.steps_per_launch < 1 ||
-        s->cfg.steps_per_launch > INT32_MAX || s->cfg.cluster_steps_per_tick < 1 || s->cfg.tick_ns < 0) {
+        s->cfg.steps_per_launch > INT32_MAX || s->cfg.cluster_steps_per_tick < 1 || s->cfg.tick_ns < 0 ||
+        s->cfg.tick_ns > 1000000000) {   // a tick of at most 1 s keeps admission and waits responsive
         delete s;
         return RGPU_ERR_ARG;
     }

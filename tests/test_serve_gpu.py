@@ -59,6 +59,8 @@ def test_time_sliced_config_is_checked(gpu):
     with pytest.raises(_lib.RGPUError):
         Server(tick_ns=-1)
     with pytest.raises(_lib.RGPUError):
+        Server(tick_ns=2_000_000_000)
+    with pytest.raises(_lib.RGPUError):
         Server(steps_per_launch=1 << 40)
 
 
