@@ -28,7 +28,11 @@ constexpr int kMaxBodies = 16;
 // bit-identity for speed) gets them from the hardware's approximate reciprocal
 // and reciprocal square root refined by Newton steps in FP64 (within an ulp or
 // two of IEEE, checked by rgpu_selftest_fastmath): fewer instructions on GB300's
-// narrow FP64 pipe.
+// narrow FP64 pipe.  A unit that defines WH_INT_DIVSQRT takes the IEEE-exact
+// division and square root built on the integer pipes (exactfp), out of line so
+// the many call sites share one copy: they leave the FP64 pipe to the rest of
+// the step (the thread-per-system ensemble: +12 % system-steps/s) and, being
+// exact, keep a bit-exact unit bit-exact.
 #ifdef WH_FAST_MATH
 __device__ __forceinline__ double fast_rcp(double b) {
     double y;
@@ -53,22 +57,17 @@ __device__ __forceinline__ double fast_sqrt(double x) {
     const bool pos = x > 0. && x < __longlong_as_double(0x7ff0000000000000LL);
     return pos ? r : (x == 0. || x > 0. ? x : __longlong_as_double(0x7ff8000000000000LL));
 }
-#ifdef WH_INT_DIVSQRT
-// A unit that also defines WH_INT_DIVSQRT (the thread-per-system ensemble) takes
-// the IEEE-exact division and square root built on the integer pipes (exactfp):
-// they leave the FP64 pipe, which binds that kernel, to the rest of the step
-// (+12 % system-steps/s on 65,536 systems).  Out of line, so the many call
-// sites share one copy of each routine.
+#endif
+#if defined(WH_INT_DIVSQRT)
 static __device__ __noinline__ double int_div(double a, double b) { return ::exactfp::div_rn(a, b); }
 static __device__ __noinline__ double int_sqrt(double x) { return ::exactfp::sqrt_rn(x); }
 #define WH_DIV(a, b) (::wh::int_div((a), (b)))
 #define WH_RCP(b) (::wh::int_div(1.0, (b)))
 #define WH_SQRT(x) (::wh::int_sqrt(x))
-#else
+#elif defined(WH_FAST_MATH)
 #define WH_DIV(a, b) (::wh::fast_div((a), (b)))
 #define WH_RCP(b) (::wh::fast_rcp(b))
 #define WH_SQRT(x) (::wh::fast_sqrt(x))
-#endif
 #else
 #define WH_DIV(a, b) ((a) / (b))
 #define WH_RCP(b) (1. / (b))

@@ -277,31 +277,57 @@ __device__ void kick_helio(wh::Jacobi<NB>& h, const wh::System<NB>& s, const dou
     }
 }
 
-// BASIC gravity for any gravity_ignore_terms (src/gravity.c:180-257): pairs from
-// starti (1, or 2 to skip the 0-1 pair) against startj (0, or 1 to skip body 0).
+// BASIC gravity for any gravity_ignore_terms (src/gravity.c:180-257): pairs (i, jj)
+// with i from starti (1, or 2 to skip the 0-1 pair) and jj from startj (0, or 1
+// to skip body 0) below min(i, Ng); a_i always takes the pair's term, a_jj when i
+// is active or testparticle_type is 1.  One body per lane, bit for bit: in the
+// reference's serial loop a body's acceleration takes its terms in ascending
+// partner order (the partners below it while it is the outer index, then those
+// above it), so each lane forms its own body's sum in that order, recomputing
+// each pair's factor G / r^3 as the reference does.  One warp runs one simulation, so every
+// FP64 warp instruction holds the FP64 pipe for 64 clocks however many lanes
+// work: a row per lane takes N - 1 pair evaluations per warp instead of the
+// N (N - 1) / 2 of the serial loop on lane 0.
 template <int NB>
-__device__ void gravity_basic(const wh::System<NB>& s, double ax[NB], double ay[NB], double az[NB], double G,
-                              double eps2, int N, int Ng, int tp, int starti, int startj) {
+struct GravShared {
+    double x[NB], y[NB], z[NB], m[NB], ax[NB], ay[NB], az[NB];
+};
+
+template <int NB>
+__device__ void gravity_basic_lanes(const wh::System<NB>& s, double ax[NB], double ay[NB], double az[NB],
+                                    GravShared<NB>& g, int lane, double G, double eps2, int N, int Ng, int tp,
+                                    int starti, int startj) {
+    if (lane == 0) {
 #pragma unroll 1
-    for (int i = 0; i < N; i++) { ax[i] = 0.; ay[i] = 0.; az[i] = 0.; }
-    const int st = Ng > starti ? Ng : starti;
+        for (int i = 0; i < N; i++) { g.x[i] = s.x[i]; g.y[i] = s.y[i]; g.z[i] = s.z[i]; g.m[i] = s.m[i]; }
+    }
+    __syncwarp();
+    if (lane < N) {
+        const int k = lane;
+        const int st = Ng > starti ? Ng : starti;
+        double axk = 0., ayk = 0., azk = 0.;
 #pragma unroll 1
-    for (int i = starti; i < N; i++) {
-        const int jend = i < Ng ? i : Ng;
-#pragma unroll 1
-        for (int jj = startj; jj < jend; jj++) {
-            const double dx = (0. + s.x[i]) - s.x[jj];
-            const double dy = (0. + s.y[i]) - s.y[jj];
-            const double dz = (0. + s.z[i]) - s.z[jj];
+        for (int q = 0; q < N; q++) {
+            if (q == k) continue;
+            const bool low = q < k;                  // pair (i = k, jj = q), else (i = q, jj = k)
+            const int i = low ? k : q, jj = low ? q : k;
+            const int jend = i < Ng ? i : Ng;
+            if (i < starti || jj < startj || jj >= jend) continue;
+            if (!low && !(i < st ? true : tp != 0)) continue;
+            const double dx = (0. + g.x[i]) - g.x[jj];
+            const double dy = (0. + g.y[i]) - g.y[jj];
+            const double dz = (0. + g.z[i]) - g.z[jj];
             const double r = sqrt(dx * dx + dy * dy + dz * dz + eps2);
             const double pf = G / (r * r * r);
-            const double pfj = -pf * s.m[jj];
-            ax[i] += pfj * dx; ay[i] += pfj * dy; az[i] += pfj * dz;
-            if (i < st ? true : tp != 0) {
-                const double pfi = pf * s.m[i];
-                ax[jj] += pfi * dx; ay[jj] += pfi * dy; az[jj] += pfi * dz;
-            }
+            const double c = low ? -pf * g.m[jj] : pf * g.m[i];
+            axk += c * dx; ayk += c * dy; azk += c * dz;
         }
+        g.ax[k] = axk; g.ay[k] = ayk; g.az[k] = azk;
+    }
+    __syncwarp();
+    if (lane == 0) {
+#pragma unroll 1
+        for (int i = 0; i < N; i++) { ax[i] = g.ax[i]; ay[i] = g.ay[i]; az[i] = g.az[i]; }
     }
 }
 
@@ -350,6 +376,7 @@ __global__ void __launch_bounds__(32) whfast_program(ParticlesSoA p, double* jac
     // Lane 0 interprets the program; every lane takes part in the drifts (one body
     // each).  The coordinates live in shared memory so that all lanes see them.
     __shared__ wh::Jacobi<NB> j;
+    __shared__ GravShared<NB> gsh;
     __shared__ int stop;
     const int lane = threadIdx.x;
     wh::System<NB> s;
@@ -378,6 +405,11 @@ __global__ void __launch_bounds__(32) whfast_program(ParticlesSoA p, double* jac
             __syncwarp();
             continue;
         }
+        if (op == kOpGravity) {
+            gravity_basic_lanes(s, ax, ay, az, gsh, lane, G, eps2, N, Ng, tp, starti, startj);
+            __syncwarp();
+            continue;
+        }
         if (lane == 0) {
             switch (op) {
                 case kOpFromInertial:
@@ -393,7 +425,6 @@ __global__ void __launch_bounds__(32) whfast_program(ParticlesSoA p, double* jac
                     else if (coords == 2) whds_to_inertial(s, j, N, Na);
                     else bary_to_inertial(s, j, N, Na);
                     break;
-                case kOpGravity: gravity_basic(s, ax, ay, az, G, eps2, N, Ng, tp, starti, startj); break;
                 case kOpGravityJacobi: gravity_jacobi(s, ax, ay, az, G, N); break;
                 case kOpGravityCompensated:
                     gravity_compensated(s, ax, ay, az, G, eps2, N, Ng, tp, coords == 0 ? 1 : coords == 3 ? 0 : 2);
