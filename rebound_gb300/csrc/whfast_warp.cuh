@@ -40,6 +40,38 @@ __device__ __forceinline__ double lane_exclusive(double v, int lane) {  // sum o
     return lane == 0 ? 0. : e;
 }
 
+// Q inclusive prefix (SUFFIX: suffix) sums over the NB bodies at once.  Lanes are
+// regrouped so that lane L holds quantity L / NB of body L % NB, 32 / NB quantities
+// per pass, and each pass scans its groups of NB lanes together: every FP64
+// addition of the scan then serves several quantities (one warp instruction holds
+// the FP64 pipe for 64 clocks whatever the active lanes).  On return, lane b < NB
+// holds body b's sums; other lanes hold values nothing reads.
+template <int NB, int Q, bool SUFFIX>
+__device__ __forceinline__ void lane_scan_multi(double (&v)[Q], int lane) {
+    constexpr int PER = 32 / NB;
+    const int qi = lane / NB, b = lane % NB;
+#pragma unroll
+    for (int q0 = 0; q0 < Q; q0 += PER) {
+        double t = 0.;
+#pragma unroll
+        for (int q = 0; q < PER; q++) {
+            if (q0 + q >= Q) break;
+            const double u = __shfl_sync(kFull, v[q0 + q], b);
+            if (qi == q) t = u;
+        }
+#pragma unroll
+        for (int d = 1; d < NB; d <<= 1) {
+            const double w = SUFFIX ? __shfl_down_sync(kFull, t, d) : __shfl_up_sync(kFull, t, d);
+            if (SUFFIX ? (b + d < NB) : (b >= d)) t += w;
+        }
+#pragma unroll
+        for (int q = 0; q < PER; q++) {
+            if (q0 + q >= Q) break;
+            v[q0 + q] = __shfl_sync(kFull, t, q * NB + b);
+        }
+    }
+}
+
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -97,10 +129,9 @@ __device__ __forceinline__ int warp_steps(double* __restrict__ st, int cap, int 
         // inertial -> Jacobi (lane 0: centre of mass)
         double qx, qy, qz, ux, uy, uz;
         {
-            const double Px = lane_prefix<NB>(m * x, lane), Py = lane_prefix<NB>(m * y, lane),
-                         Pz = lane_prefix<NB>(m * z, lane);
-            const double Pvx = lane_prefix<NB>(m * vx, lane), Pvy = lane_prefix<NB>(m * vy, lane),
-                         Pvz = lane_prefix<NB>(m * vz, lane);
+            double P[6] = {m * x, m * y, m * z, m * vx, m * vy, m * vz};
+            lane_scan_multi<NB, 6, false>(P, lane);
+            const double Px = P[0], Py = P[1], Pz = P[2], Pvx = P[3], Pvy = P[4], Pvz = P[5];
             const double Ex = __shfl_up_sync(kFull, Px, 1), Ey = __shfl_up_sync(kFull, Py, 1),
                          Ez = __shfl_up_sync(kFull, Pz, 1);
             const double Evx = __shfl_up_sync(kFull, Pvx, 1), Evy = __shfl_up_sync(kFull, Pvy, 1),
@@ -122,8 +153,9 @@ __device__ __forceinline__ int warp_steps(double* __restrict__ st, int cap, int 
         // Jacobi -> inertial positions
         {
             const double Xc = __shfl_sync(kFull, qx, 0), Yc = __shfl_sync(kFull, qy, 0), Zc = __shfl_sync(kFull, qz, 0);
-            const double Wx = lane_suffix<NB>(wf * qx, lane), Wy = lane_suffix<NB>(wf * qy, lane),
-                         Wz = lane_suffix<NB>(wf * qz, lane);
+            double W[3] = {wf * qx, wf * qy, wf * qz};
+            lane_scan_multi<NB, 3, true>(W, lane);
+            const double Wx = W[0], Wy = W[1], Wz = W[2];
             x = (jac ? qx : 0.) + Xc - Wx; y = (jac ? qy : 0.) + Yc - Wy; z = (jac ? qz : 0.) + Zc - Wz;
         }
         // inertial accelerations, all pairs except (0, 1), no softening (src/gravity.c:195-257):
@@ -163,8 +195,11 @@ __device__ __forceinline__ int warp_steps(double* __restrict__ st, int cap, int 
         }
         // kick in Jacobi coordinates (src/transformations.c:147-176, src/integrator_whfast.c:447-472)
         {
-            const double Sx = lane_exclusive<NB>(m * ax, lane), Sy = lane_exclusive<NB>(m * ay, lane),
-                         Sz = lane_exclusive<NB>(m * az, lane);
+            double S[3] = {m * ax, m * ay, m * az};
+            lane_scan_multi<NB, 3, false>(S, lane);
+            const double ex = __shfl_up_sync(kFull, S[0], 1), ey = __shfl_up_sync(kFull, S[1], 1),
+                         ez = __shfl_up_sync(kFull, S[2], 1);
+            const double Sx = lane == 0 ? 0. : ex, Sy = lane == 0 ? 0. : ey, Sz = lane == 0 ? 0. : ez;
             if (jac) {
                 ux += h * (ax - Sx * ei); uy += h * (ay - Sy * ei); uz += h * (az - Sz * ei);
                 if (lane > 1) {
@@ -181,10 +216,9 @@ __device__ __forceinline__ int warp_steps(double* __restrict__ st, int cap, int 
         {
             const double Xc = __shfl_sync(kFull, qx, 0), Yc = __shfl_sync(kFull, qy, 0), Zc = __shfl_sync(kFull, qz, 0);
             const double Vx = __shfl_sync(kFull, ux, 0), Vy = __shfl_sync(kFull, uy, 0), Vz = __shfl_sync(kFull, uz, 0);
-            const double Wx = lane_suffix<NB>(wf * qx, lane), Wy = lane_suffix<NB>(wf * qy, lane),
-                         Wz = lane_suffix<NB>(wf * qz, lane);
-            const double Wvx = lane_suffix<NB>(wf * ux, lane), Wvy = lane_suffix<NB>(wf * uy, lane),
-                         Wvz = lane_suffix<NB>(wf * uz, lane);
+            double W[6] = {wf * qx, wf * qy, wf * qz, wf * ux, wf * uy, wf * uz};
+            lane_scan_multi<NB, 6, true>(W, lane);
+            const double Wx = W[0], Wy = W[1], Wz = W[2], Wvx = W[3], Wvy = W[4], Wvz = W[5];
             x = (jac ? qx : 0.) + Xc - Wx; y = (jac ? qy : 0.) + Yc - Wy; z = (jac ? qz : 0.) + Zc - Wz;
             vx = (jac ? ux : 0.) + Vx - Wvx; vy = (jac ? uy : 0.) + Vy - Wvy; vz = (jac ? uz : 0.) + Vz - Wvz;
         }
