@@ -6,7 +6,8 @@
 //     q_i = x_i - C_i,    x_i = q_i + X - sum_{k >= i} (m_k / eta_{k+1}) q_k,
 // the closed forms of the recurrences of src/transformations.c:34-81 and :178-226
 // (summed in tree order here, so results agree with the serial form to rounding).
-// Used by the serving loop's WHFast slots and by the ensemble's warp mapping.
+// Used by the serving loop's WHFast slots and by the ensemble's warp mapping, with
+// the division and square root of the including unit (WH_DIV / WH_SQRT).
 #pragma once
 #include "whfast_core.cuh"
 
@@ -169,8 +170,8 @@ __device__ __forceinline__ int warp_steps(double* __restrict__ st, int cap, int 
             const double dz = __shfl_sync(kFull, z, a) - __shfl_sync(kFull, z, b);
             double g = 0.;
             if (pj[r] < NB) {
-                const double rr = sqrt(dx * dx + dy * dy + dz * dz);
-                g = G / (rr * rr * rr);
+                const double rr = WH_SQRT(dx * dx + dy * dy + dz * dz);
+                g = WH_DIV(G, rr * rr * rr);
             }
             gx[r] = g * dx; gy[r] = g * dy; gz[r] = g * dz;
         }
@@ -203,8 +204,8 @@ __device__ __forceinline__ int warp_steps(double* __restrict__ st, int cap, int 
             if (jac) {
                 ux += h * (ax - Sx * ei); uy += h * (ay - Sy * ei); uz += h * (az - Sz * ei);
                 if (lane > 1) {
-                    const double rj2i = 1. / (qx * qx + qy * qy + qz * qz);
-                    const double pf = h * (sqrt(rj2i) * rj2i * G * eta_in);
+                    const double rj2i = WH_RCP(qx * qx + qy * qy + qz * qz);
+                    const double pf = h * (WH_SQRT(rj2i) * rj2i * G * eta_in);
                     ux += pf * qx; uy += pf * qy; uz += pf * qz;
                 }
             }
