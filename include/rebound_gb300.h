@@ -359,7 +359,7 @@ typedef struct rgpu_server_config {
     int32_t cluster_steps_per_tick;  /* default 8 */
     int32_t thread_per_system;       /* 0 (default): one warp per WHFast system, lanes = bodies
                                         (lowest latency); 1: one thread per system */
-    int64_t tick_ns;                 /* warp per system: > 0 (default 2,000,000, at most 1e9), each
+    int64_t tick_ns;                 /* warp per system: > 0 (default 8,000,000, at most 1e9), each
                                         slot steps for about this much device time per tick, so
                                         light systems are not held back by the heaviest one of the
                                         tick; 0: each slot takes exactly steps_per_launch steps per

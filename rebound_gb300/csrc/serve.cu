@@ -710,7 +710,7 @@ void rgpu_server_config_default(rgpu_server_config* c) {
     c->pool_particles = 1 << 22;
     c->steps_per_launch = 64;
     c->cluster_steps_per_tick = 8;
-    c->tick_ns = 2000000;
+    c->tick_ns = 8000000;
 }
 
 int rgpu_server_create(rgpu_server** out, const rgpu_server_config* cfg) {
