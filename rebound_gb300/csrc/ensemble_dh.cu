@@ -3,6 +3,7 @@
 // coordinates = DEMOCRATICHELIOCENTRIC), compiled with --fmad=false so that every
 // system follows the plain democratic heliocentric path bit for bit.
 #define ENSEMBLE_NS ens_dh
+#define WH_INT_DIVSQRT 1        // IEEE division and sqrt on the integer pipes (whfast_core.cuh)
 #define ENSEMBLE_STEP wh::step_safe_dh
 #include "ensemble_kernels.cuh"
 

@@ -4,8 +4,10 @@
 // the kernels DEFAULT, MODIFIEDKICK, COMPOSITION and LAZY
 // (src/integrator_whfast.c:653-785, 1113-1259; Wisdom, Holman & Touma 1996;
 // Wisdom 2006; Rein, Tamayo & Brown 2019).  The host lays each call out as a list
-// of operators in the reference's order; lane 0 of one warp runs the list and
-// the Kepler drifts take one body per lane.  Every operator has a single call
+// of operators in the reference's order; one warp runs the list.  The Kepler
+// drifts take one body per lane, the BASIC gravity one pair and then one body per
+// lane, and in Jacobi coordinates the transforms and the kick one quantity per
+// lane; the other operators run on lane 0.  Every operator has a single call
 // site in the interpreter loop, so the Kepler solver is inlined once per body
 // count however long the corrector is.  Every plain WHFast step and synchronize
 // runs here, the default configuration included.  Compiled with
@@ -280,55 +282,237 @@ __device__ void kick_helio(wh::Jacobi<NB>& h, const wh::System<NB>& s, const dou
 // BASIC gravity for any gravity_ignore_terms (src/gravity.c:180-257): pairs (i, jj)
 // with i from starti (1, or 2 to skip the 0-1 pair) and jj from startj (0, or 1
 // to skip body 0) below min(i, Ng); a_i always takes the pair's term, a_jj when i
-// is active or testparticle_type is 1.  One body per lane, bit for bit: in the
-// reference's serial loop a body's acceleration takes its terms in ascending
-// partner order (the partners below it while it is the outer index, then those
-// above it), so each lane forms its own body's sum in that order, recomputing
-// each pair's factor G / r^3 as the reference does.  One warp runs one simulation, so every
-// FP64 warp instruction holds the FP64 pipe for 64 clocks however many lanes
-// work: a row per lane takes N - 1 pair evaluations per warp instead of the
-// N (N - 1) / 2 of the serial loop on lane 0.
+// is active or testparticle_type is 1.  Bit for bit, over the lanes: the reference
+// forms each pair's displacement (from the higher index to the lower) and factor
+// G / r^3 once and adds -G m_jj / r^3 d to a_i and G m_i / r^3 d to a_jj, so in its
+// serial loop a body's acceleration takes its terms in ascending partner order
+// (the partners below it while it is the outer index, then those above it).  Here
+// lane l of round r forms pair p = 32 r + l (p = i (i - 1) / 2 + jj) into shared
+// memory, and then lane k adds body k's terms in ascending partner order.  One warp
+// runs one simulation, so every FP64 warp instruction holds the FP64 pipe for 64
+// clocks however many lanes work: N (N - 1) / 2 pairs take one round of square roots
+// and divisions up to N = 8.  The state and the accelerations are in shared memory;
+// the caller brackets the call with __syncwarp().
 template <int NB>
-struct GravShared {
-    double x[NB], y[NB], z[NB], m[NB], ax[NB], ay[NB], az[NB];
+struct PairTerms {
+    double dx[NB * (NB - 1) / 2], dy[NB * (NB - 1) / 2], dz[NB * (NB - 1) / 2], pf[NB * (NB - 1) / 2];
 };
 
 template <int NB>
-__device__ void gravity_basic_lanes(const wh::System<NB>& s, double ax[NB], double ay[NB], double az[NB],
-                                    GravShared<NB>& g, int lane, double G, double eps2, int N, int Ng, int tp,
-                                    int starti, int startj) {
-    if (lane == 0) {
+__device__ void gravity_basic_lanes(const wh::System<NB>& s, double* ax, double* ay, double* az, PairTerms<NB>& t,
+                                    int lane, double G, double eps2, int N, int Ng, int tp, int starti, int startj) {
+    const int npair = N * (N - 1) / 2;
 #pragma unroll 1
-        for (int i = 0; i < N; i++) { g.x[i] = s.x[i]; g.y[i] = s.y[i]; g.z[i] = s.z[i]; g.m[i] = s.m[i]; }
-    }
-    __syncwarp();
-    if (lane < N) {
-        const int k = lane;
-        const int st = Ng > starti ? Ng : starti;
-        double axk = 0., ayk = 0., azk = 0.;
-#pragma unroll 1
-        for (int q = 0; q < N; q++) {
-            if (q == k) continue;
-            const bool low = q < k;                  // pair (i = k, jj = q), else (i = q, jj = k)
-            const int i = low ? k : q, jj = low ? q : k;
-            const int jend = i < Ng ? i : Ng;
-            if (i < starti || jj < startj || jj >= jend) continue;
-            if (!low && !(i < st ? true : tp != 0)) continue;
-            const double dx = (0. + g.x[i]) - g.x[jj];
-            const double dy = (0. + g.y[i]) - g.y[jj];
-            const double dz = (0. + g.z[i]) - g.z[jj];
+    for (int p0 = 0; p0 < npair; p0 += 32) {
+        const int p = p0 + lane;
+        if (p < npair) {
+            int i = 1;
+            while ((i + 1) * i / 2 <= p) i++;
+            const int jj = p - i * (i - 1) / 2;
+            const double dx = (0. + s.x[i]) - s.x[jj];
+            const double dy = (0. + s.y[i]) - s.y[jj];
+            const double dz = (0. + s.z[i]) - s.z[jj];
             const double r = sqrt(dx * dx + dy * dy + dz * dz + eps2);
-            const double pf = G / (r * r * r);
-            const double c = low ? -pf * g.m[jj] : pf * g.m[i];
-            axk += c * dx; ayk += c * dy; azk += c * dz;
+            t.dx[p] = dx; t.dy[p] = dy; t.dz[p] = dz;
+            t.pf[p] = G / (r * r * r);
         }
-        g.ax[k] = axk; g.ay[k] = ayk; g.az[k] = azk;
     }
     __syncwarp();
-    if (lane == 0) {
+    if (lane >= N) return;
+    const int k = lane;
+    const int st = Ng > starti ? Ng : starti;
+    double axk = 0., ayk = 0., azk = 0.;
 #pragma unroll 1
-        for (int i = 0; i < N; i++) { ax[i] = g.ax[i]; ay[i] = g.ay[i]; az[i] = g.az[i]; }
+    for (int q = 0; q < N; q++) {
+        if (q == k) continue;
+        const bool low = q < k;                  // pair (i = k, jj = q), else (i = q, jj = k)
+        const int i = low ? k : q, jj = low ? q : k;
+        const int jend = i < Ng ? i : Ng;
+        if (i < starti || jj < startj || jj >= jend) continue;
+        if (!low && !(i < st ? true : tp != 0)) continue;
+        const int p = i * (i - 1) / 2 + jj;
+        const double pf = t.pf[p];
+        const double c = low ? -pf * s.m[jj] : pf * s.m[i];
+        axk += c * t.dx[p]; ayk += c * t.dy[p]; azk += c * t.dz[p];
     }
+    ax[k] = axk; ay[k] = ayk; az[k] = azk;
+}
+
+// --- Jacobi transforms and kick, one quantity per lane ------------------------------
+// The serial transforms carry six independent running sums (x, y, z, vx, vy, vz)
+// that share only mass scalars: the running interior mass eta, 1 / eta and the ratio of
+// successive etas.  Those form a chain of additions with a division at every link.  Here
+// lane i first forms link i's scalars (its eta by the serial chain's additions in the
+// same order, then one division that all links share as one warp instruction), and then
+// lane q forms quantity q's sum with the reference's operations in the reference's
+// order.  The results are bit-identical to the serial loops; one warp runs one
+// simulation, so each FP64 warp instruction costs the same however many lanes work, and
+// the six sums and the per-body divisions now share instructions.
+
+template <class T>
+__device__ __forceinline__ auto qrow(T& a, int q) -> decltype(&a.x[0]) {
+    return q == 0 ? a.x : q == 1 ? a.y : q == 2 ? a.z : q == 3 ? a.vx : q == 4 ? a.vy : a.vz;
+}
+
+// Mass scalars of one transform, written by the lanes that form them.
+template <int NB>
+struct ChainScalars {
+    double rcp[NB];      // forward: 1 / eta_(i-1); backward: 1 / eta before removing m_i
+    double next[NB];     // forward: eta_i / eta_(i-1); backward: eta after removing m_i
+    double total;        // forward: eta over the active bodies
+    double total_rcp;    // forward: 1 / total; backward: 1 / eta after removing them all
+    double top_rcp;      // backward: 1 / j.m[0] (test particles)
+};
+
+// Forward chain of src/transformations.c:34-81 and :147-176: eta_0 = m_0,
+// eta_i = eta_(i-1) + m_i for the active bodies 1 <= i < Na.  Lane i (1 <= i < Na)
+// forms 1 / eta_(i-1) and eta_i * (1 / eta_(i-1)); lane T = max(Na, 1) forms the total
+// and its reciprocal.  Every lane takes part in the division.  All lanes call it.
+template <int NB>
+__device__ void forward_scalars(const double* m, int Na, ChainScalars<NB>& c, int lane) {
+    const int T = Na > 1 ? Na : 1;
+    const int l = lane < 1 ? 1 : lane > T ? T : lane;
+    double e = m[0];
+#pragma unroll 1
+    for (int k = 1; k < l; k++) e += m[k];
+    const double r = 1. / e;
+    if (lane >= 1 && lane < Na) {
+        const double e2 = e + m[lane];
+        c.rcp[lane] = r;
+        c.next[lane] = e2 * r;
+    } else if (lane == T) {
+        c.total = e;
+        c.total_rcp = r;
+    }
+    __syncwarp();
+}
+
+// Backward chain of src/transformations.c:178-226: eta starts at j.m[0] and loses
+// m_i for i = Na - 1 down to 1.  Lane i (1 <= i < Na) forms 1 / eta before removing
+// m_i and eta after; lane 0 removes them all and forms the final reciprocal.  All
+// lanes call it.
+template <int NB>
+__device__ void backward_scalars(double top, const double* m, int Na, ChainScalars<NB>& c, int lane) {
+    const int l = lane < Na ? lane : 0;
+    double e = top;
+#pragma unroll 1
+    for (int k = Na - 1; k > l; k--) e -= m[k];
+    const double r = 1. / e;
+    if (lane >= 1 && lane < Na) {
+        c.rcp[lane] = r;
+        c.next[lane] = e - m[lane];
+    } else if (lane == 0) {
+        c.total_rcp = r;
+    }
+    __syncwarp();
+    // 1 / j.m[0]: lane Na - 1 divided it (nothing removed yet), or lane 0 when Na <= 1
+    if (lane == 0) c.top_rcp = Na >= 2 ? c.rcp[Na - 1] : c.total_rcp;
+    __syncwarp();
+}
+
+// reb_transformations_inertial_to_jacobi_posvel (src/transformations.c:34-81), as
+// wh::to_jacobi; lanes 0-5 form the sums, lane 0 also copies the masses.
+template <int NB>
+__device__ void to_jacobi_lanes(const wh::System<NB>& s, wh::Jacobi<NB>& j, ChainScalars<NB>& c, int N, int Na,
+                                int lane) {
+    forward_scalars(s.m, Na, c, lane);
+    if (lane >= 6) return;
+    const double* sq = qrow(s, lane);
+    double* jq = qrow(j, lane);
+    double acc = s.m[0] * sq[0];
+#pragma unroll
+    for (int i = 1; i < NB; i++) {
+        if (i >= Na) break;
+        const double v = sq[i] - acc * c.rcp[i];
+        jq[i] = v;
+        acc = acc * c.next[i] + s.m[i] * v;
+        if (lane == 0) j.m[i] = s.m[i];
+    }
+    const double ei = c.total_rcp;
+#pragma unroll
+    for (int i = 1; i < NB; i++) {
+        if (i < Na || i >= N) continue;
+        jq[i] = sq[i] - acc * ei;
+        if (lane == 0) j.m[i] = s.m[i];
+    }
+    jq[0] = acc * ei;
+    if (lane == 0) j.m[0] = c.total;
+}
+
+// reb_transformations_jacobi_to_inertial_posvel (src/transformations.c:178-226), as
+// wh::to_inertial; lanes 0-5 form the sums (the masses are not written).
+template <int NB>
+__device__ void to_inertial_lanes(wh::System<NB>& s, const wh::Jacobi<NB>& j, ChainScalars<NB>& c, int N, int Na,
+                                  int lane) {
+    backward_scalars(j.m[0], s.m, Na, c, lane);
+    if (lane >= 6) return;
+    const double* jq = qrow(j, lane);
+    double* sq = qrow(s, lane);
+    double acc = jq[0] * j.m[0];
+    const double tpi = c.top_rcp;
+#pragma unroll
+    for (int i = NB - 1; i >= 1; i--) {
+        if (i >= N || i < Na) continue;
+        sq[i] = jq[i] + acc * tpi;
+    }
+#pragma unroll
+    for (int i = NB - 1; i >= 1; i--) {
+        if (i >= Na) continue;
+        acc = (acc - s.m[i] * jq[i]) * c.rcp[i];
+        sq[i] = jq[i] + acc;
+        acc *= c.next[i];
+    }
+    sq[0] = acc * c.total_rcp;
+}
+
+// Interaction (kick) step in Jacobi coordinates, as wh::interaction_step:
+// inertial_to_jacobi_acc (src/transformations.c:147-176) and the velocity kick on
+// lanes 0-2 (one component each), then the Jacobi term (src/integrator_whfast.c:
+// 447-472) on lane i for body i >= 2, after the kick as in the serial loop.  Lane i
+// rebuilds its interior mass with the serial loop's additions in the same order.
+// All lanes call it; the caller brackets the call with __syncwarp().
+template <int NB>
+__device__ void kick_jacobi_lanes(wh::Jacobi<NB>& j, const wh::System<NB>& s, const double* const acc[3],
+                                  ChainScalars<NB>& c, double G, double dt, int N, int Na, bool jacobi_term,
+                                  int lane) {
+    forward_scalars(s.m, Na, c, lane);
+    if (lane < 3) {
+        const double* a = acc[lane];
+        double* v = lane == 0 ? j.vx : lane == 1 ? j.vy : j.vz;
+        double ja[NB];
+        double sc = s.m[0] * a[0];
+#pragma unroll
+        for (int i = 1; i < NB; i++) {
+            if (i >= Na) break;
+            ja[i] = a[i] - sc * c.rcp[i];
+            sc = sc * c.next[i] + s.m[i] * ja[i];
+        }
+#pragma unroll
+        for (int i = 1; i < NB; i++) {
+            if (i < Na || i >= N) continue;
+            ja[i] = a[i] - sc * c.total_rcp;
+        }
+#pragma unroll
+        for (int i = 1; i < NB; i++) {
+            if (i >= N) break;
+            v[i] += dt * ja[i];
+        }
+    }
+    __syncwarp();
+    if (!jacobi_term || lane < 2 || lane >= N) return;
+    const int i = lane;
+    double eta = s.m[0];
+#pragma unroll 1
+    for (int k = 1; k <= i; k++)
+        if (k < Na) eta += j.m[k];
+    const double qx = j.x[i], qy = j.y[i], qz = j.z[i];
+    const double rj2i = WH_RCP(qx * qx + qy * qy + qz * qz);
+    const double rji = WH_SQRT(rj2i);
+    const double rj3iM = rji * rj2i * G * eta;
+    const double pf = dt * rj3iM;
+    j.vx[i] += pf * qx;
+    j.vy[i] += pf * qy;
+    j.vz[i] += pf * qz;
 }
 
 // Compensated (Kahan) accumulation of one force term (src/gravity.c:431-446).
@@ -374,13 +558,19 @@ __global__ void __launch_bounds__(32) whfast_program(ParticlesSoA p, double* jac
                                                      int tp, int coords, double G, double eps2,
                                                      const __grid_constant__ Program prog, uint32_t* status) {
     // Lane 0 interprets the program; every lane takes part in the drifts (one body
-    // each).  The coordinates live in shared memory so that all lanes see them.
+    // each), the BASIC gravity (one body each) and, in Jacobi coordinates, the
+    // transforms and the kick.  The state lives in shared memory so that all lanes
+    // see it.
     __shared__ wh::Jacobi<NB> j;
-    __shared__ GravShared<NB> gsh;
+    __shared__ wh::System<NB> s;
+    __shared__ double acc[3][NB];
+    __shared__ ChainScalars<NB> chain;
+    __shared__ PairTerms<NB> pairs;
     __shared__ int stop;
     const int lane = threadIdx.x;
-    wh::System<NB> s;
-    double ax[NB], ay[NB], az[NB];
+    double* const ax = acc[0];
+    double* const ay = acc[1];
+    double* const az = acc[2];
     if (lane == 0) {
         stop = 0;
         load_sys(s, p, N);
@@ -406,22 +596,33 @@ __global__ void __launch_bounds__(32) whfast_program(ParticlesSoA p, double* jac
             continue;
         }
         if (op == kOpGravity) {
-            gravity_basic_lanes(s, ax, ay, az, gsh, lane, G, eps2, N, Ng, tp, starti, startj);
+            gravity_basic_lanes(s, ax, ay, az, pairs, lane, G, eps2, N, Ng, tp, starti, startj);
+            __syncwarp();
+            continue;
+        }
+        if (coords == 0 && (op == kOpFromInertial || op == kOpToInertial || op == kOpKick ||
+                            op == kOpKickNoJacobiTerm)) {
+            if (op == kOpFromInertial) {
+                to_jacobi_lanes(s, j, chain, N, Na, lane);
+            } else if (op == kOpToInertial) {
+                to_inertial_lanes(s, j, chain, N, Na, lane);
+            } else {
+                const double* const a3[3] = {ax, ay, az};
+                kick_jacobi_lanes(j, s, a3, chain, G, d, N, Na, op == kOpKick, lane);
+            }
             __syncwarp();
             continue;
         }
         if (lane == 0) {
             switch (op) {
                 case kOpFromInertial:
-                    if (coords == 0) wh::to_jacobi(s, j, N, Na);
-                    else if (coords == 1) wh::to_dh(s, j, N, Na);
+                    if (coords == 1) wh::to_dh(s, j, N, Na);
                     else if (coords == 2) to_whds(s, j, N, Na);
                     else to_bary(s, j, N, Na);
                     break;
                 case kOpCom: wh::com_step(j, d); break;
                 case kOpToInertial:
-                    if (coords == 0) wh::to_inertial(s, j, N, Na);
-                    else if (coords == 1) wh::dh_to_inertial(s, j, N, Na);
+                    if (coords == 1) wh::dh_to_inertial(s, j, N, Na);
                     else if (coords == 2) whds_to_inertial(s, j, N, Na);
                     else bary_to_inertial(s, j, N, Na);
                     break;
@@ -434,10 +635,7 @@ __global__ void __launch_bounds__(32) whfast_program(ParticlesSoA p, double* jac
                     for (int i = 0; i < N; i++) { ax[i] = 0.; ay[i] = 0.; az[i] = 0.; }
                     break;
                 case kOpKick:
-                case kOpKickNoJacobiTerm:
-                    if (coords == 0) wh::interaction_step(j, s, ax, ay, az, G, d, N, Na, op == kOpKick);
-                    else kick_helio(j, s, ax, ay, az, G, d, N, Na, coords);
-                    break;
+                case kOpKickNoJacobiTerm: kick_helio(j, s, ax, ay, az, G, d, N, Na, coords); break;
                 case kOpJump: jump(j, s, d, N, Na, coords); break;
                 case kOpJerk: add_jerk(s, ax, ay, az, G, d, N); break;
                 case kOpLazyShift:
