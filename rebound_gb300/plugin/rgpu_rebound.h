@@ -37,7 +37,7 @@
  *
  * Speed: the GPU pays off for direct sums and trees of thousands of particles
  * and more.  The plain WHFast path runs one small system per call on one warp,
- * about 59 µs per step for 5 bodies against about 2.5 µs for REBOUND's WHFast
+ * about 37 µs per step for 5 bodies against about 2.5 µs for REBOUND's WHFast
  * on one CPU core; many systems belong in the batched ensemble
  * (rgpu_ensemble_*) or the request loop (rgpu_server_*).
  *
