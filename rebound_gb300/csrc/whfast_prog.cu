@@ -114,91 +114,188 @@ __device__ void add_jerk(const wh::System<NB>& s, double ax[NB], double ay[NB], 
 // --- coordinate systems other than Jacobi (src/transformations.c:295-644) ---------
 // coords: 0 Jacobi, 1 democratic heliocentric, 2 WHDS (Hernandez & Dehnen 2017),
 // 3 barycentric; the values of REB_INTEGRATOR_WHFAST_COORDINATES.
+// Each transform, jump and kick below is the reference's serial loop split over the
+// lanes, by quantity (x, y, z, vx, vy, vz: independent running sums) or by body
+// (independent per-body updates), every sum kept in the reference's order, so the
+// results are bit-identical.  One warp runs one simulation and each FP64 warp
+// instruction holds the FP64 pipe for about 64 clocks however many lanes are active,
+// so the split divides the instruction count.  All lanes call these functions (some
+// hold a __syncwarp()); the caller brackets each call with __syncwarp().
 
-// reb_transformations_inertial_to_whds_posvel (:295-345): democratic heliocentric
-// positions and centre of mass, velocities of active bodies scaled by (m_0+m_i)/m_0.
+template <class T>
+__device__ __forceinline__ auto qrow(T& a, int q) -> decltype(&a.x[0]) {
+    return q == 0 ? a.x : q == 1 ? a.y : q == 2 ? a.z : q == 3 ? a.vx : q == 4 ? a.vy : a.vz;
+}
+
+// reb_transformations_inertial_to_democraticheliocentric_posvel (:388-425), as
+// wh::to_dh: lanes 0-5 one quantity each (every lane forms the same mass sum), lane 0
+// also the masses.
 template <int NB>
-__device__ void to_whds(const wh::System<NB>& s, wh::Jacobi<NB>& h, int N, int Na) {
-    wh::to_dh(s, h, N, Na);
-    const double m0 = s.m[0];
-#pragma unroll 1
-    for (int i = 1; i < Na; i++) {
-        const double mf = (m0 + s.m[i]) / m0;
-        h.vx[i] = mf * (s.vx[i] - h.vx[0]); h.vy[i] = mf * (s.vy[i] - h.vy[0]); h.vz[i] = mf * (s.vz[i] - h.vz[0]);
+__device__ void to_dh_lanes(const wh::System<NB>& s, wh::Jacobi<NB>& h, int N, int Na, int lane) {
+    if (lane >= 6) return;
+    const double* sq = qrow(s, lane);
+    double* hq = qrow(h, lane);
+    double sum = 0., m0 = 0.;
+#pragma unroll
+    for (int i = 0; i < NB; i++) {
+        if (i >= Na) break;
+        const double m = s.m[i];
+        sum += sq[i] * m;
+        m0 += m;
+    }
+    const double c = sum / m0;
+    hq[0] = c;
+    // positions relative to the star, velocities relative to the centre of mass
+    const double base = lane < 3 ? sq[0] : c;
+#pragma unroll
+    for (int i = 1; i < NB; i++) {
+        if (i >= N) break;
+        hq[i] = sq[i] - base;
+        if (lane == 0) h.m[i] = s.m[i];
+    }
+    if (lane == 0) h.m[0] = m0;
+}
+
+// reb_transformations_democraticheliocentric_to_inertial_posvel (:427-473), as
+// wh::dh_to_inertial: lanes 0-2 the positions (lane 0 also copies the masses), lanes
+// 3-5 the velocities, which read the masses from h (the values lane 0 copies).
+template <int NB>
+__device__ void dh_to_inertial_lanes(wh::System<NB>& s, const wh::Jacobi<NB>& h, int N, int Na, int lane) {
+    if (lane >= 6) return;
+    const double* hq = qrow(h, lane);
+    double* sq = qrow(s, lane);
+    if (lane < 3) {
+        const double mtot = h.m[0];
+        double c = 0.;
+#pragma unroll
+        for (int i = 1; i < NB; i++) {
+            if (i >= Na) break;
+            const double m = h.m[i];
+            c += hq[i] * m / mtot;
+            if (lane == 0) s.m[i] = m;
+        }
+        const double s0 = hq[0] - c;
+        sq[0] = s0;
+#pragma unroll
+        for (int i = 1; i < NB; i++) {
+            if (i >= N) break;
+            sq[i] = hq[i] + s0;
+        }
+    } else {
+        const double m0 = s.m[0];
+#pragma unroll
+        for (int i = 1; i < NB; i++) {
+            if (i >= N) break;
+            sq[i] = hq[i] + hq[0];
+        }
+        double c = 0.;
+#pragma unroll
+        for (int i = 1; i < NB; i++) {
+            if (i >= Na) break;
+            const double m = h.m[i];
+            c += hq[i] * m / m0;
+        }
+        sq[0] = hq[0] - c;
     }
 }
 
-// reb_transformations_whds_to_inertial_posvel (:347-381).
+// reb_transformations_inertial_to_whds_posvel (:295-345): democratic heliocentric
+// positions and centre of mass, then lane i scales active body i's velocity by
+// (m_0 + m_i) / m_0.
 template <int NB>
-__device__ void whds_to_inertial(wh::System<NB>& s, const wh::Jacobi<NB>& h, int N, int Na) {
-    wh::dh_to_inertial(s, h, N, Na);          // positions and masses as democratic heliocentric
+__device__ void to_whds_lanes(const wh::System<NB>& s, wh::Jacobi<NB>& h, int N, int Na, int lane) {
+    to_dh_lanes(s, h, N, Na, lane);
+    __syncwarp();
+    const int i = lane;
+    if (i < 1 || i >= Na) return;
     const double m0 = s.m[0];
-#pragma unroll 1
-    for (int i = 1; i < Na; i++) {
+    const double mf = (m0 + s.m[i]) / m0;
+    h.vx[i] = mf * (s.vx[i] - h.vx[0]); h.vy[i] = mf * (s.vy[i] - h.vy[0]); h.vz[i] = mf * (s.vz[i] - h.vz[0]);
+}
+
+// reb_transformations_whds_to_inertial_posvel (:347-381): positions and masses as
+// democratic heliocentric, then lane i rescales active body i's velocity and lanes 0-2
+// form the star's velocity, one component each.
+template <int NB>
+__device__ void whds_to_inertial_lanes(wh::System<NB>& s, const wh::Jacobi<NB>& h, int N, int Na, int lane) {
+    dh_to_inertial_lanes(s, h, N, Na, lane);
+    __syncwarp();
+    const double m0 = s.m[0];
+    if (lane >= 1 && lane < Na) {
+        const int i = lane;
         const double mf = (m0 + s.m[i]) / m0;
         s.vx[i] = h.vx[i] / mf + h.vx[0]; s.vy[i] = h.vy[i] / mf + h.vy[0]; s.vz[i] = h.vz[i] / mf + h.vz[0];
     }
-    double vx0 = 0., vy0 = 0., vz0 = 0.;
-#pragma unroll 1
-    for (int i = 1; i < Na; i++) {
-        const double m = s.m[i];
-        vx0 += h.vx[i] * m / (m0 + m); vy0 += h.vy[i] * m / (m0 + m); vz0 += h.vz[i] * m / (m0 + m);
+    if (lane < 3) {
+        const double* hv = qrow(h, 3 + lane);
+        double v0 = 0.;
+#pragma unroll
+        for (int i = 1; i < NB; i++) {
+            if (i >= Na) break;
+            const double m = s.m[i];
+            v0 += hv[i] * m / (m0 + m);
+        }
+        qrow(s, 3 + lane)[0] = hv[0] - v0;
     }
-    s.vx[0] = h.vx[0] - vx0; s.vy[0] = h.vy[0] - vy0; s.vz[0] = h.vz[0] - vz0;
 }
 
-// reb_transformations_inertial_to_barycentric_posvel (:595-644).
+// reb_transformations_inertial_to_barycentric_posvel (:595-644): lanes 0-5 one
+// quantity each (every lane forms the same mass sum), lane 0 also the masses.
 template <int NB>
-__device__ void to_bary(const wh::System<NB>& s, wh::Jacobi<NB>& b, int N, int Na) {
+__device__ void to_bary_lanes(const wh::System<NB>& s, wh::Jacobi<NB>& b, int N, int Na, int lane) {
+    if (lane >= 6) return;
+    const double* sq = qrow(s, lane);
+    double* bq = qrow(b, lane);
     const double m0 = s.m[0];
-    double x = m0 * s.x[0], y = m0 * s.y[0], z = m0 * s.z[0];
-    double vx = m0 * s.vx[0], vy = m0 * s.vy[0], vz = m0 * s.vz[0], M = m0;
-    double sx = 0., sy = 0., sz = 0., svx = 0., svy = 0., svz = 0., sm = 0.;
-#pragma unroll 1
-    for (int i = 1; i < Na; i++) {
+    double t = m0 * sq[0], M = m0, sum = 0., sm = 0.;
+#pragma unroll
+    for (int i = 1; i < NB; i++) {
+        if (i >= Na) break;
         const double m = s.m[i];
-        sx += s.x[i] * m; sy += s.y[i] * m; sz += s.z[i] * m;
-        svx += s.vx[i] * m; svy += s.vy[i] * m; svz += s.vz[i] * m;
+        sum += sq[i] * m;
         sm += m;
     }
-    x += sx; y += sy; z += sz; vx += svx; vy += svy; vz += svz; M += sm;
+    t += sum;
+    M += sm;
     const double mi = 1.0 / M;
-    b.x[0] = x * mi; b.y[0] = y * mi; b.z[0] = z * mi;
-    b.vx[0] = vx * mi; b.vy[0] = vy * mi; b.vz[0] = vz * mi;
-    b.m[0] = M;
-#pragma unroll 1
-    for (int i = 1; i < N; i++) {
-        b.m[i] = s.m[i];
-        b.x[i] = s.x[i] - b.x[0]; b.y[i] = s.y[i] - b.y[0]; b.z[i] = s.z[i] - b.z[0];
-        b.vx[i] = s.vx[i] - b.vx[0]; b.vy[i] = s.vy[i] - b.vy[0]; b.vz[i] = s.vz[i] - b.vz[0];
+    const double c = t * mi;
+    bq[0] = c;
+    if (lane == 0) b.m[0] = M;
+#pragma unroll
+    for (int i = 1; i < NB; i++) {
+        if (i >= N) break;
+        if (lane == 0) b.m[i] = s.m[i];
+        bq[i] = sq[i] - c;
     }
 }
 
 // reb_transformations_barycentric_to_inertial_posvel (:544-593); it also rebuilds
-// the star's mass as the total minus the active bodies'.
+// the star's mass as the total minus the active bodies'.  Lanes 0-5 one quantity
+// each (every lane forms the same mass sum), lane 0 also the masses.
 template <int NB>
-__device__ void bary_to_inertial(wh::System<NB>& s, const wh::Jacobi<NB>& b, int N, int Na) {
+__device__ void bary_to_inertial_lanes(wh::System<NB>& s, const wh::Jacobi<NB>& b, int N, int Na, int lane) {
+    if (lane >= 6) return;
+    const double* bq = qrow(b, lane);
+    double* sq = qrow(s, lane);
     const double M = b.m[0];
-    double x0 = M * b.x[0], y0 = M * b.y[0], z0 = M * b.z[0];
-    double vx0 = M * b.vx[0], vy0 = M * b.vy[0], vz0 = M * b.vz[0], m0 = M;
-    double sx = 0., sy = 0., sz = 0., svx = 0., svy = 0., svz = 0., sm = 0.;
-#pragma unroll 1
-    for (int i = 1; i < N; i++) {
-        s.x[i] = b.x[i] + b.x[0]; s.y[i] = b.y[i] + b.y[0]; s.z[i] = b.z[i] + b.z[0];
-        s.vx[i] = b.vx[i] + b.vx[0]; s.vy[i] = b.vy[i] + b.vy[0]; s.vz[i] = b.vz[i] + b.vz[0];
+    double t0 = M * bq[0], m0 = M, sum = 0., sm = 0.;
+#pragma unroll
+    for (int i = 1; i < NB; i++) {
+        if (i >= N) break;
+        const double v = bq[i] + bq[0];
+        sq[i] = v;
         if (i < Na) {
             const double m = b.m[i];
-            s.m[i] = m;
-            sx += s.x[i] * m; sy += s.y[i] * m; sz += s.z[i] * m;
-            svx += s.vx[i] * m; svy += s.vy[i] * m; svz += s.vz[i] * m;
+            if (lane == 0) s.m[i] = m;
+            sum += v * m;
             sm += m;
         }
     }
-    x0 -= sx; y0 -= sy; z0 -= sz; vx0 -= svx; vy0 -= svy; vz0 -= svz; m0 -= sm;
+    t0 -= sum;
+    m0 -= sm;
     const double m0i = 1. / m0;
-    s.m[0] = m0;
-    s.x[0] = x0 * m0i; s.y[0] = y0 * m0i; s.z[0] = z0 * m0i;
-    s.vx[0] = vx0 * m0i; s.vy[0] = vy0 * m0i; s.vz[0] = vz0 * m0i;
+    if (lane == 0) s.m[0] = m0;
+    sq[0] = t0 * m0i;
 }
 
 // reb_integrator_whfast_kepler_step (src/integrator_whfast.c:589-636), one body
@@ -231,51 +328,59 @@ __device__ void drift_lane(wh::Jacobi<NB>& j, double m0, double G, double dt, in
 }
 
 // reb_integrator_whfast_jump_step (:526-584); nothing in Jacobi or barycentric.
+// Lanes 0-2, one component each.
 template <int NB>
-__device__ void jump(wh::Jacobi<NB>& h, const wh::System<NB>& s, double dt, int N, int Na, int coords) {
-    if (coords == 1) { wh::jump_step_dh(h, s, dt, N, Na); return; }
-    if (coords != 2) return;
+__device__ void jump_lanes(wh::Jacobi<NB>& h, const wh::System<NB>& s, double dt, int N, int Na, int coords,
+                           int lane) {
+    if ((coords != 1 && coords != 2) || lane >= 3) return;
+    const double* v = qrow(h, 3 + lane);
+    double* x = qrow(h, lane);
     const double m0 = s.m[0];
-    double px = 0., py = 0., pz = 0.;
+    double p = 0.;
+    if (coords == 1) {
+#pragma unroll 1
+        for (int i = 1; i < Na; i++) p += s.m[i] * v[i];
+#pragma unroll 1
+        for (int i = 1; i < N; i++) x[i] += dt * (p / m0);
+        return;
+    }
 #pragma unroll 1
     for (int i = 1; i < Na; i++) {
         const double m = s.m[i];
-        px += m * h.vx[i] / (m0 + m); py += m * h.vy[i] / (m0 + m); pz += m * h.vz[i] / (m0 + m);
+        p += m * v[i] / (m0 + m);
     }
 #pragma unroll 1
     for (int i = 1; i < N; i++) {
         if (i < Na) {
             const double m = s.m[i];
-            h.x[i] += dt * (px - (m * h.vx[i] / (m0 + m)));
-            h.y[i] += dt * (py - (m * h.vy[i] / (m0 + m)));
-            h.z[i] += dt * (pz - (m * h.vz[i] / (m0 + m)));
+            x[i] += dt * (p - (m * v[i] / (m0 + m)));
         } else {
-            h.x[i] += dt * px; h.y[i] += dt * py; h.z[i] += dt * pz;
+            x[i] += dt * p;
         }
     }
 }
 
-// reb_integrator_whfast_interaction_step (:431-524) outside Jacobi coordinates.
+// reb_integrator_whfast_interaction_step (:431-524) outside Jacobi coordinates: lane i
+// kicks body i.
 template <int NB>
-__device__ void kick_helio(wh::Jacobi<NB>& h, const wh::System<NB>& s, const double ax[NB], const double ay[NB],
-                           const double az[NB], double G, double dt, int N, int Na, int coords) {
+__device__ void kick_helio_lanes(wh::Jacobi<NB>& h, const wh::System<NB>& s, const double* ax, const double* ay,
+                                 const double* az, double G, double dt, int N, int Na, int coords, int lane) {
+    const int i = lane;
+    if (i < 1 || i >= N) return;
     const double m0 = s.m[0];
-#pragma unroll 1
-    for (int i = 1; i < N; i++) {
-        if (coords == 2 && i < Na) {
-            const double mi = s.m[i];
-            h.vx[i] += dt * (m0 + mi) * ax[i] / m0;
-            h.vy[i] += dt * (m0 + mi) * ay[i] / m0;
-            h.vz[i] += dt * (m0 + mi) * az[i] / m0;
-        } else if (coords == 3) {
-            const double dr = sqrt(h.x[i] * h.x[i] + h.y[i] * h.y[i] + h.z[i] * h.z[i]);
-            const double pf = G * h.m[0] / (dr * dr * dr);
-            h.vx[i] += dt * (pf * h.x[i] + ax[i]);
-            h.vy[i] += dt * (pf * h.y[i] + ay[i]);
-            h.vz[i] += dt * (pf * h.z[i] + az[i]);
-        } else {
-            h.vx[i] += dt * ax[i]; h.vy[i] += dt * ay[i]; h.vz[i] += dt * az[i];
-        }
+    if (coords == 2 && i < Na) {
+        const double mi = s.m[i];
+        h.vx[i] += dt * (m0 + mi) * ax[i] / m0;
+        h.vy[i] += dt * (m0 + mi) * ay[i] / m0;
+        h.vz[i] += dt * (m0 + mi) * az[i] / m0;
+    } else if (coords == 3) {
+        const double dr = sqrt(h.x[i] * h.x[i] + h.y[i] * h.y[i] + h.z[i] * h.z[i]);
+        const double pf = G * h.m[0] / (dr * dr * dr);
+        h.vx[i] += dt * (pf * h.x[i] + ax[i]);
+        h.vy[i] += dt * (pf * h.y[i] + ay[i]);
+        h.vz[i] += dt * (pf * h.z[i] + az[i]);
+    } else {
+        h.vx[i] += dt * ax[i]; h.vy[i] += dt * ay[i]; h.vz[i] += dt * az[i];
     }
 }
 
@@ -348,11 +453,6 @@ __device__ void gravity_basic_lanes(const wh::System<NB>& s, double* ax, double*
 // order.  The results are bit-identical to the serial loops; one warp runs one
 // simulation, so each FP64 warp instruction costs the same however many lanes work, and
 // the six sums and the per-body divisions now share instructions.
-
-template <class T>
-__device__ __forceinline__ auto qrow(T& a, int q) -> decltype(&a.x[0]) {
-    return q == 0 ? a.x : q == 1 ? a.y : q == 2 ? a.z : q == 3 ? a.vx : q == 4 ? a.vy : a.vz;
-}
 
 // Mass scalars of one transform, written by the lanes that form them.
 template <int NB>
@@ -600,32 +700,32 @@ __global__ void __launch_bounds__(32) whfast_program(ParticlesSoA p, double* jac
             __syncwarp();
             continue;
         }
-        if (coords == 0 && (op == kOpFromInertial || op == kOpToInertial || op == kOpKick ||
-                            op == kOpKickNoJacobiTerm)) {
+        if (op == kOpFromInertial || op == kOpToInertial || op == kOpKick || op == kOpKickNoJacobiTerm ||
+            op == kOpJump) {
             if (op == kOpFromInertial) {
-                to_jacobi_lanes(s, j, chain, N, Na, lane);
+                if (coords == 0) to_jacobi_lanes(s, j, chain, N, Na, lane);
+                else if (coords == 1) to_dh_lanes(s, j, N, Na, lane);
+                else if (coords == 2) to_whds_lanes(s, j, N, Na, lane);
+                else to_bary_lanes(s, j, N, Na, lane);
             } else if (op == kOpToInertial) {
-                to_inertial_lanes(s, j, chain, N, Na, lane);
-            } else {
+                if (coords == 0) to_inertial_lanes(s, j, chain, N, Na, lane);
+                else if (coords == 1) dh_to_inertial_lanes(s, j, N, Na, lane);
+                else if (coords == 2) whds_to_inertial_lanes(s, j, N, Na, lane);
+                else bary_to_inertial_lanes(s, j, N, Na, lane);
+            } else if (op == kOpJump) {
+                jump_lanes(j, s, d, N, Na, coords, lane);
+            } else if (coords == 0) {
                 const double* const a3[3] = {ax, ay, az};
                 kick_jacobi_lanes(j, s, a3, chain, G, d, N, Na, op == kOpKick, lane);
+            } else {
+                kick_helio_lanes(j, s, ax, ay, az, G, d, N, Na, coords, lane);
             }
             __syncwarp();
             continue;
         }
         if (lane == 0) {
             switch (op) {
-                case kOpFromInertial:
-                    if (coords == 1) wh::to_dh(s, j, N, Na);
-                    else if (coords == 2) to_whds(s, j, N, Na);
-                    else to_bary(s, j, N, Na);
-                    break;
                 case kOpCom: wh::com_step(j, d); break;
-                case kOpToInertial:
-                    if (coords == 1) wh::dh_to_inertial(s, j, N, Na);
-                    else if (coords == 2) whds_to_inertial(s, j, N, Na);
-                    else bary_to_inertial(s, j, N, Na);
-                    break;
                 case kOpGravityJacobi: gravity_jacobi(s, ax, ay, az, G, N); break;
                 case kOpGravityCompensated:
                     gravity_compensated(s, ax, ay, az, G, eps2, N, Ng, tp, coords == 0 ? 1 : coords == 3 ? 0 : 2);
@@ -634,9 +734,6 @@ __global__ void __launch_bounds__(32) whfast_program(ParticlesSoA p, double* jac
 #pragma unroll 1
                     for (int i = 0; i < N; i++) { ax[i] = 0.; ay[i] = 0.; az[i] = 0.; }
                     break;
-                case kOpKick:
-                case kOpKickNoJacobiTerm: kick_helio(j, s, ax, ay, az, G, d, N, Na, coords); break;
-                case kOpJump: jump(j, s, d, N, Na, coords); break;
                 case kOpJerk: add_jerk(s, ax, ay, az, G, d, N); break;
                 case kOpLazyShift:
 #pragma unroll 1
