@@ -657,10 +657,10 @@ template <int NB>
 __global__ void __launch_bounds__(32) whfast_program(ParticlesSoA p, double* jac, size_t cap, int N, int Na, int Ng,
                                                      int tp, int coords, double G, double eps2,
                                                      const __grid_constant__ Program prog, uint32_t* status) {
-    // Lane 0 interprets the program; every lane takes part in the drifts (one body
-    // each), the BASIC gravity (one body each) and, in Jacobi coordinates, the
-    // transforms and the kick.  The state lives in shared memory so that all lanes
-    // see it.
+    // Every lane walks the program; the drifts (one body each), the BASIC gravity
+    // (one pair, then one body each), the coordinate transforms, jumps and kicks
+    // (one quantity or one body each) run on the lanes, the other operators on
+    // lane 0.  The state lives in shared memory so that all lanes see it.
     __shared__ wh::Jacobi<NB> j;
     __shared__ wh::System<NB> s;
     __shared__ double acc[3][NB];
