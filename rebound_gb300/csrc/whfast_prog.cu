@@ -5,9 +5,9 @@
 // (src/integrator_whfast.c:653-785, 1113-1259; Wisdom, Holman & Touma 1996;
 // Wisdom 2006; Rein, Tamayo & Brown 2019).  The host lays each call out as a list
 // of operators in the reference's order; one warp runs the list.  The Kepler
-// drifts take one body per lane, the BASIC gravity one pair and then one body per
-// lane, and in Jacobi coordinates the transforms and the kick one quantity per
-// lane; the other operators run on lane 0.  Every operator has a single call
+// drifts take one body per lane, the forces one pair and then one body per lane,
+// and the coordinate transforms, jumps and kicks one quantity or one body per
+// lane; the rest runs on lane 0.  Every operator has a single call
 // site in the interpreter loop, so the Kepler solver is inlined once per body
 // count however long the corrector is.  Every plain WHFast step and synchronize
 // runs here, the default configuration included.  Compiled with
@@ -18,97 +18,189 @@ namespace {
 
 using namespace wh_plain;
 
+// --- forces over the lanes -------------------------------------------------------
+// The reference's serial force loops visit the pairs (i, j) in a fixed order and
+// add each pair's terms to both bodies.  In every loop below, a body's sum takes its
+// terms in ascending partner order, so the same sums can be formed one body per lane:
+// first each pair's displacement and factors are formed once, one pair per lane
+// (pair p = hi (hi - 1) / 2 + lo for lo < hi), and each lane then adds its body's
+// terms in the reference's order.  Per-body quantities that the serial loop builds
+// from running sums (the Jacobi vectors) are formed one body per lane, each lane
+// repeating the running sums' additions in the same order.  Every result is
+// bit-identical to the serial loop.  One warp runs one simulation, and each FP64 warp
+// instruction holds the FP64 pipe for about 64 clocks however few lanes are active, so
+// the split divides the step's FP64 instruction count.  All lanes call these
+// functions; the caller brackets each call with __syncwarp().  The JACOBI force, the
+// jerk and the COMPENSATED force (kernels MODIFIEDKICK and LAZY, gravity
+// COMPENSATED) are compiled out of line, apart from the default step's code.
+
+template <int NB>
+struct PairTerms {
+    static constexpr int kPairs = NB * (NB - 1) / 2;
+    double dx[kPairs], dy[kPairs], dz[kPairs], pf[kPairs];   // displacement, G / r^3
+    double ex[kPairs], ey[kPairs], ez[kPairs], pf1[kPairs];  // jerk: acceleration difference, 3 alpha G / r^5
+};
+
+template <int NB>
+struct BodyTerms {
+    double qx[NB], qy[NB], qz[NB];            // Jacobi vector of body j
+    double ex[NB], ey[NB], ez[NB];            // its acceleration relative to the interior centre of mass
+    double fm[NB], fM[NB], f1m[NB], f1M[NB];  // factors with dQ = -m_j and dQ = M
+};
+
+// Pair p's indices (lo < hi).
+__device__ __forceinline__ void pair_of(int p, int& hi, int& lo) {
+    hi = 1;
+    while ((hi + 1) * hi / 2 <= p) hi++;
+    lo = p - hi * (hi - 1) / 2;
+}
+
 // reb_gravity_jacobi_calculate_acceleration (src/gravity.c:108-162): direct terms
 // plus the Jacobi terms of the Jacobi Hamiltonian's interaction part; no
-// softening, every body treated as active.  Rolled loops: the operator is off
-// the hot path and keeps the program kernel small.
+// softening, every body treated as active.  Body k takes, in the serial loop's
+// order: the pair terms of the partners below it and its own Jacobi term (outer
+// index j = k), then for each j > k the Jacobi term of j and the pair term.
 template <int NB>
-__device__ void gravity_jacobi(const wh::System<NB>& s, double ax[NB], double ay[NB], double az[NB], double G,
-                               int N) {
-    double Rx = 0., Ry = 0., Rz = 0., M = 0.;
+__device__ __noinline__ void gravity_jacobi_lanes(const wh::System<NB>& s, double* ax, double* ay, double* az,
+                                     PairTerms<NB>& t, BodyTerms<NB>& b, int lane, double G, int N) {
+    if (lane < N && lane > 1) {
+        const int j = lane;
+        double Rx = 0., Ry = 0., Rz = 0., M = 0.;
 #pragma unroll 1
-    for (int j = 0; j < N; j++) {
-        ax[j] = 0.; ay[j] = 0.; az[j] = 0.;
-        const double xj = s.x[j], yj = s.y[j], zj = s.z[j], mj = s.m[j];
-        // the Jacobi vector of body j and its length do not depend on i
-        double Qx = 0., Qy = 0., Qz = 0., dr3 = 1.;
-        if (j > 1) {
-            Qx = xj - Rx / M; Qy = yj - Ry / M; Qz = zj - Rz / M;
-            const double dr = sqrt(Qx * Qx + Qy * Qy + Qz * Qz);
-            dr3 = dr * dr * dr;
+        for (int k = 0; k < j; k++) {
+            const double mk = s.m[k];
+            Rx += mk * s.x[k]; Ry += mk * s.y[k]; Rz += mk * s.z[k];
+            M += mk;
         }
-#pragma unroll 1
-        for (int i = 0; i <= j; i++) {
-            if (j > 1) {
-                const double dQ = i < j ? -mj : M;          // arranged so that m_j = 0 does not divide
-                const double pf = G * dQ / dr3;
-                ax[i] += pf * Qx; ay[i] += pf * Qy; az[i] += pf * Qz;
-            }
-            if (i != j && (i != 0 || j != 1)) {
-                const double dx = s.x[i] - xj, dy = s.y[i] - yj, dz = s.z[i] - zj;
-                const double dr = sqrt(dx * dx + dy * dy + dz * dz);
-                const double pf = G / (dr * dr * dr);
-                const double pfi = pf * s.m[i], pfj = pf * mj;
-                ax[i] -= pfj * dx; ay[i] -= pfj * dy; az[i] -= pfj * dz;
-                ax[j] += pfi * dx; ay[j] += pfi * dy; az[j] += pfi * dz;
-            }
-        }
-        Rx += mj * xj; Ry += mj * yj; Rz += mj * zj;
-        M += mj;
+        const double Qx = s.x[j] - Rx / M, Qy = s.y[j] - Ry / M, Qz = s.z[j] - Rz / M;
+        const double dr = sqrt(Qx * Qx + Qy * Qy + Qz * Qz);
+        const double dr3 = dr * dr * dr;
+        b.qx[j] = Qx; b.qy[j] = Qy; b.qz[j] = Qz;
+        b.fm[j] = G * (-s.m[j]) / dr3;
+        b.fM[j] = G * M / dr3;
     }
+    const int npair = N * (N - 1) / 2;
+#pragma unroll 1
+    for (int p0 = 0; p0 < npair; p0 += 32) {
+        const int p = p0 + lane;
+        if (p < npair && p > 0) {                   // pair 0 is (0, 1), skipped
+            int hi, lo;
+            pair_of(p, hi, lo);
+            const double dx = s.x[lo] - s.x[hi], dy = s.y[lo] - s.y[hi], dz = s.z[lo] - s.z[hi];
+            const double dr = sqrt(dx * dx + dy * dy + dz * dz);
+            t.dx[p] = dx; t.dy[p] = dy; t.dz[p] = dz;
+            t.pf[p] = G / (dr * dr * dr);
+        }
+    }
+    __syncwarp();
+    if (lane >= N) return;
+    const int k = lane;
+    double sx = 0., sy = 0., sz = 0.;
+#pragma unroll 1
+    for (int i = 0; i < k; i++) {                   // outer index k: partners below
+        if (i == 0 && k == 1) continue;
+        const int p = k * (k - 1) / 2 + i;
+        const double pfi = t.pf[p] * s.m[i];
+        sx += pfi * t.dx[p]; sy += pfi * t.dy[p]; sz += pfi * t.dz[p];
+    }
+    if (k > 1) {
+        const double pf = b.fM[k];
+        sx += pf * b.qx[k]; sy += pf * b.qy[k]; sz += pf * b.qz[k];
+    }
+#pragma unroll 1
+    for (int j = k + 1; j < N; j++) {               // outer index j > k
+        if (j > 1) {
+            const double pf = b.fm[j];
+            sx += pf * b.qx[j]; sy += pf * b.qy[j]; sz += pf * b.qz[j];
+        }
+        if (k == 0 && j == 1) continue;
+        const int p = j * (j - 1) / 2 + k;
+        const double pfj = t.pf[p] * s.m[j];
+        sx -= pfj * t.dx[p]; sy -= pfj * t.dy[p]; sz -= pfj * t.dz[p];
+    }
+    ax[k] = sx; ay[k] = sy; az[k] = sz;
 }
 
 // reb_integrator_whfast_calculate_jerk (src/integrator_whfast.c:786-870): the time
-// derivative of the JACOBI accelerations, then a += d * jerk (:1196-1203).
+// derivative of the JACOBI accelerations, then a += d * jerk (:1196-1203).  The
+// same order as gravity_jacobi_lanes, two updates per term.
 template <int NB>
-__device__ void add_jerk(const wh::System<NB>& s, double ax[NB], double ay[NB], double az[NB], double G, double d,
-                         int N) {
-    double jx[NB], jy[NB], jz[NB];
-    double Rx = 0., Ry = 0., Rz = 0., M = 0., Ax = 0., Ay = 0., Az = 0.;
+__device__ __noinline__ void add_jerk_lanes(const wh::System<NB>& s, double* ax, double* ay, double* az, PairTerms<NB>& t,
+                               BodyTerms<NB>& b, int lane, double G, double d, int N) {
+    if (lane < N && lane > 1) {
+        const int j = lane;
+        double Rx = 0., Ry = 0., Rz = 0., M = 0., Ax = 0., Ay = 0., Az = 0.;
 #pragma unroll 1
-    for (int j = 0; j < N; j++) {
-        jx[j] = 0.; jy[j] = 0.; jz[j] = 0.;
-        const double xj = s.x[j], yj = s.y[j], zj = s.z[j], mj = s.m[j];
-        const double axj = ax[j], ayj = ay[j], azj = az[j];
-        double Qx = 0., Qy = 0., Qz = 0., dax = 0., day = 0., daz = 0., dr = 1.;
+        for (int k = 0; k < j; k++) {
+            const double mk = s.m[k];
+            Ax += ax[k] * mk; Ay += ay[k] * mk; Az += az[k] * mk;
+            Rx += s.x[k] * mk; Ry += s.y[k] * mk; Rz += s.z[k] * mk;
+            M += mk;
+        }
+        const double Qx = s.x[j] - Rx / M, Qy = s.y[j] - Ry / M, Qz = s.z[j] - Rz / M;
+        const double dax = ax[j] - Ax / M, day = ay[j] - Ay / M, daz = az[j] - Az / M;
+        const double dr = sqrt(Qx * Qx + Qy * Qy + Qz * Qz);
+        const double alpha = dax * Qx + day * Qy + daz * Qz;
+        b.qx[j] = Qx; b.qy[j] = Qy; b.qz[j] = Qz;
+        b.ex[j] = dax; b.ey[j] = day; b.ez[j] = daz;
+        const double fm = G * (-s.m[j]) / (dr * dr * dr);
+        const double fM = G * M / (dr * dr * dr);
+        b.fm[j] = fm;
+        b.fM[j] = fM;
+        b.f1m[j] = 3. * alpha * fm / (dr * dr);
+        b.f1M[j] = 3. * alpha * fM / (dr * dr);
+    }
+    const int npair = N * (N - 1) / 2;
+#pragma unroll 1
+    for (int p0 = 0; p0 < npair; p0 += 32) {
+        const int p = p0 + lane;
+        if (p < npair && p > 0) {                   // pair 0 is (0, 1), skipped
+            int hi, lo;
+            pair_of(p, hi, lo);
+            const double dx = s.x[hi] - s.x[lo], dy = s.y[hi] - s.y[lo], dz = s.z[hi] - s.z[lo];
+            const double ddx = ax[hi] - ax[lo], ddy = ay[hi] - ay[lo], ddz = az[hi] - az[lo];
+            const double r = sqrt(dx * dx + dy * dy + dz * dz);
+            const double alpha = ddx * dx + ddy * dy + ddz * dz;
+            const double pf2 = G / (r * r * r);
+            t.dx[p] = dx; t.dy[p] = dy; t.dz[p] = dz;
+            t.ex[p] = ddx; t.ey[p] = ddy; t.ez[p] = ddz;
+            t.pf[p] = pf2;
+            t.pf1[p] = 3. * alpha * pf2 / (r * r);
+        }
+    }
+    __syncwarp();
+    const int k = lane < N ? lane : 0;             // lanes beyond N repeat body 0 and write nothing
+    double jx = 0., jy = 0., jz = 0.;
+#pragma unroll 1
+    for (int i = 0; i < k; i++) {                   // outer index k: partners below
+        if (i == 0 && k == 1) continue;
+        const int p = k * (k - 1) / 2 + i;
+        const double pf2i = t.pf[p] * s.m[i];
+        jx -= t.ex[p] * pf2i; jy -= t.ey[p] * pf2i; jz -= t.ez[p] * pf2i;
+        const double pf1i = t.pf1[p] * s.m[i];
+        jx += t.dx[p] * pf1i; jy += t.dy[p] * pf1i; jz += t.dz[p] * pf1i;
+    }
+    if (k > 1) {
+        const double pf2 = b.fM[k], pf1 = b.f1M[k];
+        jx += pf2 * b.ex[k]; jy += pf2 * b.ey[k]; jz += pf2 * b.ez[k];
+        jx -= pf1 * b.qx[k]; jy -= pf1 * b.qy[k]; jz -= pf1 * b.qz[k];
+    }
+#pragma unroll 1
+    for (int j = k + 1; j < N; j++) {               // outer index j > k
         if (j > 1) {
-            Qx = xj - Rx / M; Qy = yj - Ry / M; Qz = zj - Rz / M;
-            dax = axj - Ax / M; day = ayj - Ay / M; daz = azj - Az / M;
-            dr = sqrt(Qx * Qx + Qy * Qy + Qz * Qz);
+            const double pf2 = b.fm[j], pf1 = b.f1m[j];
+            jx += pf2 * b.ex[j]; jy += pf2 * b.ey[j]; jz += pf2 * b.ez[j];
+            jx -= pf1 * b.qx[j]; jy -= pf1 * b.qy[j]; jz -= pf1 * b.qz[j];
         }
-#pragma unroll 1
-        for (int i = 0; i <= j; i++) {
-            if (j > 1) {
-                const double dQ = i < j ? -mj : M;
-                const double pf2 = G * dQ / (dr * dr * dr);
-                jx[i] += pf2 * dax; jy[i] += pf2 * day; jz[i] += pf2 * daz;
-                const double alpha = dax * Qx + day * Qy + daz * Qz;
-                const double pf1 = 3. * alpha * pf2 / (dr * dr);
-                jx[i] -= pf1 * Qx; jy[i] -= pf1 * Qy; jz[i] -= pf1 * Qz;
-            }
-            if (j != i && (i != 0 || j != 1)) {
-                const double dx = xj - s.x[i], dy = yj - s.y[i], dz = zj - s.z[i];
-                const double ddx = axj - ax[i], ddy = ayj - ay[i], ddz = azj - az[i];
-                const double r = sqrt(dx * dx + dy * dy + dz * dz);
-                const double alpha = ddx * dx + ddy * dy + ddz * dz;
-                const double pf2 = G / (r * r * r);
-                const double pf2i = pf2 * s.m[i], pf2j = pf2 * mj;
-                jx[j] -= ddx * pf2i; jy[j] -= ddy * pf2i; jz[j] -= ddz * pf2i;
-                jx[i] += ddx * pf2j; jy[i] += ddy * pf2j; jz[i] += ddz * pf2j;
-                const double pf1 = 3. * alpha * pf2 / (r * r);
-                const double pf1i = pf1 * s.m[i], pf1j = pf1 * mj;
-                jx[j] += dx * pf1i; jy[j] += dy * pf1i; jz[j] += dz * pf1i;
-                jx[i] -= dx * pf1j; jy[i] -= dy * pf1j; jz[i] -= dz * pf1j;
-            }
-        }
-        Ax += axj * mj; Ay += ayj * mj; Az += azj * mj;
-        Rx += xj * mj; Ry += yj * mj; Rz += zj * mj;
-        M += mj;
+        if (k == 0 && j == 1) continue;
+        const int p = j * (j - 1) / 2 + k;
+        const double pf2j = t.pf[p] * s.m[j];
+        jx += t.ex[p] * pf2j; jy += t.ey[p] * pf2j; jz += t.ez[p] * pf2j;
+        const double pf1j = t.pf1[p] * s.m[j];
+        jx -= t.dx[p] * pf1j; jy -= t.dy[p] * pf1j; jz -= t.dz[p] * pf1j;
     }
-#pragma unroll 1
-    for (int i = 0; i < N; i++) {
-        ax[i] += d * jx[i]; ay[i] += d * jy[i]; az[i] += d * jz[i];
-    }
+    __syncwarp();                                   // every lane has read the accelerations
+    if (lane < N) { ax[k] += d * jx; ay[k] += d * jy; az[k] += d * jz; }
 }
 
 // --- coordinate systems other than Jacobi (src/transformations.c:295-644) ---------
@@ -399,11 +491,6 @@ __device__ void kick_helio_lanes(wh::Jacobi<NB>& h, const wh::System<NB>& s, con
 // and divisions up to N = 8.  The state and the accelerations are in shared memory;
 // the caller brackets the call with __syncwarp().
 template <int NB>
-struct PairTerms {
-    double dx[NB * (NB - 1) / 2], dy[NB * (NB - 1) / 2], dz[NB * (NB - 1) / 2], pf[NB * (NB - 1) / 2];
-};
-
-template <int NB>
 __device__ void gravity_basic_lanes(const wh::System<NB>& s, double* ax, double* ay, double* az, PairTerms<NB>& t,
                                     int lane, double G, double eps2, int N, int Ng, int tp, int starti, int startj) {
     const int npair = N * (N - 1) / 2;
@@ -411,9 +498,8 @@ __device__ void gravity_basic_lanes(const wh::System<NB>& s, double* ax, double*
     for (int p0 = 0; p0 < npair; p0 += 32) {
         const int p = p0 + lane;
         if (p < npair) {
-            int i = 1;
-            while ((i + 1) * i / 2 <= p) i++;
-            const int jj = p - i * (i - 1) / 2;
+            int i, jj;
+            pair_of(p, i, jj);
             const double dx = (0. + s.x[i]) - s.x[jj];
             const double dy = (0. + s.y[i]) - s.y[jj];
             const double dz = (0. + s.z[i]) - s.z[jj];
@@ -625,47 +711,75 @@ __device__ __forceinline__ void kahan_add(double& a, double& c, double inc) {
 
 // reb_gravity_compensated_calculate_acceleration, serial branch (src/gravity.c:
 // 284-297, 415-531): pairs i < j among the active bodies, then test particles,
-// each term added with a Kahan correction; ign = gravity_ignore_terms.
+// each term added with a Kahan correction; ign = gravity_ignore_terms.  Over the
+// lanes: an active body takes its active partners' terms in ascending order and then,
+// with testparticle_type 1, the test particles' in ascending order; a test particle
+// takes the active bodies' in ascending order.  Each pair's displacement (outer index
+// minus inner: lower minus higher between active bodies, test particle minus active
+// body) and G / (r^2 r) are formed once, one pair per lane.
 template <int NB>
-__device__ void gravity_compensated(const wh::System<NB>& s, double ax[NB], double ay[NB], double az[NB], double G,
-                                    double eps2, int N, int Ng, int tp, int ign) {
-    double cx[NB], cy[NB], cz[NB];
+__device__ __noinline__ void gravity_compensated_lanes(const wh::System<NB>& s, double* ax, double* ay, double* az,
+                                          PairTerms<NB>& t, int lane, double G, double eps2, int N, int Ng,
+                                          int tp, int ign) {
+    const int npair = N * (N - 1) / 2;
 #pragma unroll 1
-    for (int i = 0; i < N; i++) { ax[i] = 0.; ay[i] = 0.; az[i] = 0.; cx[i] = 0.; cy[i] = 0.; cz[i] = 0.; }
-#pragma unroll 1
-    for (int i = 0; i < N; i++) {
-        const bool active = i < Ng;
-#pragma unroll 1
-        for (int j = active ? i + 1 : 0; j < Ng; j++) {
-            if (ign == 1 && ((j == 1 && i == 0) || (i == 1 && j == 0))) continue;
-            if (ign == 2 && (j == 0 || i == 0)) continue;
-            const double dx = s.x[i] - s.x[j], dy = s.y[i] - s.y[j], dz = s.z[i] - s.z[j];
-            const double r2 = dx * dx + dy * dy + dz * dz + eps2;
-            const double r = sqrt(r2);
-            const double pf = G / (r2 * r);
-            const double pfj = -pf * s.m[j];
-            kahan_add(ax[i], cx[i], pfj * dx); kahan_add(ay[i], cy[i], pfj * dy); kahan_add(az[i], cz[i], pfj * dz);
-            if (active || tp) {
-                const double pfi = pf * s.m[i];
-                kahan_add(ax[j], cx[j], pfi * dx); kahan_add(ay[j], cy[j], pfi * dy); kahan_add(az[j], cz[j], pfi * dz);
+    for (int p0 = 0; p0 < npair; p0 += 32) {
+        const int p = p0 + lane;
+        if (p < npair) {
+            int hi, lo;
+            pair_of(p, hi, lo);
+            if (lo < Ng) {                          // pairs of two test particles do not interact
+                const int i = hi < Ng ? lo : hi, j = hi < Ng ? hi : lo;
+                const double dx = s.x[i] - s.x[j], dy = s.y[i] - s.y[j], dz = s.z[i] - s.z[j];
+                const double r2 = dx * dx + dy * dy + dz * dz + eps2;
+                const double r = sqrt(r2);
+                t.dx[p] = dx; t.dy[p] = dy; t.dz[p] = dz;
+                t.pf[p] = G / (r2 * r);
             }
         }
     }
+    __syncwarp();
+    if (lane >= N) return;
+    const int k = lane;
+    const bool active = k < Ng;
+    double sx = 0., sy = 0., sz = 0., cx = 0., cy = 0., cz = 0.;
+#pragma unroll 1
+    for (int q = 0; q < N; q++) {
+        if (q == k) continue;
+        if (ign == 1 && ((k == 0 && q == 1) || (k == 1 && q == 0))) continue;
+        if (ign == 2 && (k == 0 || q == 0)) continue;
+        const int hi = q > k ? q : k, lo = q > k ? k : q;
+        const int p = hi * (hi - 1) / 2 + lo;
+        double c;                                   // the term's factor (pfj or pfi of the serial loop)
+        if (active && q < Ng) {
+            c = q > k ? -t.pf[p] * s.m[q] : t.pf[p] * s.m[q];   // k is the outer index when q > k
+        } else if (active) {
+            if (!tp) continue;                      // test particle q kicks k only with testparticle_type 1
+            c = t.pf[p] * s.m[q];
+        } else {
+            if (q >= Ng) continue;
+            c = -t.pf[p] * s.m[q];
+        }
+        kahan_add(sx, cx, c * t.dx[p]); kahan_add(sy, cy, c * t.dy[p]); kahan_add(sz, cz, c * t.dz[p]);
+    }
+    ax[k] = sx; ay[k] = sy; az[k] = sz;
 }
 
 template <int NB>
 __global__ void __launch_bounds__(32) whfast_program(ParticlesSoA p, double* jac, size_t cap, int N, int Na, int Ng,
                                                      int tp, int coords, double G, double eps2,
                                                      const __grid_constant__ Program prog, uint32_t* status) {
-    // Every lane walks the program; the drifts (one body each), the BASIC gravity
-    // (one pair, then one body each), the coordinate transforms, jumps and kicks
-    // (one quantity or one body each) run on the lanes, the other operators on
-    // lane 0.  The state lives in shared memory so that all lanes see it.
+    // Every lane walks the program; the drifts (one body each), the forces (one
+    // pair, then one body each), the coordinate transforms, jumps and kicks (one
+    // quantity or one body each) run on the lanes, the centre-of-mass drift, the
+    // zero force and the lazy shift on lane 0.  The state lives in shared memory so
+    // that all lanes see it.
     __shared__ wh::Jacobi<NB> j;
     __shared__ wh::System<NB> s;
     __shared__ double acc[3][NB];
     __shared__ ChainScalars<NB> chain;
     __shared__ PairTerms<NB> pairs;
+    __shared__ BodyTerms<NB> bodies;
     __shared__ int stop;
     const int lane = threadIdx.x;
     double* const ax = acc[0];
@@ -695,8 +809,17 @@ __global__ void __launch_bounds__(32) whfast_program(ParticlesSoA p, double* jac
             __syncwarp();
             continue;
         }
-        if (op == kOpGravity) {
-            gravity_basic_lanes(s, ax, ay, az, pairs, lane, G, eps2, N, Ng, tp, starti, startj);
+        if (op == kOpGravity || op == kOpGravityJacobi || op == kOpGravityCompensated || op == kOpJerk) {
+            if (op == kOpGravity) {
+                gravity_basic_lanes(s, ax, ay, az, pairs, lane, G, eps2, N, Ng, tp, starti, startj);
+            } else if (op == kOpGravityJacobi) {
+                gravity_jacobi_lanes(s, ax, ay, az, pairs, bodies, lane, G, N);
+            } else if (op == kOpGravityCompensated) {
+                gravity_compensated_lanes(s, ax, ay, az, pairs, lane, G, eps2, N, Ng, tp,
+                                          coords == 0 ? 1 : coords == 3 ? 0 : 2);
+            } else {
+                add_jerk_lanes(s, ax, ay, az, pairs, bodies, lane, G, d, N);
+            }
             __syncwarp();
             continue;
         }
@@ -726,15 +849,10 @@ __global__ void __launch_bounds__(32) whfast_program(ParticlesSoA p, double* jac
         if (lane == 0) {
             switch (op) {
                 case kOpCom: wh::com_step(j, d); break;
-                case kOpGravityJacobi: gravity_jacobi(s, ax, ay, az, G, N); break;
-                case kOpGravityCompensated:
-                    gravity_compensated(s, ax, ay, az, G, eps2, N, Ng, tp, coords == 0 ? 1 : coords == 3 ? 0 : 2);
-                    break;
                 case kOpGravityNone:
 #pragma unroll 1
                     for (int i = 0; i < N; i++) { ax[i] = 0.; ay[i] = 0.; az[i] = 0.; }
                     break;
-                case kOpJerk: add_jerk(s, ax, ay, az, G, d, N); break;
                 case kOpLazyShift:
 #pragma unroll 1
                     for (int i = 1; i < N; i++) {
