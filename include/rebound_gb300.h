@@ -339,8 +339,11 @@ int  rgpu_ensemble_times(rgpu_ensemble* ens, double* t);
 
 /* ---- serving: continuous batching of integrate requests --------------- */
 /* A request is one system the reference would run as one reb_simulation:
- * RGPU_SERVE_WHFAST: 2..16 bodies, WHFast (Jacobi, DEFAULT kernel, safe_mode 1),
- *   G = 1, no softening;
+ * RGPU_SERVE_WHFAST: 2..16 bodies, WHFast (Jacobi, DEFAULT kernel), G = 1, no
+ *   softening; one warp per system steps it in blocks of 32 steps, counted from
+ *   its last step back, that merge the drifts of consecutive steps as the
+ *   reference's safe_mode 0 does and end synchronised (the same map as
+ *   safe_mode 1 to rounding); thread_per_system = 1 runs safe_mode 1 step by step;
  * RGPU_SERVE_CLUSTER: any N up to the pool, leapfrog (order 2) with the
  *   mixed-precision direct sum (RGPU_GRAVITY_MIXED_SPLIT), softening given.
  * A worker thread admits queued requests FIFO while the device bytes of the
@@ -352,7 +355,8 @@ int  rgpu_ensemble_times(rgpu_ensemble* ens, double* t);
 enum { RGPU_SERVE_WHFAST = 1, RGPU_SERVE_CLUSTER = 2 };
 typedef struct rgpu_server_config {
     size_t hbm_budget_bytes;         /* default 120 GiB */
-    int64_t steps_per_launch;        /* WHFast steps per slot per tick when tick_ns is 0 or
+    int64_t steps_per_launch;        /* WHFast steps per slot per tick when tick_ns is 0 (warp
+                                        slots extend it to the end of a 32-step block) or
                                         thread_per_system is 1 (default 64) */
     int32_t slots_per_bucket;        /* WHFast slots per body count (default 16,384) */
     int32_t pool_particles;          /* cluster particle pool (default 4,194,304) */

@@ -9,9 +9,11 @@
 //    slots in per-body-count buckets, warp per slot (thread per slot on
 //    request); each tick, every live warp steps its slot until a device-time
 //    budget (tick_ns) has passed, so a tick lasts about the budget and no light
-//    system waits for the heaviest one (or, with tick_ns = 0 and on the thread
-//    path, min(chunk, remaining) steps); FMA contraction and the FP64-refined
-//    division and square root (WH_FAST_MATH);
+//    system waits for the heaviest one (or, with tick_ns = 0, chunk steps
+//    extended to a block end; on the thread path min(chunk, remaining) steps).
+//    Warp slots merge the drifts of consecutive steps within 32-step blocks
+//    (safe_mode 0 inside a block, synchronised at its end); FMA contraction and
+//    the FP64-refined division and square root (WH_FAST_MATH);
 //  * Plummer clusters with leapfrog (src/integrator_leapfrog.c) and the
 //    mixed-precision direct sum (FP64 displacement formed from two-float
 //    splits, FP32 force, compensated FP32 accumulation): particles in a pooled
@@ -70,8 +72,16 @@ __global__ void __launch_bounds__(128) wh_slots_kernel(double* __restrict__ st, 
 }
 
 // --- warp per system (whfast_warp.cuh) -------------------------------------------
-// Advance WHFast slot `sid` of one bucket by up to `chunk` steps, and with
-// budget_ns > 0 only for about that much device time; called by a whole warp.
+// A request's steps run in blocks of kServeBlock steps, counted from its last step
+// back (the first block takes the remainder): within a block the drifts of
+// consecutive steps merge as with the reference's safe_mode = 0, and each block ends
+// synchronised.  A slot stops only at a block end or at the request's end, so the
+// blocks, and the results, depend on the request alone, not on ticks or budgets.
+constexpr int kServeBlock = 32;
+
+// Advance WHFast slot `sid` of one bucket by `chunk` steps extended to the next
+// block end, and with budget_ns > 0 only for about that much device time; called by
+// a whole warp.
 template <int NB>
 __device__ __noinline__ void warp_advance(double* __restrict__ st, const double* __restrict__ dt,
                                           int64_t* __restrict__ remaining, int cap, int sid, int chunk, double G,
@@ -79,8 +89,13 @@ __device__ __noinline__ void warp_advance(double* __restrict__ st, const double*
     const int lane = (int)(threadIdx.x & 31);
     const int64_t rem = remaining[sid];
     if (rem <= 0) return;
-    const int nsteps = (int)(rem < chunk ? rem : chunk);
-    const int done = whw::warp_steps<NB>(st, cap, sid, nsteps, dt[sid], G, status, budget_ns);
+    int64_t n = rem < chunk ? rem : chunk;
+    if (n < rem) {
+        n = rem - (rem - n) / kServeBlock * kServeBlock;     // extend to a block end
+        if (n > INT32_MAX) n -= kServeBlock;                  // still a block end
+    }
+    const int first = (int)(rem % kServeBlock);
+    const int done = whw::warp_steps<NB>(st, cap, sid, (int)n, dt[sid], G, status, budget_ns, kServeBlock, first);
     if (lane == 0) remaining[sid] = rem - done;
 }
 

@@ -80,13 +80,22 @@ __device__ __forceinline__ unsigned long long global_ns() {
 }
 
 // Advance one system of a [field][body][system] table (`cap` systems per field
-// row) by up to `nsteps` steps of length h; called by a whole warp.  With
-// budget_ns > 0 the warp also stops after the first step that ends budget_ns
-// or more after it started (lane 0's clock decides for the whole warp).
-// Returns the steps taken.
+// row) by up to `nsteps` steps of length h; called by a whole warp.
+// The steps run in blocks of `block` steps, the first one `first` steps long
+// when first > 0, and the call's last step always closes a block.  Within a block
+// the system stays in Jacobi coordinates and the closing half drift of one step
+// and the opening half drift of the next are one Kepler drift over h, as the
+// reference's WHFast does with safe_mode = 0 (src/integrator_whfast.c:1113-1259);
+// each block ends synchronised (inertial positions and velocities), as every
+// safe_mode = 1 step does.  The two splittings are the same map and differ by
+// rounding; block = 1 is the reference's default.  With budget_ns > 0 the warp
+// also stops after the first block that ends budget_ns or more after it started
+// (lane 0's clock decides for the whole warp), so the blocks do not depend on the
+// budget.  Returns the steps taken.
 template <int NB>
 __device__ __forceinline__ int warp_steps(double* __restrict__ st, int cap, int sid, int nsteps, double h, double G,
-                                          uint32_t* status, long long budget_ns = 0) {
+                                          uint32_t* status, long long budget_ns = 0, int block = 1,
+                                          int first = 0) {
     const int lane = (int)(threadIdx.x & 31);
     const size_t f = (size_t)NB * cap;
     const bool on = lane < NB;
@@ -126,9 +135,14 @@ __device__ __forceinline__ int warp_steps(double* __restrict__ st, int cap, int 
     }
     const unsigned long long t_start = budget_ns > 0 ? global_ns() : 0ull;
     int done = 0;
+    double qx = 0., qy = 0., qz = 0., ux = 0., uy = 0., uz = 0.;
+    int left = first > 0 ? first : block;          // steps left in the current block
+    bool opens = true;                             // this step opens a block
     for (int k = 0; k < nsteps; k++) {
+        left--;
+        const bool closes = left <= 0 || k + 1 == nsteps;
+        if (opens) {
         // inertial -> Jacobi (lane 0: centre of mass)
-        double qx, qy, qz, ux, uy, uz;
         {
             double P[6] = {m * x, m * y, m * z, m * vx, m * vy, m * vz};
             lane_scan_multi<NB, 6, false>(P, lane);
@@ -151,6 +165,7 @@ __device__ __forceinline__ int warp_steps(double* __restrict__ st, int cap, int 
         // drift dt/2: Kepler per Jacobi body, free drift of the centre of mass
         if (jac) wh::kepler_solver(qx, qy, qz, ux, uy, uz, mu, h2, status);
         else if (lane == 0) { qx += h2 * ux; qy += h2 * uy; qz += h2 * uz; }
+        }
         // Jacobi -> inertial positions
         {
             const double Xc = __shfl_sync(kFull, qx, 0), Yc = __shfl_sync(kFull, qy, 0), Zc = __shfl_sync(kFull, qz, 0);
@@ -210,6 +225,14 @@ __device__ __forceinline__ int warp_steps(double* __restrict__ st, int cap, int 
                 }
             }
         }
+        opens = closes;
+        if (!closes) {
+            // this step's closing half drift and the next step's opening one
+            if (jac) wh::kepler_solver(qx, qy, qz, ux, uy, uz, mu, h, status);
+            else if (lane == 0) { qx += h * ux; qy += h * uy; qz += h * uz; }
+            continue;
+        }
+        left = block;
         // drift dt/2
         if (jac) wh::kepler_solver(qx, qy, qz, ux, uy, uz, mu, h2, status);
         else if (lane == 0) { qx += h2 * ux; qy += h2 * uy; qz += h2 * uz; }
