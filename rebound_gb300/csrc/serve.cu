@@ -213,8 +213,6 @@ __global__ void cl_split(Pool p, const ClusterItem* __restrict__ items, int k) {
     p.split[2 * q + 1] = make_float4((float)(x - (double)xh), (float)(y - (double)yh), (float)(z - (double)zh), 0.f);
 }
 
-// Mixed-precision direct sum of one cluster tile: the FP64 displacement from the
-// two-float split (exact when it cancels), FP32 force, Kahan FP32 accumulation.
 // Mixed-precision force of one cluster tile (the MIXED_SPLIT form of the direct
 // sum): two-float displacements and FP32 G m / r^3 on the packed FP32x2 pipe, two
 // j-bodies per instruction, FP32 sums over 32 j-pairs folded into a compensated
